@@ -1,0 +1,131 @@
+/*
+ * unomol_gb300 -- C ABI of the GB300 (sm_103a) direct two-electron Fock build.
+ *
+ * This is the drop-in boundary for unomol's TwoElectronInts class (TwoElectronInts.hpp:79-110).
+ * The reference computes every unique integral once in its constructor, stores them in a cache and
+ * streams the cache on every formGmatrix call.  Here the constructor uploads the basis and builds
+ * shell pairs and Schwarz bounds on the GPU; every formGmatrix call recomputes the integrals on the
+ * GPU and contracts them directly into G (direct SCF: no integral store).
+ *
+ * Conventions (identical to the reference):
+ *   - packed lower triangle, row major: element (i, j), j <= i, at i*(i+1)/2 + j, N*(N+1)/2 doubles;
+ *   - AO order = shell order of the basis; Cartesian components of a shell ordered lx descending,
+ *     then ly descending (AuxFunctions.hpp:35-43);
+ *   - centres in bohr; contraction coefficients already normalised as Basis::normalize leaves them
+ *     (Basis.hpp:56-75);
+ *   - P is the reference's RHF density C_occ C_occ^T (RHF.hpp:192-203), G = 2 J(P) - K(P);
+ *     UHF: Ga = J(Pa + Pb) - K(Pa), Gb = J(Pa + Pb) - K(Pb) (TwoElectronInts.cpp:749-820);
+ *   - formGmatrix ADDS into the caller's G (the callers zero it first: RHF.hpp:89-90, UHF.hpp:103-107).
+ *
+ * Every entry point returns 0 on success and a negative UNOMOL_E* code on failure; the message is
+ * available from unomol_gpu_last_error().  There is no CPU fallback: without a usable GPU the calls
+ * fail with UNOMOL_ENODEV.
+ */
+#ifndef UNOMOL_GB300_H
+#define UNOMOL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UNOMOL_OK 0
+#define UNOMOL_EINVAL (-1)   /* bad argument (sizes, L > supported, null pointers) */
+#define UNOMOL_ENODEV (-2)   /* no CUDA device / driver */
+#define UNOMOL_ECUDA (-3)    /* a CUDA runtime or library call failed */
+#define UNOMOL_ENOMEM (-4)   /* device allocation failed */
+#define UNOMOL_ETIMEOUT (-5) /* a bounded device wait gave up */
+#define UNOMOL_ESCF (-6)     /* SCF driver: singular overlap, eigen-solver failure */
+
+/* Precision modes (unomol_gpu_set_precision). */
+#define UNOMOL_PREC_FP64 0  /* every quartet in FP64 (the plain path; the default) */
+#define UNOMOL_PREC_MIXED 1 /* quartets with Schwarz bound * max|P| below the cutoff in FP32 */
+
+/* Flat description of a basis (the data of unomol::Basis, Basis.hpp:157-170). */
+typedef struct UnomolBasisDesc {
+    int nshell;               /* number of shells */
+    int norb;                 /* number of basis functions (sum of (L+1)(L+2)/2) */
+    int ncen;                 /* number of centres */
+    const int* shell_l;       /* [nshell] angular momentum, 0..4 */
+    const int* shell_nprim;   /* [nshell] primitives per shell */
+    const int* shell_center;  /* [nshell] centre index */
+    const int* shell_offset;  /* [nshell] first AO of the shell (Basis::offset, Basis.hpp:226-232) */
+    const double* alpha;      /* [sum nprim] exponents, shell after shell */
+    const double* coef;       /* [sum nprim] normalised contraction coefficients */
+    const double* centers;    /* [ncen*3] positions in bohr */
+} UnomolBasisDesc;
+
+typedef struct UnomolCtx UnomolCtx;
+
+/* Counters of the last Fock build (for throughput figures). */
+typedef struct UnomolStats {
+    int64_t shell_quartets;        /* unique shell quartets after Schwarz screening */
+    int64_t shell_quartets_fp32;   /* of which evaluated in FP32 (mixed mode) */
+    int64_t shell_quartets_total;  /* unique shell quartets before screening */
+    int64_t function_quartets;     /* unique function quartets after screening (canonical count) */
+    int64_t primitive_quartets;    /* primitive quartets after Schwarz screening (before the 1e-12 cut) */
+    double ms_eri;                 /* device time of the last build's ERI + J/K kernels */
+    double ms_total;               /* device time of the last build (including P expand / G fold) */
+    int nbf;                       /* basis functions */
+    int npairs;                    /* shell pairs kept */
+    int kernel_launches;           /* kernels launched by the last build */
+} UnomolStats;
+
+/* TwoElectronInts(basis, start_shell, label) -- TwoElectronInts.hpp:83-88.
+ * Uploads the basis, builds shell pairs, Schwarz bounds and the class work lists on device 0 (or
+ * the current device).  start_shell: only quartets whose largest shell index is >= start_shell
+ * contribute (TwoElectronInts.cpp:541; used by the DPM path, RHF.hpp:315). */
+int unomol_gpu_create(const UnomolBasisDesc* basis, int start_shell, UnomolCtx** out);
+
+/* TwoElectronInts::recalculate(basis) -- TwoElectronInts.hpp:94-96 (centre moved: RHF.hpp:354).
+ * centers: [ncen*3] new positions in bohr; shells and exponents are unchanged. */
+int unomol_gpu_recalculate(UnomolCtx* ctx, const double* centers);
+
+/* TwoElectronInts::formGmatrix(P, G) -- TwoElectronInts.cpp:822-844.  Host pointers, packed. */
+int unomol_gpu_fock_rhf(UnomolCtx* ctx, const double* P, double* G);
+
+/* TwoElectronInts::formGmatrix(Pa, Pb, Ga, Gb) -- TwoElectronInts.cpp:846-869.  Host pointers. */
+int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, double* Ga, double* Gb);
+
+/* Device-resident variants of the two calls above: all pointers are device pointers (packed),
+ * `stream` is a cudaStream_t (NULL = the context's own stream).  G is added into, as above. */
+int unomol_gpu_fock_rhf_device(UnomolCtx* ctx, const double* dP, double* dG, void* stream);
+int unomol_gpu_fock_uhf_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa,
+                               double* dGb, void* stream);
+
+/* Precision form: UNOMOL_PREC_FP64 (default) or UNOMOL_PREC_MIXED with the FP32 cutoff on
+ * (Schwarz bound of the quartet) x (max |P| over the quartet's density blocks).  No reference
+ * counterpart (the reference is FP64 only). */
+int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cutoff);
+
+/* Rys quadrature of the two-root classes (unomol_gpu_set_rys_mode).
+ * UNOMOL_RYS_REFERENCE (default): for 15 < T <= 40 the two-root nodes and weights follow the
+ *   reference's own fit (Rys::root2, Rys.cpp:611-623), which departs from the exact quadrature by up
+ *   to 3.5e-4 relative at T = 15; G and energies then match the reference's.
+ * UNOMOL_RYS_EXACT: exact quadrature at every T (all other root counts are exact in both modes;
+ *   the reference's root1 and root3..5 agree with exact quadrature to ~1e-13). */
+#define UNOMOL_RYS_REFERENCE 0
+#define UNOMOL_RYS_EXACT 1
+int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode);
+
+/* Schwarz cutoff on sqrt((ab|ab)) sqrt((cd|cd)).  Default 1e-14: the reference drops stored
+ * integrals with |v| <= 1e-14 (TwoElectronInts.cpp:668), so quartets whose bound is below that
+ * contribute nothing there either.  Rebuilds the work lists. */
+int unomol_gpu_set_screening(UnomolCtx* ctx, double schwarz_cutoff);
+
+int unomol_gpu_get_stats(const UnomolCtx* ctx, UnomolStats* out);
+
+void unomol_gpu_destroy(UnomolCtx* ctx);
+
+/* Last error of this context (ctx may be NULL for errors raised before a context existed). */
+const char* unomol_gpu_last_error(const UnomolCtx* ctx);
+
+/* Library version string. */
+const char* unomol_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UNOMOL_GB300_H */

@@ -1,0 +1,136 @@
+"""Generates the golden fixtures in this folder from the reference itself (oracle/_ref, built from the
+reference sources by oracle/Makefile).  Run in a container that has the reference tree:
+
+    make -C oracle && python tests/golden/make_golden.py [--big]
+
+Per case (<name>.npz):
+  patin            the input text (patin.dat format)
+  S, T, H          one-electron matrices (OneElectronInts.cpp), packed
+  P_rand, G_rand   a seeded random symmetric density and the reference's G(P) (TwoElectronInts.cpp:822-844)
+  Pa, Pb, Ga, Gb   seeded random alpha/beta densities and the reference's UHF G (TwoElectronInts.cpp:846-869)
+  n_stored         number of integral records the reference stored (|v| > 1e-14)
+  scf_*            (SCF cases) final / initial energy, iterations and final P of the stock SCF
+  golden_energy    (reference test inputs) the published energy of test/scfout.dat.*
+  ints_*           (small cases) the reference's stored integral records (val, i, j, k, l)
+
+--big adds the n-decane 6-31G RHF/UHF-cation G(P) fixtures (about 15 s of reference integral pass)
+and the 32-water 6-31G G(P) fixture (about 10 minutes).
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+
+import refh  # noqa: E402
+
+from unomol_gb300 import molecules  # noqa: E402
+
+REF = "/root/reference"
+
+
+def rand_density(n: int, seed: int, scale: float = 0.3) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    m = rng.uniform(-scale, scale, (n, n))
+    m = 0.5 * (m + m.T) + np.diag(rng.uniform(0.0, 1.0, n))
+    return np.ascontiguousarray(m[np.tril_indices(n)])
+
+
+def make_case(name: str, patin: str, scf: bool, golden_energy: float | None, dump_ints: bool, md: bool = False):
+    path = os.path.join(HERE, f"_{name}.patin")
+    with open(path, "w") as f:
+        f.write(patin)
+    b = refh.RefBasis(path, md)
+    S, T, H = b.one_electron()
+    t = refh.RefTwoElectronInts(b)
+    n = b.norb
+    out = {"patin": np.array(patin), "S": S, "T": T, "H": H}
+    seed = abs(hash(name)) % (2 ** 31)
+    seed = sum(ord(c) * 131 ** i for i, c in enumerate(name)) % (2 ** 31)
+    P = rand_density(n, seed)
+    out["P_rand"], out["G_rand"] = P, t.form_g(P)
+    Pa, Pb = rand_density(n, seed + 1), rand_density(n, seed + 2)
+    Ga, Gb = t.form_g_uhf(Pa, Pb)
+    out.update(Pa=Pa, Pb=Pb, Ga=Ga, Gb=Gb)
+    vals, ijkl = t.records()
+    out["n_stored"] = np.array(len(vals))
+    if dump_ints:
+        out["ints_val"], out["ints_ijkl"] = vals, ijkl
+    del t
+    if not md:
+        # the same reference with its two-root Rys fit replaced by exact quadrature
+        be = refh.RefBasis(path, "exact")
+        te = refh.RefTwoElectronInts(be)
+        out["G_rand_exact"] = te.form_g(P)
+        out["Ga_exact"], out["Gb_exact"] = te.form_g_uhf(Pa, Pb)
+        del te
+    if scf:
+        r = refh.run_scf(path, md)
+        out.update(scf_energy=np.array(r["energy"]), scf_init_energy=np.array(r["init_energy"]),
+                   scf_iterations=np.array(r["iterations"]), scf_P=r["P"], scf_nucrep=np.array(r["nucrep"]))
+        if not md:
+            re = refh.run_scf(path, "exact")
+            out.update(scf_energy_exact=np.array(re["energy"]), scf_iterations_exact=np.array(re["iterations"]))
+    if golden_energy is not None:
+        out["golden_energy"] = np.array(golden_energy)
+    os.remove(path)
+    np.savez_compressed(os.path.join(HERE, f"{name}{'_md' if md else ''}.npz"), **out)
+    print(name, "nbf", n, "stored", len(vals), "E" if scf else "", out.get("scf_energy", ""), file=sys.stderr)
+
+
+def published_energy(tag: str) -> float:
+    with open(os.path.join(REF, "test", f"scfout.dat.{tag}")) as f:
+        for line in f:
+            if line.startswith("Hartree Fock Energy"):
+                return float(line.split("=")[1].split()[0])
+    raise ValueError(tag)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--big", action="store_true")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    cases = []
+    # the configuration-0 water (STO-3G, eps 1e-10, flags 2 1 0)
+    cases.append(("h2o_sto3g_c0", molecules.patin_text(molecules.water(), "STO-3G", eps=1e-10), True, None, True))
+    cases.append(("h2o_631g", molecules.patin_text(molecules.water(), "6-31G", eps=1e-10), True, None, True))
+    # the reference's own test inputs with published energies (test/scfout.dat.*)
+    for bas in ("3g", "431", "631"):
+        for mol in ("h2", "n2", "co", "hf", "h2o", "nh3", "ch4"):
+            tag = f"{bas}.{mol}"
+            with open(os.path.join(REF, "test", f"patin.dat.{tag}")) as f:
+                txt = f.read()
+            cases.append((f"ref_{bas}_{mol}", txt, True, published_energy(tag), False))
+    # inputs without published outputs: open shells (UHF) and d shells
+    for tag in ("b.dhdz", "n.dhdz", "f.dhdz", "dh95.h2", "dh95.co2", "d6s3p.h2", "tzp.ch4"):
+        with open(os.path.join(REF, "test", f"patin.dat.{tag}")) as f:
+            txt = f.read()
+        cases.append((f"ref_{tag.replace('.', '_')}", txt, True, None, False))
+    # small UHF radicals and small alkanes
+    cases.append(("h2o_cation_631g", molecules.patin_text(molecules.water(), "6-31G", charge=1, eps=1e-10), True, None, False))
+    cases.append(("ethane_631g", molecules.patin_text(molecules.alkane(2), "6-31G", eps=1e-10), True, None, False))
+    cases.append(("propane_cation_sto3g", molecules.patin_text(molecules.alkane(3), "STO-3G", charge=1, eps=1e-10), True, None, False))
+    cases.append(("water3_631g", molecules.patin_text(molecules.water_cluster(3, 7), "6-31G", eps=1e-10), True, None, False))
+    if a.big:
+        cases.append(("decane_631g", molecules.patin_text(molecules.alkane(10), "6-31G", eps=1e-10), False, None, False))
+        cases.append(("water32_631g", molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10), False, None, False))
+    for c in cases:
+        if a.only and a.only not in c[0]:
+            continue
+        make_case(*c)
+    # MD-only reference build on a few cases (parity target of an MD kernel)
+    if not a.only:
+        for c in cases[:2]:
+            make_case(c[0], c[1], False, None, False, md=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,669 @@
+// C ABI of the direct Fock build (include/unomol_gb300.h): the GPU counterpart of unomol's
+// TwoElectronInts (TwoElectronInts.hpp:79-110).
+//
+// Setup (create / recalculate): shell pairs with their primitive-pair data are built and sorted into
+// blocks of equal (pair class, primitive-pair count); the Schwarz diagonal (ab|ab) is computed on the
+// GPU; pairs are re-sorted by descending bound within their block; then for every pair of blocks the
+// Schwarz "staircase" (bra i keeps the first n_i ket pairs) gives a compact work list per quartet class.
+// Fock build (fock_rhf / fock_uhf): expand packed P to a dense N x N copy, zero the accumulators,
+// launch one kernel per quartet class, fold G += T + T^T into packed storage.
+#include <algorithm>
+#include <memory>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/unomol_gb300.h"
+#include "fock_dispatch.cuh"
+#include "fock_kernels.cuh"
+
+using namespace ugb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct ClassLaunch {
+    int bc, kc;          // bra / ket pair classes
+    int bp_begin, nbp;   // range in the block-pair array
+    long long nwork;     // padded work items
+    long long quartets;  // unpadded
+};
+
+}  // namespace
+
+struct UnomolCtx {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    int nshell = 0, nbf = 0, ncen = 0, start_shell = 0, maxl = 0;
+    std::vector<int> sl, snp, scen, soff, sprim;
+    std::vector<double> alpha, coef, centers;
+    NormTable nt{};
+    // host copies of the setup
+    std::vector<ShellPair> pairs;
+    std::vector<PrimPair> prims;
+    std::vector<int> block_begin, block_count, block_class;
+    std::vector<char> block_new;
+    std::vector<BlockPair> bps;
+    std::vector<long long> prefix;
+    std::vector<ClassLaunch> launches;
+    // device buffers
+    ShellPair* d_pairs = nullptr;
+    PrimPair* d_prims = nullptr;
+    PrimPair32* d_prims32 = nullptr;
+    BlockPair* d_bps = nullptr;
+    long long* d_prefix = nullptr;
+    double* d_rys = nullptr;
+    float* d_rys32 = nullptr;
+    double* d_q = nullptr;
+    double *d_Pa = nullptr, *d_Pb = nullptr, *d_Ta = nullptr, *d_Tb = nullptr;
+    double *d_Ga = nullptr, *d_Gb = nullptr, *d_pk_a = nullptr, *d_pk_b = nullptr;
+    float* d_pmax = nullptr;
+    int *d_soff = nullptr, *d_sl = nullptr;
+    int* d_status = nullptr;
+    unsigned long long* d_counters = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // options
+    double schwarz_cut = STORE_CUT;
+    int prec_mode = UNOMOL_PREC_FP64;
+    int rys_mode = UNOMOL_RYS_REFERENCE;
+    double fp32_cut = 1e-10;
+    UnomolStats stats{};
+    std::string err;
+};
+
+namespace {
+
+int fail(UnomolCtx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+#define CU(call)                                                                                \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? UNOMOL_ENOMEM : UNOMOL_ECUDA,    \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// Component normalisation 1/sqrt(d(lx) d(ly) d(lz)) with the double-factorial table of
+// AuxFunctions.hpp:48-63, kept exactly as the reference builds it (d = 1, 1, 3, 45, 4725 for
+// l = 0..4; the l >= 3 entries differ from (2l-1)!!, which only matters for f and g shells).
+void build_norms(NormTable& nt) {
+    double dfact[5];
+    dfact[0] = 1.0;
+    double dx = 1.0;
+    for (int i = 1; i < 5; ++i) {
+        dfact[i] = dfact[i - 1] * dx;
+        dx *= (2 * i + 1);
+    }
+    for (int l = 0; l <= LMAX; ++l)
+        for (int c = 0; c < ncart(l); ++c)
+            nt.v[l][c] = 1.0 / std::sqrt(dfact[cart_lx(l, c)] * dfact[cart_ly(l, c)] * dfact[cart_lz(l, c)]);
+}
+
+// Primitive pairs of shell pair (ish, jsh) after the L swap (a = larger L), following the loops of
+// TwoElectronInts.cpp:439-460: a same-shell pair keeps j <= i with the factor 2 for j < i.
+void build_pair(UnomolCtx* ctx, int ish, int jsh, ShellPair& sp, std::vector<PrimPair>& prims) {
+    int a = ish, b = jsh;
+    if (ctx->sl[a] < ctx->sl[b]) std::swap(a, b);
+    sp.ish = ish;
+    sp.jsh = jsh;
+    sp.maxsh = ish;
+    sp.canon = ish * (ish + 1) / 2 + jsh;
+    sp.same = (ish == jsh);
+    sp.la = ctx->sl[a];
+    sp.lb = ctx->sl[b];
+    sp.a_off = ctx->soff[a];
+    sp.b_off = ctx->soff[b];
+    const double* A = &ctx->centers[3 * ctx->scen[a]];
+    const double* B = &ctx->centers[3 * ctx->scen[b]];
+    for (int k = 0; k < 3; ++k) sp.AB[k] = A[k] - B[k];
+    const double ab2 = sp.AB[0] * sp.AB[0] + sp.AB[1] * sp.AB[1] + sp.AB[2] * sp.AB[2];
+    sp.prim_begin = (int)prims.size();
+    const int na = ctx->snp[a], nb = ctx->snp[b];
+    for (int i = 0; i < na; ++i) {
+        const double ai = ctx->alpha[ctx->sprim[a] + i], ci = ctx->coef[ctx->sprim[a] + i];
+        const int jend = sp.same ? i + 1 : nb;
+        for (int j = 0; j < jend; ++j) {
+            const double bj = ctx->alpha[ctx->sprim[b] + j], cj = ctx->coef[ctx->sprim[b] + j];
+            const double f = (sp.same && i != j) ? 2.0 : 1.0;
+            PrimPair pp;
+            pp.p = ai + bj;
+            pp.rp = 1.0 / pp.p;
+            for (int k = 0; k < 3; ++k) {
+                pp.P[k] = (ai * A[k] + bj * B[k]) * pp.rp;
+                pp.PA[k] = pp.P[k] - A[k];
+            }
+            pp.E = std::exp(-ai * bj * ab2 * pp.rp) * pp.rp;
+            pp.cc = ci * cj * f;
+            prims.push_back(pp);
+        }
+    }
+    sp.nprim = (int)prims.size() - sp.prim_begin;
+    sp.q = 0.0;
+}
+
+void free_setup(UnomolCtx* c) {
+    dfree(c->d_pairs);
+    dfree(c->d_prims);
+    dfree(c->d_prims32);
+    dfree(c->d_bps);
+    dfree(c->d_prefix);
+    dfree(c->d_q);
+}
+
+// Work lists for the current Schwarz cutoff (host side; O(npairs * nblocks log npairs)).
+int build_worklists(UnomolCtx* ctx) {
+    ctx->bps.clear();
+    ctx->prefix.clear();
+    ctx->launches.clear();
+    const int nb = (int)ctx->block_begin.size();
+    const double cut = ctx->schwarz_cut;
+    int64_t total_quartets = 0, screened = 0, fq = 0, pq = 0;
+    // group block pairs by quartet class
+    std::vector<std::vector<BlockPair>> per_class(NPAIRCLASS * NPAIRCLASS);
+    for (int X = 0; X < nb; ++X) {
+        for (int Y = 0; Y <= X; ++Y) {
+            if (ctx->start_shell > 0 && !ctx->block_new[X] && !ctx->block_new[Y]) continue;
+            BlockPair bp{};
+            bp.bra_begin = ctx->block_begin[X];
+            bp.bra_count = ctx->block_count[X];
+            bp.ket_begin = ctx->block_begin[Y];
+            bp.ket_count = ctx->block_count[Y];
+            bp.triangle = (X == Y);
+            bp.prefix_off = (int)ctx->prefix.size();
+            long long run = 0;
+            ctx->prefix.push_back(0);
+            const ShellPair* kp = &ctx->pairs[bp.ket_begin];
+            const int nbra = bp.bra_count, nket = bp.ket_count;
+            const int la = ctx->pairs[bp.bra_begin].la, lb = ctx->pairs[bp.bra_begin].lb;
+            const int lc = kp[0].la, ld = kp[0].lb;
+            const int nfq = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
+            for (int i = 0; i < nbra; ++i) {
+                const double qi = ctx->pairs[bp.bra_begin + i].q;
+                // ket pairs sorted by descending q: count those with qi*qj >= cut
+                int lo = 0, hi = nket;
+                while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    if (qi * kp[mid].q >= cut) lo = mid + 1; else hi = mid;
+                }
+                int n = lo;
+                const int full = bp.triangle ? i + 1 : nket;
+                if (n > full) n = full;
+                total_quartets += full;
+                run += n;
+                ctx->prefix.push_back(run);
+                pq += (long long)n * ctx->pairs[bp.bra_begin + i].nprim * 0;  // filled below
+            }
+            bp.work_count = run;
+            screened += run;
+            fq += run * nfq;
+            (void)pq;
+            const int cls = ctx->block_class[X] * NPAIRCLASS + ctx->block_class[Y];
+            if (run > 0) per_class[cls].push_back(bp);
+            else ctx->prefix.resize(bp.prefix_off);  // drop the unused prefix
+        }
+    }
+    // primitive-quartet count: nprim is uniform within a block
+    int64_t prim_q = 0;
+    for (int cls = 0; cls < NPAIRCLASS * NPAIRCLASS; ++cls) {
+        auto& v = per_class[cls];
+        if (v.empty()) continue;
+        ClassLaunch L{};
+        L.bc = cls / NPAIRCLASS;
+        L.kc = cls % NPAIRCLASS;
+        L.bp_begin = (int)ctx->bps.size();
+        L.nbp = (int)v.size();
+        long long w = 0;
+        for (auto& bp : v) {
+            bp.work_begin = w;
+            w += (bp.work_count + 31) / 32 * 32;
+            L.quartets += bp.work_count;
+            prim_q += bp.work_count * (int64_t)ctx->pairs[bp.bra_begin].nprim * ctx->pairs[bp.ket_begin].nprim;
+            ctx->bps.push_back(bp);
+        }
+        L.nwork = w;
+        ctx->launches.push_back(L);
+    }
+    ctx->stats.shell_quartets = screened;
+    ctx->stats.shell_quartets_total = total_quartets;
+    ctx->stats.primitive_quartets = prim_q;
+    ctx->stats.function_quartets = fq;
+    dfree(ctx->d_bps);
+    dfree(ctx->d_prefix);
+    if (!ctx->bps.empty()) {
+        CU(cudaMalloc(&ctx->d_bps, sizeof(BlockPair) * ctx->bps.size()));
+        CU(cudaMemcpyAsync(ctx->d_bps, ctx->bps.data(), sizeof(BlockPair) * ctx->bps.size(), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMalloc(&ctx->d_prefix, sizeof(long long) * ctx->prefix.size()));
+        CU(cudaMemcpyAsync(ctx->d_prefix, ctx->prefix.data(), sizeof(long long) * ctx->prefix.size(), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CU(cudaStreamSynchronize(ctx->stream));
+    return UNOMOL_OK;
+}
+
+// Pairs, Schwarz bounds, block structure and work lists for the current geometry.
+int build_setup(UnomolCtx* ctx) {
+    free_setup(ctx);
+    ctx->pairs.clear();
+    ctx->prims.clear();
+    const int ns = ctx->nshell;
+    std::vector<ShellPair> raw;
+    raw.reserve((size_t)ns * (ns + 1) / 2);
+    for (int i = 0; i < ns; ++i)
+        for (int j = 0; j <= i; ++j) {
+            ShellPair sp{};
+            build_pair(ctx, i, j, sp, ctx->prims);
+            raw.push_back(sp);
+        }
+    // blocks: (class, nprim, new-ness) ascending by class
+    auto key = [&](const ShellPair& s) {
+        const int cls = pair_class(s.la, s.lb);
+        const int isnew = (s.maxsh >= ctx->start_shell) ? 1 : 0;
+        return ((long long)cls << 40) | ((long long)isnew << 32) | (long long)s.nprim;
+    };
+    std::stable_sort(raw.begin(), raw.end(), [&](const ShellPair& x, const ShellPair& y) { return key(x) < key(y); });
+    // Schwarz diagonal on the device
+    CU(cudaMalloc(&ctx->d_pairs, sizeof(ShellPair) * raw.size()));
+    CU(cudaMalloc(&ctx->d_prims, sizeof(PrimPair) * ctx->prims.size()));
+    CU(cudaMalloc(&ctx->d_q, sizeof(double) * raw.size()));
+    CU(cudaMemcpyAsync(ctx->d_pairs, raw.data(), sizeof(ShellPair) * raw.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->d_prims, ctx->prims.data(), sizeof(PrimPair) * ctx->prims.size(), cudaMemcpyHostToDevice, ctx->stream));
+    {
+        size_t i = 0;
+        while (i < raw.size()) {
+            const int cls = pair_class(raw[i].la, raw[i].lb);
+            size_t j = i;
+            while (j < raw.size() && pair_class(raw[j].la, raw[j].lb) == cls) ++j;
+            CU(launch_schwarz(cls, ctx->d_pairs, ctx->d_prims, (int)i, (int)(j - i), ctx->nt, ctx->d_rys, ctx->d_q, ctx->stream));
+            i = j;
+        }
+    }
+    std::vector<double> q(raw.size());
+    CU(cudaMemcpyAsync(q.data(), ctx->d_q, sizeof(double) * raw.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < raw.size(); ++i) raw[i].q = q[i];
+    // within each block, descending q
+    ctx->block_begin.clear();
+    ctx->block_count.clear();
+    ctx->block_class.clear();
+    ctx->block_new.clear();
+    size_t i = 0;
+    while (i < raw.size()) {
+        size_t j = i;
+        while (j < raw.size() && key(raw[j]) == key(raw[i])) ++j;
+        std::stable_sort(raw.begin() + i, raw.begin() + j, [](const ShellPair& x, const ShellPair& y) { return x.q > y.q; });
+        ctx->block_begin.push_back((int)i);
+        ctx->block_count.push_back((int)(j - i));
+        ctx->block_class.push_back(pair_class(raw[i].la, raw[i].lb));
+        ctx->block_new.push_back(raw[i].maxsh >= ctx->start_shell);
+        i = j;
+    }
+    ctx->pairs = raw;
+    ctx->stats.npairs = (int)raw.size();
+    CU(cudaMemcpyAsync(ctx->d_pairs, raw.data(), sizeof(ShellPair) * raw.size(), cudaMemcpyHostToDevice, ctx->stream));
+    // FP32 copy of the primitive pairs
+    std::vector<PrimPair32> p32(ctx->prims.size());
+    for (size_t k = 0; k < ctx->prims.size(); ++k) {
+        const PrimPair& s = ctx->prims[k];
+        PrimPair32& d = p32[k];
+        d.p = (float)s.p;
+        d.rp = (float)s.rp;
+        for (int m = 0; m < 3; ++m) {
+            d.P[m] = (float)s.P[m];
+            d.PA[m] = (float)s.PA[m];
+        }
+        d.E = (float)s.E;
+        d.cc = (float)s.cc;
+    }
+    CU(cudaMalloc(&ctx->d_prims32, sizeof(PrimPair32) * p32.size()));
+    CU(cudaMemcpyAsync(ctx->d_prims32, p32.data(), sizeof(PrimPair32) * p32.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return build_worklists(ctx);
+}
+
+// packed lower triangle -> dense symmetric N x N
+__global__ void expand_packed(const double* __restrict__ pk, double* __restrict__ full, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    const int i = (int)(t / n), j = (int)(t % n);
+    const int hi = i > j ? i : j, lo = i > j ? j : i;
+    full[t] = pk[(long long)hi * (hi + 1) / 2 + lo];
+}
+
+// G_packed[ij] += T[i][j] + T[j][i]
+__global__ void fold_packed(const double* __restrict__ T, double* __restrict__ G, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n2 = (long long)n * (n + 1) / 2;
+    if (t >= n2) return;
+    // invert t = i(i+1)/2 + j
+    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)i * (i + 1) / 2 > t) --i;
+    while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+    const int j = (int)(t - (long long)i * (i + 1) / 2);
+    G[t] += T[(long long)i * n + j] + T[(long long)j * n + i];
+}
+
+// max |P| over every shell pair block, for density-weighted screening
+__global__ void shell_pmax(const double* __restrict__ Pa, const double* __restrict__ Pb, const int* __restrict__ soff,
+                           const int* __restrict__ sl, int nshell, int n, float* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nshell * nshell) return;
+    const int a = t / nshell, b = t % nshell;
+    const int na = (sl[a] + 1) * (sl[a] + 2) / 2, nb = (sl[b] + 1) * (sl[b] + 2) / 2;
+    double m = 0.0;
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j) {
+            const long long ix = (long long)(soff[a] + i) * n + soff[b] + j;
+            double v = fabs(Pa[ix]);
+            if (Pb) v = fmax(v, fabs(Pb[ix]));
+            m = fmax(m, v);
+        }
+    out[t] = (float)m;
+}
+
+int ensure_density_buffers(UnomolCtx* ctx, bool uhf) {
+    const size_t n2 = (size_t)ctx->nbf * ctx->nbf;
+    const size_t np = (size_t)ctx->nbf * (ctx->nbf + 1) / 2;
+    if (!ctx->d_Pa) {
+        CU(cudaMalloc(&ctx->d_Pa, n2 * sizeof(double)));
+        CU(cudaMalloc(&ctx->d_Ta, n2 * sizeof(double)));
+        CU(cudaMalloc(&ctx->d_Ga, np * sizeof(double)));
+        CU(cudaMalloc(&ctx->d_pk_a, np * sizeof(double)));
+    }
+    if (uhf && !ctx->d_Pb) {
+        CU(cudaMalloc(&ctx->d_Pb, n2 * sizeof(double)));
+        CU(cudaMalloc(&ctx->d_Tb, n2 * sizeof(double)));
+        CU(cudaMalloc(&ctx->d_Gb, np * sizeof(double)));
+        CU(cudaMalloc(&ctx->d_pk_b, np * sizeof(double)));
+    }
+    return UNOMOL_OK;
+}
+
+// The Fock build proper: packed device P in, packed device G added into.
+int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa, double* dGb, cudaStream_t s) {
+    const bool uhf = dPb != nullptr;
+    int rc = ensure_density_buffers(ctx, uhf);
+    if (rc) return rc;
+    const int n = ctx->nbf;
+    const long long n2 = (long long)n * n, np = (long long)n * (n + 1) / 2;
+    int launches = 0;
+    CU(cudaEventRecord(ctx->ev[0], s));
+    expand_packed<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(dPa, ctx->d_Pa, n);
+    ++launches;
+    if (uhf) {
+        expand_packed<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(dPb, ctx->d_Pb, n);
+        ++launches;
+    }
+    CU(cudaMemsetAsync(ctx->d_Ta, 0, n2 * sizeof(double), s));
+    if (uhf) CU(cudaMemsetAsync(ctx->d_Tb, 0, n2 * sizeof(double), s));
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(ctx->ev[1], s));
+    FockArgs A{};
+    A.pairs = ctx->d_pairs;
+    A.prims = ctx->d_prims;
+    A.prims32 = ctx->d_prims32;
+    A.nbf = n;
+    A.Pa = ctx->d_Pa;
+    A.Pb = uhf ? ctx->d_Pb : nullptr;
+    A.Ta = ctx->d_Ta;
+    A.Tb = uhf ? ctx->d_Tb : nullptr;
+    A.thr_int = STORE_CUT;
+    A.prim_cut = PRIM_CUT;
+    A.fp32_cut = ctx->fp32_cut;
+    A.nshell = ctx->nshell;
+    A.rys_compat = ctx->rys_mode == UNOMOL_RYS_REFERENCE;
+    A.pmax = ctx->d_pmax;
+    A.status = ctx->d_status;
+    const bool mixed = ctx->prec_mode == UNOMOL_PREC_MIXED;
+    if (mixed) {
+        if (!ctx->d_pmax) CU(cudaMalloc(&ctx->d_pmax, sizeof(float) * ctx->nshell * ctx->nshell));
+        A.pmax = ctx->d_pmax;
+        const int ns2 = ctx->nshell * ctx->nshell;
+        shell_pmax<<<(ns2 + 255) / 256, 256, 0, s>>>(ctx->d_Pa, A.Pb, ctx->d_soff, ctx->d_sl, ctx->nshell, n, ctx->d_pmax);
+        CU(cudaGetLastError());
+        ++launches;
+    }
+    for (const ClassLaunch& L : ctx->launches) {
+        A.bps = ctx->d_bps + L.bp_begin;
+        A.prefix = ctx->d_prefix;
+        A.nbp = L.nbp;
+        A.nwork = L.nwork;
+        if (!mixed) {
+            A.mode = 0;
+            CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
+            ++launches;
+        } else {
+            A.mode = 1;
+            CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
+            A.mode = 2;
+            CU(launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s));
+            launches += 2;
+        }
+    }
+    CU(cudaEventRecord(ctx->ev[2], s));
+    fold_packed<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(ctx->d_Ta, dGa, n);
+    ++launches;
+    if (uhf) {
+        fold_packed<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(ctx->d_Tb, dGb, n);
+        ++launches;
+    }
+    CU(cudaGetLastError());
+    ctx->stats.kernel_launches = launches;
+    return UNOMOL_OK;
+}
+
+int finish_timing(UnomolCtx* ctx, cudaStream_t s) {
+    cudaEvent_t e3;
+    CU(cudaEventCreate(&e3));
+    CU(cudaEventRecord(e3, s));
+    CU(cudaEventSynchronize(e3));
+    float ms_eri = 0.f, ms_tot = 0.f;
+    CU(cudaEventElapsedTime(&ms_eri, ctx->ev[1], ctx->ev[2]));
+    CU(cudaEventElapsedTime(&ms_tot, ctx->ev[0], e3));
+    cudaEventDestroy(e3);
+    ctx->stats.ms_eri = ms_eri;
+    ctx->stats.ms_total = ms_tot;
+    return UNOMOL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* unomol_gpu_version(void) { return "unomol_gb300 0.1 (sm_103a)"; }
+
+const char* unomol_gpu_last_error(const UnomolCtx* ctx) {
+    if (ctx && !ctx->err.empty()) return ctx->err.c_str();
+    return g_last_error.c_str();
+}
+
+int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out) {
+    UnomolCtx* ctx = nullptr;
+    if (!b || !out) return fail(nullptr, UNOMOL_EINVAL, "null argument");
+    *out = nullptr;
+    if (b->nshell <= 0 || b->ncen <= 0 || b->norb <= 0 || !b->shell_l || !b->shell_nprim || !b->shell_center ||
+        !b->shell_offset || !b->alpha || !b->coef || !b->centers)
+        return fail(nullptr, UNOMOL_EINVAL, "incomplete basis description");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, UNOMOL_ENODEV, "no CUDA device: the GB300 Fock build has no CPU fallback");
+    std::unique_ptr<UnomolCtx> c(new UnomolCtx());
+    ctx = c.get();
+    ctx->nshell = b->nshell;
+    ctx->nbf = b->norb;
+    ctx->ncen = b->ncen;
+    ctx->start_shell = start_shell < 0 ? 0 : start_shell;
+    int np = 0, off = 0;
+    for (int i = 0; i < b->nshell; ++i) {
+        const int l = b->shell_l[i];
+        if (l < 0 || l > LMAX) return fail(nullptr, UNOMOL_EINVAL, "shell angular momentum above 2 is not supported by this build");
+        if (b->shell_nprim[i] <= 0) return fail(nullptr, UNOMOL_EINVAL, "shell with no primitives");
+        if (b->shell_center[i] < 0 || b->shell_center[i] >= b->ncen) return fail(nullptr, UNOMOL_EINVAL, "shell centre out of range");
+        if (b->shell_offset[i] != off) return fail(nullptr, UNOMOL_EINVAL, "shell offsets must follow shell order");
+        ctx->sl.push_back(l);
+        ctx->snp.push_back(b->shell_nprim[i]);
+        ctx->scen.push_back(b->shell_center[i]);
+        ctx->soff.push_back(b->shell_offset[i]);
+        ctx->sprim.push_back(np);
+        np += b->shell_nprim[i];
+        off += ncart(l);
+        ctx->maxl = std::max(ctx->maxl, l);
+    }
+    if (off != b->norb) return fail(nullptr, UNOMOL_EINVAL, "norb does not match the shells");
+    ctx->alpha.assign(b->alpha, b->alpha + np);
+    ctx->coef.assign(b->coef, b->coef + np);
+    ctx->centers.assign(b->centers, b->centers + 3 * b->ncen);
+    build_norms(ctx->nt);
+    CU(cudaGetDevice(&ctx->dev));
+    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
+    // Rys tables (polynomial blocks, then the large-T limit)
+    {
+        std::vector<double> t64(rys_table_len(RYS_DEG));
+        std::memcpy(t64.data(), RYS_TABLE_H, sizeof(double) * RYS_TABLE_SIZE);
+        std::vector<float> t32(rys_table_len(RYS32_DEG));
+        std::memcpy(t32.data(), RYS32_TABLE_H, sizeof(float) * RYS32_TABLE_SIZE);
+        for (int n = 0; n < 5; ++n)
+            for (int i = 0; i < 5; ++i) {
+                t64[RYS_TABLE_SIZE + n * 5 + i] = RYS_HERMITE_X_H[n][i];
+                t64[RYS_TABLE_SIZE + 25 + n * 5 + i] = RYS_HERMITE_W_H[n][i];
+                t32[RYS32_TABLE_SIZE + n * 5 + i] = (float)RYS_HERMITE_X_H[n][i];
+                t32[RYS32_TABLE_SIZE + 25 + n * 5 + i] = (float)RYS_HERMITE_W_H[n][i];
+            }
+        static_assert(rys_table_len(RYS_DEG) == RYS_TABLE_SIZE + 50, "table layout");
+        static_assert(rys_table_len(RYS32_DEG) == RYS32_TABLE_SIZE + 50, "table layout");
+        CU(cudaMalloc(&ctx->d_rys, sizeof(double) * t64.size()));
+        CU(cudaMalloc(&ctx->d_rys32, sizeof(float) * t32.size()));
+        CU(cudaMemcpy(ctx->d_rys, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ctx->d_rys32, t32.data(), sizeof(float) * t32.size(), cudaMemcpyHostToDevice));
+    }
+    CU(cudaMalloc(&ctx->d_status, sizeof(int)));
+    CU(cudaMemset(ctx->d_status, 0, sizeof(int)));
+    CU(cudaMalloc(&ctx->d_soff, sizeof(int) * ctx->nshell));
+    CU(cudaMalloc(&ctx->d_sl, sizeof(int) * ctx->nshell));
+    CU(cudaMemcpy(ctx->d_soff, ctx->soff.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(ctx->d_sl, ctx->sl.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
+    ctx->stats.nbf = ctx->nbf;
+    int rc = build_setup(ctx);
+    if (rc) {
+        g_last_error = ctx->err;
+        unomol_gpu_destroy(c.release());
+        return rc;
+    }
+    *out = c.release();
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_recalculate(UnomolCtx* ctx, const double* centers) {
+    if (!ctx || !centers) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    ctx->centers.assign(centers, centers + 3 * ctx->ncen);
+    return build_setup(ctx);
+}
+
+int unomol_gpu_set_screening(UnomolCtx* ctx, double cut) {
+    if (!ctx || !(cut >= 0.0)) return fail(ctx, UNOMOL_EINVAL, "bad screening cutoff");
+    ctx->schwarz_cut = cut;
+    return build_worklists(ctx);
+}
+
+int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cut) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    if (mode != UNOMOL_PREC_FP64 && mode != UNOMOL_PREC_MIXED) return fail(ctx, UNOMOL_EINVAL, "unknown precision mode");
+    if (!(fp32_cut >= 0.0)) return fail(ctx, UNOMOL_EINVAL, "bad FP32 cutoff");
+    ctx->prec_mode = mode;
+    ctx->fp32_cut = fp32_cut;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    if (mode != UNOMOL_RYS_REFERENCE && mode != UNOMOL_RYS_EXACT) return fail(ctx, UNOMOL_EINVAL, "unknown Rys mode");
+    ctx->rys_mode = mode;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_get_stats(const UnomolCtx* ctx, UnomolStats* out) {
+    if (!ctx || !out) return UNOMOL_EINVAL;
+    *out = ctx->stats;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_fock_rhf_device(UnomolCtx* ctx, const double* dP, double* dG, void* stream) {
+    if (!ctx || !dP || !dG) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return fock_device(ctx, dP, nullptr, dG, nullptr, s);
+}
+
+int unomol_gpu_fock_uhf_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa, double* dGb,
+                               void* stream) {
+    if (!ctx || !dPa || !dPb || !dGa || !dGb) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return fock_device(ctx, dPa, dPb, dGa, dGb, s);
+}
+
+int unomol_gpu_fock_rhf(UnomolCtx* ctx, const double* P, double* G) {
+    if (!ctx || !P || !G) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    int rc = ensure_density_buffers(ctx, false);
+    if (rc) return rc;
+    const size_t np = (size_t)ctx->nbf * (ctx->nbf + 1) / 2;
+    CU(cudaMemcpyAsync(ctx->d_pk_a, P, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->d_Ga, G, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    rc = fock_device(ctx, ctx->d_pk_a, nullptr, ctx->d_Ga, nullptr, ctx->stream);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(G, ctx->d_Ga, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    return finish_timing(ctx, ctx->stream);
+}
+
+int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, double* Ga, double* Gb) {
+    if (!ctx || !Pa || !Pb || !Ga || !Gb) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    int rc = ensure_density_buffers(ctx, true);
+    if (rc) return rc;
+    const size_t np = (size_t)ctx->nbf * (ctx->nbf + 1) / 2;
+    CU(cudaMemcpyAsync(ctx->d_pk_a, Pa, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->d_pk_b, Pb, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->d_Ga, Ga, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->d_Gb, Gb, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    rc = fock_device(ctx, ctx->d_pk_a, ctx->d_pk_b, ctx->d_Ga, ctx->d_Gb, ctx->stream);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(Ga, ctx->d_Ga, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(Gb, ctx->d_Gb, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    return finish_timing(ctx, ctx->stream);
+}
+
+void unomol_gpu_destroy(UnomolCtx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_setup(ctx);
+    dfree(ctx->d_rys);
+    dfree(ctx->d_rys32);
+    dfree(ctx->d_Pa);
+    dfree(ctx->d_Pb);
+    dfree(ctx->d_Ta);
+    dfree(ctx->d_Tb);
+    dfree(ctx->d_Ga);
+    dfree(ctx->d_Gb);
+    dfree(ctx->d_pk_a);
+    dfree(ctx->d_pk_b);
+    dfree(ctx->d_pmax);
+    dfree(ctx->d_status);
+    dfree(ctx->d_counters);
+    dfree(ctx->d_soff);
+    dfree(ctx->d_sl);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+}  // extern "C"

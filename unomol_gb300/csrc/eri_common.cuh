@@ -1,0 +1,96 @@
+// Shared device/host definitions of the direct Fock build: data layout of shell pairs and primitive
+// pairs in HBM, Cartesian component tables, and the Rys root/weight evaluation.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ugb {
+
+constexpr int LMAX = 2;                 // angular momentum handled by the templated Rys kernels
+constexpr int NPAIRCLASS = (LMAX + 1) * (LMAX + 2) / 2;  // (la >= lb) pair classes
+constexpr double SRTERM = 34.9868366552497250;  // 2 pi^{5/2} (TwoElectronInts.cpp:427)
+constexpr double PRIM_CUT = 1.e-12;     // primitive prefactor cut (TwoElectronInts.cpp:428,478-479)
+constexpr double STORE_CUT = 1.e-14;    // integral storage cut (TwoElectronInts.cpp:517,668)
+
+__host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+__host__ __device__ constexpr int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
+
+// Cartesian exponents of component c of a shell with angular momentum l, in the reference's order:
+// lx descending, then ly descending (AuxFunctions.hpp:35-43).
+// Closed form (components with lx = l - i form the i-th block of i+1 entries, ly descending), so
+// that unrolled kernels fold it to constants without evaluating loops.
+__host__ __device__ constexpr int cart_blk(int c) { return (c >= 1) + (c >= 3) + (c >= 6) + (c >= 10); }
+__host__ __device__ constexpr int cart_lx(int l, int c) { return l - cart_blk(c); }
+__host__ __device__ constexpr int cart_ly(int l, int c) {
+    return cart_blk(c) - (c - cart_blk(c) * (cart_blk(c) + 1) / 2);
+}
+__host__ __device__ constexpr int cart_lz(int l, int c) { return l - cart_lx(l, c) - cart_ly(l, c); }
+
+// One primitive pair of a shell pair (a has the larger L after the swap of
+// TwoElectronInts.cpp:563-579).  72 bytes; the kernels read it through the read-only path.
+struct PrimPair {
+    double p;          // alpha_a + alpha_b
+    double rp;         // 1 / p
+    double P[3];       // Gaussian product centre
+    double PA[3];      // P - A
+    double E;          // exp(-alpha_a alpha_b |AB|^2 / p) / p, coefficient free (prefactor screen)
+    double cc;         // c_a c_b, times 2 for the i != j half of a same-shell pair
+                       // (TwoElectronInts.cpp:444-449)
+};
+
+struct PrimPair32 {
+    float p, rp, P[3], PA[3], E, cc;
+};
+
+// One shell pair, sorted into blocks of equal (class, primitive-pair count), within a block by
+// descending Schwarz bound.
+struct ShellPair {
+    int a_off, b_off;      // first AO of shell a (larger L) and of shell b
+    int la, lb;            // la >= lb
+    int prim_begin, nprim; // range in the PrimPair array
+    int canon;             // canonical pair id ish*(ish+1)/2 + jsh (ish >= jsh, original order)
+    int same;              // ish == jsh
+    double AB[3];          // A - B
+    double q;              // Schwarz bound: max over functions of sqrt|(ab|ab)|
+    int ish, jsh;          // shell indices (ish >= jsh)
+    int maxsh;             // max(ish, jsh)
+    int pad;
+};
+
+// A rectangle (or triangle, when bra block == ket block) of quartets between two pair blocks,
+// trimmed by the Schwarz staircase: bra pair i pairs with the first cnt[i] ket pairs of its block.
+struct BlockPair {
+    int bra_begin, bra_count;   // pair index range of the bra block
+    int ket_begin, ket_count;   // pair index range of the ket block
+    int triangle;               // bra block == ket block: ket index <= bra index
+    int prefix_off;             // offset of this block pair's prefix array (bra_count + 1 entries)
+    long long work_begin;       // first work item (multiple of 32, so warps never straddle)
+    long long work_count;       // quartets in this block pair
+};
+
+// Kernel arguments shared by every class instance.
+struct FockArgs {
+    const ShellPair* pairs;
+    const PrimPair* prims;
+    const PrimPair32* prims32;
+    const BlockPair* bps;
+    const long long* prefix;    // concatenated staircase prefix sums
+    int nbp;                    // block pairs of this launch
+    long long nwork;            // work items of this launch (padded)
+    int nbf;
+    const double* Pa;           // full N x N density (RHF: P; UHF: Pa)
+    const double* Pb;           // UHF: Pb; RHF: nullptr
+    const float* pmax;          // shell-pair max |P| (nshell x nshell), for density screening
+    double* Ta;                 // N x N accumulators; G = T + T^T
+    double* Tb;                 // UHF beta accumulator
+    double thr_int;             // per-integral cut (1e-14)
+    double prim_cut;            // primitive prefactor cut (1e-12)
+    double fp32_cut;            // mixed mode: bound*pmax below this -> FP32 kernel, else FP64
+    int mode;                   // 0 all quartets; 1 only "large" (FP64 part); 2 only "small" (FP32 part)
+    int nshell;
+    int rys_compat;             // reference-compatible two-root Rys regime (FP64 only)
+    unsigned long long* counters;  // [0] quartets evaluated
+    int* status;                // device error flag
+};
+
+}  // namespace ugb

@@ -1,0 +1,630 @@
+// Direct J/K Fock build: one thread per unique shell quartet, templated on the angular class
+// (la lb | lc ld) and on the arithmetic type (double for the plain path, float for the FP32 part
+// of the mixed-precision path).  Per primitive quartet: Rys roots and weights from piecewise
+// polynomials (registers), the 2D Rys recurrence and the horizontal transfer per Cartesian axis
+// (registers), and the contracted integrals accumulated in registers.  After the primitive loops
+// the integrals are contracted with the density and the six J/K contributions of every function
+// quartet are summed in registers and scattered with FP64 atomics into a dense N x N accumulator T,
+// whose symmetrisation T + T^T is the G matrix.
+//
+// Reference: TwoElectronInts.cpp:420-509 (calc_two_electron_ints_rys), Rys.hpp:85-212 (Recur,
+// Shift, RecurKernel, ShiftKernel), TwoElectronInts.cpp:699-820 (formGMatrixKernel{,2}).
+#pragma once
+#include "eri_common.cuh"
+#include "rys_tables.inc"
+
+namespace ugb {
+
+template <typename R> struct RysDeg;
+template <> struct RysDeg<double> { static constexpr int value = RYS_DEG; };
+template <> struct RysDeg<float> { static constexpr int value = RYS32_DEG; };
+
+__host__ __device__ constexpr double rys_tmax(int n) {
+    return n == 1 ? RYS_TMAX_1 : n == 2 ? RYS_TMAX_2 : n == 3 ? RYS_TMAX_3 : n == 4 ? RYS_TMAX_4 : RYS_TMAX_5;
+}
+// Offset of the n-root block in a table of polynomials of degree deg (layout of rys_tables.inc).
+__host__ __device__ constexpr int rys_off(int n, int deg) {
+    int o = 0;
+    for (int m = 1; m < n; ++m) o += int(rys_tmax(m) / RYS_H) * 2 * m * (deg + 1);
+    return o;
+}
+// Size of a device table: polynomial blocks, then hermite x[5][5] and w[5][5].
+__host__ __device__ constexpr int rys_table_len(int deg) { return rys_off(RYS_NMAX + 1, deg) + 50; }
+
+// Reference-compatible two-root regime.  For 15 < T <= 40 the reference's Rys::root2 evaluates a
+// large-T form with fitted e^{-T} corrections (Rys.cpp:611-623) that departs from the exact
+// quadrature by up to 3.5e-4 relative at T = 15 (below 1e-12 from T ~ 31 on); the golden energies of
+// the reference carry that departure.  The same form is evaluated here when the context runs in the
+// reference-compatible Rys mode, so that the drop-in reproduces the reference's G and energies.
+// Constants: the Hermite limit r12, r22, w22 and pi/4 as the reference writes them (Rys.cpp:416-419)
+// and the six fitted coefficients of that regime.
+__device__ __forceinline__ void rys2_reference_regime(double T, double* x, double* w) {
+    const double r12 = .275255128608411, r22 = 2.72474487139158, w22 = .0917517095361369;
+    const double g = exp(-T);
+    const double w0 = sqrt(.785398163397448 / T);
+    const double u0 = (T * -.87894730749888 + 10.9243702330261) * g + r12 / (T - r12);
+    const double u1 = (T * -9.28903924275977 + 81.0642367843811) * g + r22 / (T - r22);
+    const double w1 = (T * 4.468573893084 - 77.9250653461045) * g + w22 * w0;
+    x[0] = u0 / (1.0 + u0);  // the reference stores u = t^2 / (1 - t^2) (Rys.cpp:307-310)
+    x[1] = u1 / (1.0 + u1);
+    w[0] = w0 - w1;
+    w[1] = w1;
+}
+
+// Rys nodes x_r = t_r^2 and weights w_r at T (NR roots).  compat: reference-compatible two-root
+// regime (FP64 only; see rys2_reference_regime).
+template <int NR, typename R>
+__device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, R* w, bool compat = false) {
+    constexpr int DEG = RysDeg<R>::value;
+    constexpr R TMAX = R(rys_tmax(NR));
+    if constexpr (NR == 2 && sizeof(R) == 8) {
+        if (compat && T > R(15) && T <= R(40)) {
+            rys2_reference_regime(T, x, w);
+            return;
+        }
+    }
+    if (T < TMAX) {
+        int k = (int)T;  // interval width RYS_H == 1
+        R y = R(2) * (T - R(k)) - R(1);
+        const R* c = tab + rys_off(NR, DEG) + k * (2 * NR * (DEG + 1));
+#pragma unroll
+        for (int i = 0; i < NR; ++i) {
+            const R* cx = c + (2 * i) * (DEG + 1);
+            const R* cw = cx + (DEG + 1);
+            R vx = __ldg(cx), vw = __ldg(cw);
+#pragma unroll
+            for (int d = 1; d <= DEG; ++d) {
+                vx = fma(vx, y, __ldg(cx + d));
+                vw = fma(vw, y, __ldg(cw + d));
+            }
+            x[i] = vx;
+            w[i] = vw;
+        }
+    } else {  // large-T limit (also taken by a NaN T, which keeps the table index in range)
+        const R* herm = tab + rys_table_len(DEG) - 50;
+        R rT = R(1) / T;
+        R s = sqrt(rT);
+#pragma unroll
+        for (int i = 0; i < NR; ++i) {
+            x[i] = __ldg(herm + (NR - 1) * 5 + i) * rT;
+            w[i] = __ldg(herm + 25 + (NR - 1) * 5 + i) * s;
+        }
+    }
+}
+
+// Per axis: 2D Rys recurrence G[i][j] (i <= la+lb, j <= lc+ld) from G[0][0] = g00, then the
+// horizontal transfer to I[a][b][c][d] (a <= la, b <= lb, c <= lc, d <= ld):
+//   I(a, b+1) = I(a+1, b) + AB I(a, b), and the same on the ket with CD.
+// Rys.hpp:194-212 writes the same recurrence; Rys.hpp:173-192 applies the transfer by binomial
+// sums per function quartet instead.
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void rys_axis(R g00, R C, R Cp, R B00, R B1, R B1p, R AB, R CD,
+                                         R (&I)[(LA + 1) * (LB + 1) * (LC + 1) * (LD + 1)]) {
+    constexpr int L12 = LA + LB, L34 = LC + LD;
+    R G[L12 + 1][L34 + 1];
+    G[0][0] = g00;
+    if constexpr (L12 > 0) G[1][0] = C * g00;
+#pragma unroll
+    for (int i = 1; i < L12; ++i) G[i + 1][0] = C * G[i][0] + R(i) * B1 * G[i - 1][0];
+#pragma unroll
+    for (int j = 0; j < L34; ++j) {
+#pragma unroll
+        for (int i = 0; i <= L12; ++i) {
+            R v = Cp * G[i][j];
+            if (j > 0) v = fma(R(j) * B1p, G[i][j - 1], v);
+            if (i > 0) v = fma(R(i) * B00, G[i - 1][j], v);
+            G[i][j + 1] = v;
+        }
+    }
+    // bra transfer: X[b][a][j], a <= L12 - b
+    R X[LB + 1][L12 + 1][L34 + 1];
+#pragma unroll
+    for (int a = 0; a <= L12; ++a)
+#pragma unroll
+        for (int j = 0; j <= L34; ++j) X[0][a][j] = G[a][j];
+#pragma unroll
+    for (int b = 1; b <= LB; ++b)
+#pragma unroll
+        for (int a = 0; a <= L12 - b; ++a)
+#pragma unroll
+            for (int j = 0; j <= L34; ++j) X[b][a][j] = fma(AB, X[b - 1][a][j], X[b - 1][a + 1][j]);
+    // ket transfer per (a, b)
+#pragma unroll
+    for (int a = 0; a <= LA; ++a)
+#pragma unroll
+        for (int b = 0; b <= LB; ++b) {
+            R Y[LD + 1][L34 + 1];
+#pragma unroll
+            for (int c = 0; c <= L34; ++c) Y[0][c] = X[b][a][c];
+#pragma unroll
+            for (int d = 1; d <= LD; ++d)
+#pragma unroll
+                for (int c = 0; c <= L34 - d; ++c) Y[d][c] = fma(CD, Y[d - 1][c], Y[d - 1][c + 1]);
+#pragma unroll
+            for (int c = 0; c <= LC; ++c)
+#pragma unroll
+                for (int d = 0; d <= LD; ++d) I[((a * (LB + 1) + b) * (LC + 1) + c) * (LD + 1) + d] = Y[d][c];
+        }
+}
+
+template <int LA, int LB, int LC, int LD>
+struct QClass {
+    static constexpr int L12 = LA + LB, L34 = LC + LD, NR = (L12 + L34) / 2 + 1;
+    static constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    static constexpr int NF = NA * NB * NC * ND;
+    static constexpr int NI = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
+    __host__ __device__ static constexpr int iidx(int a, int b, int c, int d) {
+        return ((a * (LB + 1) + b) * (LC + 1) + c) * (LD + 1) + d;
+    }
+};
+
+// Contracted integrals (ab|cd) of one shell quartet, without the component normalisation factors,
+// accumulated into acc[NF] (function quartet f = ((ia*NB + ib)*NC + ic)*ND + id).
+template <int LA, int LB, int LC, int LD, typename R, typename PP>
+__device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const ShellPair& ket,
+                                                  const PP* __restrict__ prims,
+                                                  const R* __restrict__ rys, R prim_cut, bool compat,
+                                                  R (&acc)[QClass<LA, LB, LC, LD>::NF]) {
+    using Q = QClass<LA, LB, LC, LD>;
+    constexpr int NR = Q::NR;
+#pragma unroll
+    for (int f = 0; f < Q::NF; ++f) acc[f] = R(0);
+    const R ABx = R(bra.AB[0]), ABy = R(bra.AB[1]), ABz = R(bra.AB[2]);
+    const R CDx = R(ket.AB[0]), CDy = R(ket.AB[1]), CDz = R(ket.AB[2]);
+    const PP* pb = prims + bra.prim_begin;
+    const PP* pk = prims + ket.prim_begin;
+    const int nb = bra.nprim, nk = ket.nprim;
+    for (int ib = 0; ib < nb; ++ib) {
+        const R p = pb[ib].p, rp = pb[ib].rp, Eab = pb[ib].E, cab = pb[ib].cc;
+        const R Px = pb[ib].P[0], Py = pb[ib].P[1], Pz = pb[ib].P[2];
+        const R PAx = pb[ib].PA[0], PAy = pb[ib].PA[1], PAz = pb[ib].PA[2];
+        for (int ik = 0; ik < nk; ++ik) {
+            const R q = pk[ik].p, rq = pk[ik].rp, Ecd = pk[ik].E, ccd = pk[ik].cc;
+            const R rpq = R(1) / (p + q);
+            R sr = R(SRTERM) * Eab * Ecd * sqrt(rpq);
+            if (sr < prim_cut) continue;  // TwoElectronInts.cpp:478-479 (before the coefficients)
+            sr *= cab * ccd;
+            const R QCx = pk[ik].PA[0], QCy = pk[ik].PA[1], QCz = pk[ik].PA[2];
+            const R PQx = Px - R(pk[ik].P[0]), PQy = Py - R(pk[ik].P[1]), PQz = Pz - R(pk[ik].P[2]);
+            const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
+            R x[NR], w[NR];
+            rys_roots<NR, R>(T, rys, x, w, compat);
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const R fff = x[r] * rpq;  // t^2 / (p + q)   (Rys.hpp:126-129)
+                const R B00 = R(0.5) * fff;
+                const R B1 = (R(0.5) - B00 * q) * rp;
+                const R B1p = (R(0.5) - B00 * p) * rq;
+                const R qf = q * fff, pf = p * fff;
+                R Ix[Q::NI], Iy[Q::NI], Iz[Q::NI];
+                rys_axis<LA, LB, LC, LD, R>(R(1), PAx - qf * PQx, QCx + pf * PQx, B00, B1, B1p, ABx, CDx, Ix);
+                rys_axis<LA, LB, LC, LD, R>(R(1), PAy - qf * PQy, QCy + pf * PQy, B00, B1, B1p, ABy, CDy, Iy);
+                rys_axis<LA, LB, LC, LD, R>(w[r] * sr, PAz - qf * PQz, QCz + pf * PQz, B00, B1, B1p, ABz, CDz, Iz);
+#pragma unroll
+                for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+                    for (int ibb = 0; ibb < Q::NB; ++ibb)
+#pragma unroll
+                        for (int ic = 0; ic < Q::NC; ++ic)
+#pragma unroll
+                            for (int id = 0; id < Q::ND; ++id) {
+                                const int f = ((ia * Q::NB + ibb) * Q::NC + ic) * Q::ND + id;
+                                const int jx = Q::iidx(cart_lx(LA, ia), cart_lx(LB, ibb), cart_lx(LC, ic), cart_lx(LD, id));
+                                const int jy = Q::iidx(cart_ly(LA, ia), cart_ly(LB, ibb), cart_ly(LC, ic), cart_ly(LD, id));
+                                const int jz = Q::iidx(cart_lz(LA, ia), cart_lz(LB, ibb), cart_lz(LC, ic), cart_lz(LD, id));
+                                acc[f] = fma(Ix[jx] * Iy[jy], Iz[jz], acc[f]);
+                            }
+            }
+        }
+    }
+}
+
+// Decode work item g of a launch into (bra pair, ket pair).  Returns false for padding.
+__device__ __forceinline__ bool decode_work(const FockArgs& A, long long g, int& bra_idx, int& ket_idx) {
+    if (g >= A.nwork) return false;
+    int lo = 0, hi = A.nbp - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (A.bps[mid].work_begin <= g) lo = mid; else hi = mid - 1;
+    }
+    const BlockPair& bp = A.bps[lo];
+    long long w = g - bp.work_begin;
+    if (w >= bp.work_count) return false;
+    const long long* pre = A.prefix + bp.prefix_off;
+    int a = 0, b = bp.bra_count - 1;  // largest i with pre[i] <= w
+    while (a < b) {
+        int mid = (a + b + 1) >> 1;
+        if (pre[mid] <= w) a = mid; else b = mid - 1;
+    }
+    bra_idx = bp.bra_begin + a;
+    ket_idx = bp.ket_begin + (int)(w - pre[a]);
+    return true;
+}
+
+// Density contraction of one shell quartet and scatter into T (G = T + T^T):
+//   T[a][b] += 4 v' P_cd   T[c][d] += 4 v' P_ab   (2J)
+//   T[a][c] -= v' P_bd  T[b][c] -= v' P_ad  T[a][d] -= v' P_bc  T[b][d] -= v' P_ac   (K)
+// with v' = v / |stabiliser of the shell quartet| (1/2 for a == b, c == d, (ab) == (cd) each);
+// the sum over the 8 index permutations of every function quartet of the rectangle a x b x c x d
+// then counts every ordered (ij|kl) exactly once.  UHF (UHF = true): Ta collects J(Pa + Pb) - K(Pa)
+// and Tb collects J(Pa + Pb) - K(Pb) in the same T + T^T form (TwoElectronInts.cpp:749-820).
+template <int LA, int LB, int LC, int LD, bool UHF, typename R>
+__device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& bra, const ShellPair& ket,
+                                          bool same_pair, const R (&acc)[QClass<LA, LB, LC, LD>::NF],
+                                          const double (&nrm)[LMAX + 1][6]) {
+    using Q = QClass<LA, LB, LC, LD>;
+    const int N = A.nbf;
+    double deg = 1.0;
+    if (bra.same) deg *= 0.5;
+    if (ket.same) deg *= 0.5;
+    if (same_pair) deg *= 0.5;
+    const double* __restrict__ Pa = A.Pa;
+    const double* __restrict__ Pb = A.Pb;
+    double jcd[Q::NC * Q::ND];
+    double kbc[Q::NB * Q::NC], kbd[Q::NB * Q::ND];
+    double kbcB[UHF ? Q::NB * Q::NC : 1], kbdB[UHF ? Q::NB * Q::ND : 1];
+#pragma unroll
+    for (int i = 0; i < Q::NC * Q::ND; ++i) jcd[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < Q::NB * Q::NC; ++i) { kbc[i] = 0.0; if constexpr (UHF) kbcB[i] = 0.0; }
+#pragma unroll
+    for (int i = 0; i < Q::NB * Q::ND; ++i) { kbd[i] = 0.0; if constexpr (UHF) kbdB[i] = 0.0; }
+#pragma unroll
+    for (int ia = 0; ia < Q::NA; ++ia) {
+        const int a = bra.a_off + ia;
+        double kac[Q::NC], kad[Q::ND], kacB[UHF ? Q::NC : 1], kadB[UHF ? Q::ND : 1];
+#pragma unroll
+        for (int i = 0; i < Q::NC; ++i) { kac[i] = 0.0; if constexpr (UHF) kacB[i] = 0.0; }
+#pragma unroll
+        for (int i = 0; i < Q::ND; ++i) { kad[i] = 0.0; if constexpr (UHF) kadB[i] = 0.0; }
+#pragma unroll
+        for (int ib = 0; ib < Q::NB; ++ib) {
+            const int b = bra.b_off + ib;
+            double Pab = __ldg(Pa + a * N + b);
+            if constexpr (UHF) Pab += __ldg(Pb + a * N + b);
+            double jab = 0.0;
+#pragma unroll
+            for (int ic = 0; ic < Q::NC; ++ic) {
+                const int c = ket.a_off + ic;
+#pragma unroll
+                for (int id = 0; id < Q::ND; ++id) {
+                    const int d = ket.b_off + id;
+                    const int f = ((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id;
+                    double v = double(acc[f]) * (nrm[LA][ia] * nrm[LB][ib] * nrm[LC][ic] * nrm[LD][id]);
+                    if (!(fabs(v) > A.thr_int)) continue;  // TwoElectronInts.cpp:668
+                    v *= deg;
+                    double Pcd = __ldg(Pa + c * N + d);
+                    if constexpr (UHF) Pcd += __ldg(Pb + c * N + d);
+                    jab = fma(v, Pcd, jab);
+                    jcd[ic * Q::ND + id] = fma(v, Pab, jcd[ic * Q::ND + id]);
+                    kac[ic] = fma(v, __ldg(Pa + b * N + d), kac[ic]);
+                    kad[id] = fma(v, __ldg(Pa + b * N + c), kad[id]);
+                    kbc[ib * Q::NC + ic] = fma(v, __ldg(Pa + a * N + d), kbc[ib * Q::NC + ic]);
+                    kbd[ib * Q::ND + id] = fma(v, __ldg(Pa + a * N + c), kbd[ib * Q::ND + id]);
+                    if constexpr (UHF) {
+                        kacB[ic] = fma(v, __ldg(Pb + b * N + d), kacB[ic]);
+                        kadB[id] = fma(v, __ldg(Pb + b * N + c), kadB[id]);
+                        kbcB[ib * Q::NC + ic] = fma(v, __ldg(Pb + a * N + d), kbcB[ib * Q::NC + ic]);
+                        kbdB[ib * Q::ND + id] = fma(v, __ldg(Pb + a * N + c), kbdB[ib * Q::ND + id]);
+                    }
+                }
+            }
+            if constexpr (UHF) {
+                atomicAdd(A.Ta + a * N + b, 2.0 * jab);
+                atomicAdd(A.Tb + a * N + b, 2.0 * jab);
+            } else {
+                atomicAdd(A.Ta + a * N + b, 4.0 * jab);
+            }
+        }
+#pragma unroll
+        for (int ic = 0; ic < Q::NC; ++ic) {
+            const int c = ket.a_off + ic;
+            atomicAdd(A.Ta + a * N + c, -kac[ic]);
+            if constexpr (UHF) atomicAdd(A.Tb + a * N + c, -kacB[ic]);
+        }
+#pragma unroll
+        for (int id = 0; id < Q::ND; ++id) {
+            const int d = ket.b_off + id;
+            atomicAdd(A.Ta + a * N + d, -kad[id]);
+            if constexpr (UHF) atomicAdd(A.Tb + a * N + d, -kadB[id]);
+        }
+    }
+#pragma unroll
+    for (int ic = 0; ic < Q::NC; ++ic)
+#pragma unroll
+        for (int id = 0; id < Q::ND; ++id) {
+            const int c = ket.a_off + ic, d = ket.b_off + id;
+            if constexpr (UHF) {
+                atomicAdd(A.Ta + c * N + d, 2.0 * jcd[ic * Q::ND + id]);
+                atomicAdd(A.Tb + c * N + d, 2.0 * jcd[ic * Q::ND + id]);
+            } else {
+                atomicAdd(A.Ta + c * N + d, 4.0 * jcd[ic * Q::ND + id]);
+            }
+        }
+#pragma unroll
+    for (int ib = 0; ib < Q::NB; ++ib) {
+        const int b = bra.b_off + ib;
+#pragma unroll
+        for (int ic = 0; ic < Q::NC; ++ic) {
+            const int c = ket.a_off + ic;
+            atomicAdd(A.Ta + b * N + c, -kbc[ib * Q::NC + ic]);
+            if constexpr (UHF) atomicAdd(A.Tb + b * N + c, -kbcB[ib * Q::NC + ic]);
+        }
+#pragma unroll
+        for (int id = 0; id < Q::ND; ++id) {
+            const int d = ket.b_off + id;
+            atomicAdd(A.Ta + b * N + d, -kbd[ib * Q::ND + id]);
+            if constexpr (UHF) atomicAdd(A.Tb + b * N + d, -kbdB[ib * Q::ND + id]);
+        }
+    }
+}
+
+struct NormTable {
+    double v[LMAX + 1][6];
+};
+
+template <int LA, int LB, int LC, int LD, bool UHF, typename R>
+__global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
+    using Q = QClass<LA, LB, LC, LD>;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int bi, ki;
+    if (!decode_work(A, g, bi, ki)) return;
+    const ShellPair bra = A.pairs[bi];
+    const ShellPair ket = A.pairs[ki];
+    if (A.mode != 0) {
+        // mixed precision: the FP64 launch (mode 1) takes quartets whose bound * max|P| is at or
+        // above the cutoff, the FP32 launch (mode 2) the rest
+        const double pm = (double)A.pmax[bra.ish * A.nshell + bra.jsh] + 0.0;
+        const double pk = (double)A.pmax[ket.ish * A.nshell + ket.jsh];
+        const double big = bra.q * ket.q * fmax(pm, pk);
+        const bool is_big = big >= A.fp32_cut;
+        if ((A.mode == 1) != is_big) return;
+    }
+    R acc[Q::NF];
+    if constexpr (sizeof(R) == 8)
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.rys_compat != 0, acc);
+    else
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, R(A.prim_cut), false, acc);
+    digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt.v);
+}
+
+// Schwarz diagonal: q[pair] = sqrt(max_{a,b} |(ab|ab)|) for every pair of one class (no primitive
+// cut, so the bound is that of the exact integrals).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) schwarz_kernel(const ShellPair* __restrict__ pairs, const PrimPair* __restrict__ prims,
+                                                      int begin, int count, const NormTable nt,
+                                                      const double* __restrict__ rys, double* __restrict__ q_out) {
+    using Q = QClass<LA, LB, LA, LB>;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const ShellPair sp = pairs[begin + t];
+    double acc[Q::NF];
+    shell_quartet_eri<LA, LB, LA, LB, double, PrimPair>(sp, sp, prims, rys, 0.0, false, acc);
+    double m = 0.0;
+#pragma unroll
+    for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < Q::NB; ++ib) {
+            const int f = ((ia * Q::NB + ib) * Q::NC + ia) * Q::ND + ib;
+            const double n = nt.v[LA][ia] * nt.v[LB][ib];
+            m = fmax(m, fabs(acc[f]) * n * n);
+        }
+    q_out[begin + t] = sqrt(m);
+}
+
+}  // namespace ugb
+
+namespace ugb {
+
+// ---------------------------------------------------------------------------------------------
+// Generic path for the classes with more than 81 function quartets (d shells): the same
+// arithmetic with runtime angular momenta and loops, the integrals in thread-local memory.
+// ---------------------------------------------------------------------------------------------
+constexpr int GEN_LMAX = 2;
+constexpr int GEN_NC = (GEN_LMAX + 1) * (GEN_LMAX + 2) / 2;
+constexpr int GEN_NF = GEN_NC * GEN_NC * GEN_NC * GEN_NC;
+constexpr int GEN_NI = (GEN_LMAX + 1) * (GEN_LMAX + 1) * (GEN_LMAX + 1) * (GEN_LMAX + 1);
+
+template <typename R>
+__device__ void rys_axis_rt(int la, int lb, int lc, int ld, R g00, R C, R Cp, R B00, R B1, R B1p, R AB,
+                            R CD, R* I) {
+    const int L12 = la + lb, L34 = lc + ld;
+    R G[2 * GEN_LMAX + 1][2 * GEN_LMAX + 1];
+    G[0][0] = g00;
+    if (L12 > 0) G[1][0] = C * g00;
+    for (int i = 1; i < L12; ++i) G[i + 1][0] = C * G[i][0] + R(i) * B1 * G[i - 1][0];
+    for (int j = 0; j < L34; ++j)
+        for (int i = 0; i <= L12; ++i) {
+            R v = Cp * G[i][j];
+            if (j > 0) v = fma(R(j) * B1p, G[i][j - 1], v);
+            if (i > 0) v = fma(R(i) * B00, G[i - 1][j], v);
+            G[i][j + 1] = v;
+        }
+    R X[GEN_LMAX + 1][2 * GEN_LMAX + 1][2 * GEN_LMAX + 1];
+    for (int a = 0; a <= L12; ++a)
+        for (int j = 0; j <= L34; ++j) X[0][a][j] = G[a][j];
+    for (int b = 1; b <= lb; ++b)
+        for (int a = 0; a <= L12 - b; ++a)
+            for (int j = 0; j <= L34; ++j) X[b][a][j] = fma(AB, X[b - 1][a][j], X[b - 1][a + 1][j]);
+    for (int a = 0; a <= la; ++a)
+        for (int b = 0; b <= lb; ++b) {
+            R Y[GEN_LMAX + 1][2 * GEN_LMAX + 1];
+            for (int c = 0; c <= L34; ++c) Y[0][c] = X[b][a][c];
+            for (int d = 1; d <= ld; ++d)
+                for (int c = 0; c <= L34 - d; ++c) Y[d][c] = fma(CD, Y[d - 1][c], Y[d - 1][c + 1]);
+            for (int c = 0; c <= lc; ++c)
+                for (int d = 0; d <= ld; ++d) I[((a * (lb + 1) + b) * (lc + 1) + c) * (ld + 1) + d] = Y[d][c];
+        }
+}
+
+template <typename R>
+__device__ __forceinline__ void rys_roots_rt(int nr, R T, const R* __restrict__ tab, R* x, R* w, bool compat = false) {
+    switch (nr) {
+        case 1: rys_roots<1, R>(T, tab, x, w); break;
+        case 2: rys_roots<2, R>(T, tab, x, w, compat); break;
+        case 3: rys_roots<3, R>(T, tab, x, w); break;
+        case 4: rys_roots<4, R>(T, tab, x, w); break;
+        default: rys_roots<5, R>(T, tab, x, w); break;
+    }
+}
+
+template <bool UHF, typename R, typename PP>
+__global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const NormTable nt, const R* __restrict__ rys,
+                                                      const PP* __restrict__ prims, int la, int lb, int lc, int ld) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int bi, ki;
+    if (!decode_work(A, g, bi, ki)) return;
+    const ShellPair bra = A.pairs[bi];
+    const ShellPair ket = A.pairs[ki];
+    if (A.mode != 0) {
+        const double pm = fmax((double)A.pmax[bra.ish * A.nshell + bra.jsh], (double)A.pmax[ket.ish * A.nshell + ket.jsh]);
+        if ((A.mode == 1) != (bra.q * ket.q * pm >= A.fp32_cut)) return;
+    }
+    const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
+    const int NF = NA * NB * NC * ND;
+    const int nr = (la + lb + lc + ld) / 2 + 1;
+    R acc[GEN_NF];
+    for (int f = 0; f < NF; ++f) acc[f] = R(0);
+    const R prim_cut = R(A.prim_cut);
+    const PP* pb = prims + bra.prim_begin;
+    const PP* pk = prims + ket.prim_begin;
+    for (int ib = 0; ib < bra.nprim; ++ib) {
+        const R p = pb[ib].p, rp = pb[ib].rp, Eab = pb[ib].E, cab = pb[ib].cc;
+        for (int ik = 0; ik < ket.nprim; ++ik) {
+            const R q = pk[ik].p, rq = pk[ik].rp, Ecd = pk[ik].E, ccd = pk[ik].cc;
+            const R rpq = R(1) / (p + q);
+            R sr = R(SRTERM) * Eab * Ecd * sqrt(rpq);
+            if (sr < prim_cut) continue;
+            sr *= cab * ccd;
+            R PQ[3], x[5], w[5];
+            for (int k = 0; k < 3; ++k) PQ[k] = R(pb[ib].P[k]) - R(pk[ik].P[k]);
+            const R T = p * q * rpq * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
+            rys_roots_rt<R>(nr, T, rys, x, w, A.rys_compat != 0);
+            for (int r = 0; r < nr; ++r) {
+                const R fff = x[r] * rpq;
+                const R B00 = R(0.5) * fff;
+                const R B1 = (R(0.5) - B00 * q) * rp;
+                const R B1p = (R(0.5) - B00 * p) * rq;
+                R I[3][GEN_NI];
+                for (int k = 0; k < 3; ++k)
+                    rys_axis_rt<R>(la, lb, lc, ld, k == 2 ? w[r] * sr : R(1), R(pb[ib].PA[k]) - q * fff * PQ[k],
+                                   R(pk[ik].PA[k]) + p * fff * PQ[k], B00, B1, B1p, R(bra.AB[k]), R(ket.AB[k]), I[k]);
+                int f = 0;
+                for (int ia = 0; ia < NA; ++ia)
+                    for (int ibb = 0; ibb < NB; ++ibb)
+                        for (int ic = 0; ic < NC; ++ic)
+                            for (int id = 0; id < ND; ++id, ++f) {
+                                auto idx = [&](int ax, int ca, int cb, int cc, int cd) {
+                                    auto comp = [&](int l, int c) {
+                                        return ax == 0 ? cart_lx(l, c) : ax == 1 ? cart_ly(l, c) : cart_lz(l, c);
+                                    };
+                                    return ((comp(la, ca) * (lb + 1) + comp(lb, cb)) * (lc + 1) + comp(lc, cc)) * (ld + 1) + comp(ld, cd);
+                                };
+                                acc[f] = fma(I[0][idx(0, ia, ibb, ic, id)] * I[1][idx(1, ia, ibb, ic, id)],
+                                             I[2][idx(2, ia, ibb, ic, id)], acc[f]);
+                            }
+            }
+        }
+    }
+    // density contraction and scatter, as digest_jk with runtime sizes
+    const int N = A.nbf;
+    double deg = 1.0;
+    if (bra.same) deg *= 0.5;
+    if (ket.same) deg *= 0.5;
+    if (bi == ki) deg *= 0.5;
+    const double* __restrict__ Pa = A.Pa;
+    const double* __restrict__ Pb = A.Pb;
+    int f = 0;
+    for (int ia = 0; ia < NA; ++ia) {
+        const int a = bra.a_off + ia;
+        for (int ib = 0; ib < NB; ++ib) {
+            const int b = bra.b_off + ib;
+            double Pab = Pa[a * N + b];
+            if (UHF) Pab += Pb[a * N + b];
+            double jab = 0.0;
+            for (int ic = 0; ic < NC; ++ic) {
+                const int c = ket.a_off + ic;
+                for (int id = 0; id < ND; ++id, ++f) {
+                    const int d = ket.b_off + id;
+                    double v = double(acc[f]) * (nt.v[la][ia] * nt.v[lb][ib] * nt.v[lc][ic] * nt.v[ld][id]);
+                    if (!(fabs(v) > A.thr_int)) continue;
+                    v *= deg;
+                    double Pcd = Pa[c * N + d];
+                    if (UHF) Pcd += Pb[c * N + d];
+                    jab = fma(v, Pcd, jab);
+                    const double jf = UHF ? 2.0 : 4.0;
+                    atomicAdd(A.Ta + c * N + d, jf * v * Pab);
+                    atomicAdd(A.Ta + a * N + c, -v * Pa[b * N + d]);
+                    atomicAdd(A.Ta + a * N + d, -v * Pa[b * N + c]);
+                    atomicAdd(A.Ta + b * N + c, -v * Pa[a * N + d]);
+                    atomicAdd(A.Ta + b * N + d, -v * Pa[a * N + c]);
+                    if (UHF) {
+                        atomicAdd(A.Tb + c * N + d, jf * v * Pab);
+                        atomicAdd(A.Tb + a * N + c, -v * Pb[b * N + d]);
+                        atomicAdd(A.Tb + a * N + d, -v * Pb[b * N + c]);
+                        atomicAdd(A.Tb + b * N + c, -v * Pb[a * N + d]);
+                        atomicAdd(A.Tb + b * N + d, -v * Pb[a * N + c]);
+                    }
+                }
+            }
+            const double jf = UHF ? 2.0 : 4.0;
+            atomicAdd(A.Ta + a * N + b, jf * jab);
+            if (UHF) atomicAdd(A.Tb + a * N + b, jf * jab);
+        }
+    }
+}
+
+}  // namespace ugb
+
+namespace ugb {
+
+// Schwarz diagonal for the large pair classes (runtime loops, integrals in local memory).
+static __global__ void __launch_bounds__(64) schwarz_generic(const ShellPair* __restrict__ pairs, const PrimPair* __restrict__ prims,
+                                                      int begin, int count, const NormTable nt,
+                                                      const double* __restrict__ rys, double* __restrict__ q_out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const ShellPair sp = pairs[begin + t];
+    const int la = sp.la, lb = sp.lb;
+    const int NA = ncart(la), NB = ncart(lb);
+    const int nr = (2 * la + 2 * lb) / 2 + 1;
+    double acc[GEN_NC * GEN_NC];  // only the diagonal (ab|ab) is needed
+    for (int f = 0; f < NA * NB; ++f) acc[f] = 0.0;
+    const PrimPair* pp = prims + sp.prim_begin;
+    for (int ib = 0; ib < sp.nprim; ++ib) {
+        const double p = pp[ib].p, rp = pp[ib].rp;
+        for (int ik = 0; ik < sp.nprim; ++ik) {
+            const double q = pp[ik].p, rq = pp[ik].rp;
+            const double rpq = 1.0 / (p + q);
+            const double sr = SRTERM * pp[ib].E * pp[ik].E * sqrt(rpq) * pp[ib].cc * pp[ik].cc;
+            double PQ[3], x[5], w[5];
+            for (int k = 0; k < 3; ++k) PQ[k] = pp[ib].P[k] - pp[ik].P[k];
+            const double T = p * q * rpq * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
+            rys_roots_rt<double>(nr, T, rys, x, w);
+            for (int r = 0; r < nr; ++r) {
+                const double fff = x[r] * rpq, B00 = 0.5 * fff;
+                const double B1 = (0.5 - B00 * q) * rp, B1p = (0.5 - B00 * p) * rq;
+                double I[3][GEN_NI];
+                for (int k = 0; k < 3; ++k)
+                    rys_axis_rt<double>(la, lb, la, lb, k == 2 ? w[r] * sr : 1.0, pp[ib].PA[k] - q * fff * PQ[k],
+                                        pp[ik].PA[k] + p * fff * PQ[k], B00, B1, B1p, sp.AB[k], sp.AB[k], I[k]);
+                for (int ia = 0; ia < NA; ++ia)
+                    for (int ibb = 0; ibb < NB; ++ibb) {
+                        const int ix = ((cart_lx(la, ia) * (lb + 1) + cart_lx(lb, ibb)) * (la + 1) + cart_lx(la, ia)) * (lb + 1) + cart_lx(lb, ibb);
+                        const int iy = ((cart_ly(la, ia) * (lb + 1) + cart_ly(lb, ibb)) * (la + 1) + cart_ly(la, ia)) * (lb + 1) + cart_ly(lb, ibb);
+                        const int iz = ((cart_lz(la, ia) * (lb + 1) + cart_lz(lb, ibb)) * (la + 1) + cart_lz(la, ia)) * (lb + 1) + cart_lz(lb, ibb);
+                        acc[ia * NB + ibb] += I[0][ix] * I[1][iy] * I[2][iz];
+                    }
+            }
+        }
+    }
+    double m = 0.0;
+    for (int ia = 0; ia < NA; ++ia)
+        for (int ibb = 0; ibb < NB; ++ibb) {
+            const double n = nt.v[la][ia] * nt.v[lb][ibb];
+            m = fmax(m, fabs(acc[ia * NB + ibb]) * n * n);
+        }
+    q_out[begin + t] = sqrt(m);
+}
+
+}  // namespace ugb

@@ -1,0 +1,198 @@
+"""ctypes binding of the C ABI (include/unomol_gb300.h) and the Python mirror of TwoElectronInts.
+
+The library libunomol_gb300.so is built in-tree by unomol_gb300.build.  There is no CPU fallback:
+loading fails loudly when the library is missing, and every call raises on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .basis import Basis
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libunomol_gb300.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# Exported symbols of include/unomol_gb300.h (checked by the CPU tests).
+EXPORTS = [
+    "unomol_gpu_create", "unomol_gpu_recalculate", "unomol_gpu_fock_rhf", "unomol_gpu_fock_uhf",
+    "unomol_gpu_fock_rhf_device", "unomol_gpu_fock_uhf_device", "unomol_gpu_set_precision",
+    "unomol_gpu_set_screening", "unomol_gpu_set_rys_mode", "unomol_gpu_get_stats", "unomol_gpu_destroy",
+    "unomol_gpu_last_error", "unomol_gpu_version",
+]
+RYS_REFERENCE = 0
+RYS_EXACT = 1
+
+
+class BasisDesc(C.Structure):
+    _fields_ = [("nshell", C.c_int), ("norb", C.c_int), ("ncen", C.c_int),
+                ("shell_l", C.POINTER(C.c_int)), ("shell_nprim", C.POINTER(C.c_int)),
+                ("shell_center", C.POINTER(C.c_int)), ("shell_offset", C.POINTER(C.c_int)),
+                ("alpha", C.POINTER(C.c_double)), ("coef", C.POINTER(C.c_double)),
+                ("centers", C.POINTER(C.c_double))]
+
+
+class Stats(C.Structure):
+    _fields_ = [("shell_quartets", C.c_int64), ("shell_quartets_fp32", C.c_int64),
+                ("shell_quartets_total", C.c_int64), ("function_quartets", C.c_int64),
+                ("primitive_quartets", C.c_int64), ("ms_eri", C.c_double), ("ms_total", C.c_double),
+                ("nbf", C.c_int), ("npairs", C.c_int), ("kernel_launches", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class UnomolError(RuntimeError):
+    pass
+
+
+_LIB = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise UnomolError(f"{LIB_PATH} is missing: build it with `python -m unomol_gb300.build` "
+                          "(the Fock build has no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    L.unomol_gpu_create.argtypes = [C.POINTER(BasisDesc), C.c_int, C.POINTER(C.c_void_p)]
+    L.unomol_gpu_recalculate.argtypes = [C.c_void_p, _dp]
+    L.unomol_gpu_fock_rhf.argtypes = [C.c_void_p, _dp, _dp]
+    L.unomol_gpu_fock_uhf.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+    L.unomol_gpu_fock_rhf_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.unomol_gpu_fock_uhf_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.unomol_gpu_set_precision.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.unomol_gpu_set_screening.argtypes = [C.c_void_p, C.c_double]
+    L.unomol_gpu_set_rys_mode.argtypes = [C.c_void_p, C.c_int]
+    L.unomol_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.unomol_gpu_destroy.argtypes = [C.c_void_p]
+    L.unomol_gpu_destroy.restype = None
+    L.unomol_gpu_last_error.argtypes = [C.c_void_p]
+    L.unomol_gpu_last_error.restype = C.c_char_p
+    L.unomol_gpu_version.restype = C.c_char_p
+    _LIB = L
+    return L
+
+
+def _check(rc: int, h=None):
+    if rc != 0:
+        msg = lib().unomol_gpu_last_error(h).decode(errors="replace")
+        raise UnomolError(f"unomol_gb300 error {rc}: {msg}")
+
+
+def basis_desc(b: Basis):
+    """Keeps the arrays alive together with the descriptor."""
+    keep = {
+        "l": np.ascontiguousarray(b.shell_l, np.int32), "np": np.ascontiguousarray(b.shell_nprim, np.int32),
+        "c": np.ascontiguousarray(b.shell_center, np.int32), "o": np.ascontiguousarray(b.shell_offset, np.int32),
+        "a": np.ascontiguousarray(b.alpha, np.float64), "k": np.ascontiguousarray(b.coef, np.float64),
+        "x": np.ascontiguousarray(b.centers, np.float64).reshape(-1),
+    }
+    ip = C.POINTER(C.c_int)
+    dp = C.POINTER(C.c_double)
+    d = BasisDesc(b.nshell, b.norb, b.ncen, keep["l"].ctypes.data_as(ip), keep["np"].ctypes.data_as(ip),
+                  keep["c"].ctypes.data_as(ip), keep["o"].ctypes.data_as(ip), keep["a"].ctypes.data_as(dp),
+                  keep["k"].ctypes.data_as(dp), keep["x"].ctypes.data_as(dp))
+    return d, keep
+
+
+class TwoElectronInts:
+    """GPU drop-in for unomol::TwoElectronInts (TwoElectronInts.hpp:79-110).
+
+    The constructor sets up shell pairs and Schwarz bounds on the GPU (the reference computes and
+    stores every integral there); formGmatrix recomputes the integrals and contracts them into G,
+    adding into the caller's array as the reference does.
+    """
+
+    def __init__(self, basis: Basis, start_shell: int = 0, label: str = "MINTS.DAT"):
+        self.basis = basis
+        self.start = start_shell
+        self.label = label  # kept for interface parity; nothing is stored
+        self._h = C.c_void_p()
+        d, self._keep = basis_desc(basis)
+        _check(lib().unomol_gpu_create(C.byref(d), int(start_shell), C.byref(self._h)))
+
+    def recalculate(self, basis: Basis):
+        """TwoElectronInts::recalculate (centre moved)."""
+        self.basis = basis
+        _check(lib().unomol_gpu_recalculate(self._h, np.ascontiguousarray(basis.centers, np.float64).reshape(-1)), self._h)
+
+    def formGmatrix(self, *args):
+        """formGmatrix(P, G) (RHF) or formGmatrix(Pa, Pb, Ga, Gb) (UHF); G arrays are added into."""
+        if len(args) == 2:
+            P, G = args
+            _check(lib().unomol_gpu_fock_rhf(self._h, _c(P), _out(G)), self._h)
+        elif len(args) == 4:
+            Pa, Pb, Ga, Gb = args
+            _check(lib().unomol_gpu_fock_uhf(self._h, _c(Pa), _c(Pb), _out(Ga), _out(Gb)), self._h)
+        else:
+            raise TypeError("formGmatrix(P, G) or formGmatrix(Pa, Pb, Ga, Gb)")
+
+    def directFormGMatrix(self, P, G, basis: Basis | None = None):
+        """The reference's direct variant (TwoElectronInts.cpp:871-1055) has a lossy pair cut; here it
+        is the same exact direct build as formGmatrix."""
+        self.formGmatrix(P, G)
+
+    def form_g(self, P) -> np.ndarray:
+        G = np.zeros(self.basis.no2)
+        self.formGmatrix(np.ascontiguousarray(P, np.float64), G)
+        return G
+
+    def form_g_uhf(self, Pa, Pb):
+        Ga = np.zeros(self.basis.no2)
+        Gb = np.zeros(self.basis.no2)
+        self.formGmatrix(np.ascontiguousarray(Pa, np.float64), np.ascontiguousarray(Pb, np.float64), Ga, Gb)
+        return Ga, Gb
+
+    def fock_device(self, dP_ptr: int, dG_ptr: int, stream: int = 0):
+        _check(lib().unomol_gpu_fock_rhf_device(self._h, C.c_void_p(dP_ptr), C.c_void_p(dG_ptr), C.c_void_p(stream)), self._h)
+
+    def fock_device_uhf(self, dPa, dPb, dGa, dGb, stream: int = 0):
+        _check(lib().unomol_gpu_fock_uhf_device(self._h, C.c_void_p(dPa), C.c_void_p(dPb), C.c_void_p(dGa),
+                                                C.c_void_p(dGb), C.c_void_p(stream)), self._h)
+
+    def set_precision(self, mode: int, fp32_cutoff: float = 1e-10):
+        _check(lib().unomol_gpu_set_precision(self._h, int(mode), float(fp32_cutoff)), self._h)
+
+    def set_rys_mode(self, mode: int):
+        """RYS_REFERENCE (default, the reference's two-root fit) or RYS_EXACT (exact quadrature)."""
+        _check(lib().unomol_gpu_set_rys_mode(self._h, int(mode)), self._h)
+
+    def set_screening(self, cutoff: float):
+        _check(lib().unomol_gpu_set_screening(self._h, float(cutoff)), self._h)
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(lib().unomol_gpu_get_stats(self._h, C.byref(s)), self._h)
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().unomol_gpu_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _c(a):
+    a = np.asarray(a)
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a
+
+
+def _out(a):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("G must be a C-contiguous float64 numpy array (it is added into)")
+    return a
