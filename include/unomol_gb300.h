@@ -71,6 +71,11 @@ typedef struct UnomolStats {
     int nbf;                       /* basis functions */
     int npairs;                    /* shell pairs kept */
     int kernel_launches;           /* kernels launched by the last build */
+    int pad_;
+    /* filled only while counting is on (unomol_gpu_set_counting): */
+    int64_t primitive_quartets_computed; /* primitive quartets past the 1e-12 prefactor cut */
+    double eri_flops;              /* algorithmic flops of the ERI + J/K kernels (FMA = 2), see DESIGN */
+    double eri_flops_fp32;         /* of which in the FP32 kernels (mixed mode) */
 } UnomolStats;
 
 /* TwoElectronInts(basis, start_shell, label) -- TwoElectronInts.hpp:83-88.
@@ -116,6 +121,20 @@ int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode);
 int unomol_gpu_set_screening(UnomolCtx* ctx, double schwarz_cutoff);
 
 int unomol_gpu_get_stats(const UnomolCtx* ctx, UnomolStats* out);
+
+/* Work counting for throughput figures (no reference counterpart): while on, every Fock build counts
+ * the primitive quartets its kernels evaluate and fills the counting fields of UnomolStats; the build
+ * then synchronises its stream before returning. */
+int unomol_gpu_set_counting(UnomolCtx* ctx, int on);
+
+/* Device time of the last Fock build, from CUDA events recorded on the build's stream (no reference
+ * counterpart): ms_eri covers the ERI + J/K kernels, ms_total the whole build.  Waits for the build. */
+int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total);
+
+/* FMA throughput of the current device (no reference counterpart): TFLOP/s of a dependent-chain FMA
+ * kernel over every SM, FP64 (fp64 = 1) or FP32 (fp64 = 0).  The roofline denominator of the Fock
+ * kernels, which are bound by the FP64 (or FP32) pipe. */
+int unomol_gpu_fma_peak(int fp64, double* tflops);
 
 void unomol_gpu_destroy(UnomolCtx* ctx);
 

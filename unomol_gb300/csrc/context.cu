@@ -64,11 +64,12 @@ struct UnomolCtx {
     int *d_soff = nullptr, *d_sl = nullptr;
     int* d_status = nullptr;
     unsigned long long* d_counters = nullptr;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // options
     double schwarz_cut = STORE_CUT;
     int prec_mode = UNOMOL_PREC_FP64;
     int rys_mode = UNOMOL_RYS_REFERENCE;
+    int counting = 0;
     double fp32_cut = 1e-10;
     UnomolStats stats{};
     std::string err;
@@ -152,6 +153,29 @@ void build_pair(UnomolCtx* ctx, int ish, int jsh, ShellPair& sp, std::vector<Pri
     }
     sp.nprim = (int)prims.size() - sp.prim_begin;
     sp.q = 0.0;
+}
+
+// Algorithmic flops of the Rys kernels (FMA = 2, every +,-,*,/,sqrt = 1), counted from the steps of
+// fock_kernels.cuh.  Per primitive quartet past the prefactor cut: setup 20; Rys nodes and weights
+// NR * (2 polynomials * 13 Horner steps * 2) + 3; per root 10 for B00, B1, B1', then per axis 4 for
+// C, C', the 2D recurrence, the two horizontal transfers (2 per step), and 3 per function quartet for
+// the product and accumulation.  Per shell quartet: 17 per function quartet for normalisation and the
+// six density contractions.
+double flops_per_prim(int la, int lb, int lc, int ld) {
+    const int L12 = la + lb, L34 = lc + ld, NR = (L12 + L34) / 2 + 1;
+    const int NF = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
+    double vrr = 0;
+    if (L12 > 0) vrr += 1;
+    for (int i = 1; i < L12; ++i) vrr += 4;
+    for (int j = 0; j < L34; ++j)
+        for (int i = 0; i <= L12; ++i) vrr += 1 + (j > 0 ? 3 : 0) + (i > 0 ? 3 : 0);
+    double hrr = 0;
+    for (int b = 1; b <= lb; ++b) hrr += 2.0 * (L12 - b + 1) * (L34 + 1);
+    for (int d = 1; d <= ld; ++d) hrr += 2.0 * (la + 1) * (lb + 1) * (L34 - d + 1);
+    return 20 + NR * 52.0 + 3 + NR * (10 + 3 * (4 + vrr + hrr) + 3.0 * NF);
+}
+double flops_per_quartet(int la, int lb, int lc, int ld) {
+    return 17.0 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
 }
 
 void free_setup(UnomolCtx* c) {
@@ -434,11 +458,19 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         CU(cudaGetLastError());
         ++launches;
     }
+    const int ncls = NPAIRCLASS * NPAIRCLASS;
+    A.counters = nullptr;
+    if (ctx->counting) {
+        if (!ctx->d_counters) CU(cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 2 * ncls * 32));
+        CU(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 2 * ncls * 32, s));
+        A.counters = ctx->d_counters;
+    }
     for (const ClassLaunch& L : ctx->launches) {
         A.bps = ctx->d_bps + L.bp_begin;
         A.prefix = ctx->d_prefix;
         A.nbp = L.nbp;
         A.nwork = L.nwork;
+        A.counter_base = (L.bc * NPAIRCLASS + L.kc) * 32;  // FP32 launches use the second half
         if (!mixed) {
             A.mode = 0;
             CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
@@ -447,6 +479,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             A.mode = 1;
             CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
             A.mode = 2;
+            A.counter_base += ncls * 32;
             CU(launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s));
             launches += 2;
         }
@@ -458,20 +491,41 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         fold_packed<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(ctx->d_Tb, dGb, n);
         ++launches;
     }
+    CU(cudaEventRecord(ctx->ev[3], s));
     CU(cudaGetLastError());
     ctx->stats.kernel_launches = launches;
+    if (ctx->counting) {
+        std::vector<unsigned long long> c(2 * ncls * 32);
+        CU(cudaMemcpyAsync(c.data(), ctx->d_counters, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        int64_t prims = 0;
+        double fl = 0.0, fl32 = 0.0;
+        for (const ClassLaunch& L : ctx->launches) {
+            const int cls = L.bc * NPAIRCLASS + L.kc;
+            const int la = pc_la(L.bc), lb = pc_lb(L.bc), lc = pc_la(L.kc), ld = pc_lb(L.kc);
+            for (int half = 0; half < 2; ++half) {
+                unsigned long long n = 0;
+                for (int k = 0; k < 32; ++k) n += c[(half * ncls + cls) * 32 + k];
+                prims += (int64_t)n;
+                const double f = (double)n * flops_per_prim(la, lb, lc, ld);
+                if (half) fl32 += f; else fl += f;
+            }
+            // quartet-level work: all quartets of the class (both halves together in mixed mode)
+            fl += (double)L.quartets * flops_per_quartet(la, lb, lc, ld);
+        }
+        ctx->stats.primitive_quartets_computed = prims;
+        ctx->stats.eri_flops = fl + fl32;
+        ctx->stats.eri_flops_fp32 = fl32;
+    }
     return UNOMOL_OK;
 }
 
 int finish_timing(UnomolCtx* ctx, cudaStream_t s) {
-    cudaEvent_t e3;
-    CU(cudaEventCreate(&e3));
-    CU(cudaEventRecord(e3, s));
-    CU(cudaEventSynchronize(e3));
+    (void)s;
+    CU(cudaEventSynchronize(ctx->ev[3]));
     float ms_eri = 0.f, ms_tot = 0.f;
     CU(cudaEventElapsedTime(&ms_eri, ctx->ev[1], ctx->ev[2]));
-    CU(cudaEventElapsedTime(&ms_tot, ctx->ev[0], e3));
-    cudaEventDestroy(e3);
+    CU(cudaEventElapsedTime(&ms_tot, ctx->ev[0], ctx->ev[3]));
     ctx->stats.ms_eri = ms_eri;
     ctx->stats.ms_total = ms_tot;
     return UNOMOL_OK;
@@ -593,6 +647,21 @@ int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode) {
     return UNOMOL_OK;
 }
 
+int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total) {
+    if (!ctx || !ms_eri || !ms_total) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    int rc = finish_timing(ctx, ctx->stream);
+    if (rc) return rc;
+    *ms_eri = ctx->stats.ms_eri;
+    *ms_total = ctx->stats.ms_total;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_set_counting(UnomolCtx* ctx, int on) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    ctx->counting = on ? 1 : 0;
+    return UNOMOL_OK;
+}
+
 int unomol_gpu_get_stats(const UnomolCtx* ctx, UnomolStats* out) {
     if (!ctx || !out) return UNOMOL_EINVAL;
     *out = ctx->stats;
@@ -622,6 +691,7 @@ int unomol_gpu_fock_rhf(UnomolCtx* ctx, const double* P, double* G) {
     rc = fock_device(ctx, ctx->d_pk_a, nullptr, ctx->d_Ga, nullptr, ctx->stream);
     if (rc) return rc;
     CU(cudaMemcpyAsync(G, ctx->d_Ga, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));  // G is the caller's host array: wait for the copy back
     return finish_timing(ctx, ctx->stream);
 }
 
@@ -638,6 +708,7 @@ int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, doub
     if (rc) return rc;
     CU(cudaMemcpyAsync(Ga, ctx->d_Ga, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaMemcpyAsync(Gb, ctx->d_Gb, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));  // G is the caller's host array: wait for the copy back
     return finish_timing(ctx, ctx->stream);
 }
 

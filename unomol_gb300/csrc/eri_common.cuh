@@ -89,7 +89,8 @@ struct FockArgs {
     int mode;                   // 0 all quartets; 1 only "large" (FP64 part); 2 only "small" (FP32 part)
     int nshell;
     int rys_compat;             // reference-compatible two-root Rys regime (FP64 only)
-    unsigned long long* counters;  // [0] quartets evaluated
+    unsigned long long* counters;  // optional: primitive quartets past the prefactor cut, 32 slots per launch
+    int counter_base;           // first slot of this launch (class id * 32)
     int* status;                // device error flag
 };
 

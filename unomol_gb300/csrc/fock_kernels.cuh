@@ -164,7 +164,7 @@ template <int LA, int LB, int LC, int LD, typename R, typename PP>
 __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const ShellPair& ket,
                                                   const PP* __restrict__ prims,
                                                   const R* __restrict__ rys, R prim_cut, bool compat,
-                                                  R (&acc)[QClass<LA, LB, LC, LD>::NF]) {
+                                                  R (&acc)[QClass<LA, LB, LC, LD>::NF], unsigned* npass = nullptr) {
     using Q = QClass<LA, LB, LC, LD>;
     constexpr int NR = Q::NR;
 #pragma unroll
@@ -184,6 +184,7 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
             R sr = R(SRTERM) * Eab * Ecd * sqrt(rpq);
             if (sr < prim_cut) continue;  // TwoElectronInts.cpp:478-479 (before the coefficients)
             sr *= cab * ccd;
+            if (npass) ++*npass;
             const R QCx = pk[ik].PA[0], QCy = pk[ik].PA[1], QCz = pk[ik].PA[2];
             const R PQx = Px - R(pk[ik].P[0]), PQy = Py - R(pk[ik].P[1]), PQz = Pz - R(pk[ik].P[2]);
             const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
@@ -363,12 +364,25 @@ struct NormTable {
     double v[LMAX + 1][6];
 };
 
+// Optional work counter: primitive quartets past the prefactor cut, summed over the converged lanes of
+// the warp and added to one of 32 slots of the launch (spread to avoid a hot address).
+__device__ __forceinline__ void count_flush(const FockArgs& A, unsigned v) {
+    const unsigned m = __activemask();
+    const unsigned s = __reduce_add_sync(m, v);
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1 && s)
+        atomicAdd(A.counters + A.counter_base + (blockIdx.x & 31), (unsigned long long)s);
+}
+
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
     using Q = QClass<LA, LB, LC, LD>;
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bi, ki;
-    if (!decode_work(A, g, bi, ki)) return;
+    unsigned npass = 0;
+    if (!decode_work(A, g, bi, ki)) {
+        if (A.counters) count_flush(A, 0u);
+        return;
+    }
     const ShellPair bra = A.pairs[bi];
     const ShellPair ket = A.pairs[ki];
     if (A.mode != 0) {
@@ -382,10 +396,13 @@ __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const No
     }
     R acc[Q::NF];
     if constexpr (sizeof(R) == 8)
-        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.rys_compat != 0, acc);
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.rys_compat != 0, acc,
+                                                       A.counters ? &npass : nullptr);
     else
-        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, R(A.prim_cut), false, acc);
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, R(A.prim_cut), false, acc,
+                                                         A.counters ? &npass : nullptr);
     digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt.v);
+    if (A.counters) count_flush(A, npass);
 }
 
 // Schwarz diagonal: q[pair] = sqrt(max_{a,b} |(ab|ab)|) for every pair of one class (no primitive
@@ -473,6 +490,7 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
                                                       const PP* __restrict__ prims, int la, int lb, int lc, int ld) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bi, ki;
+    unsigned npass = 0;
     if (!decode_work(A, g, bi, ki)) return;
     const ShellPair bra = A.pairs[bi];
     const ShellPair ket = A.pairs[ki];
@@ -496,6 +514,7 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
             R sr = R(SRTERM) * Eab * Ecd * sqrt(rpq);
             if (sr < prim_cut) continue;
             sr *= cab * ccd;
+            ++npass;
             R PQ[3], x[5], w[5];
             for (int k = 0; k < 3; ++k) PQ[k] = R(pb[ib].P[k]) - R(pk[ik].P[k]);
             const R T = p * q * rpq * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
@@ -572,6 +591,7 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
             if (UHF) atomicAdd(A.Tb + a * N + b, jf * jab);
         }
     }
+    if (A.counters) count_flush(A, npass);
 }
 
 }  // namespace ugb

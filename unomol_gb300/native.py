@@ -22,7 +22,8 @@ EXPORTS = [
     "unomol_gpu_create", "unomol_gpu_recalculate", "unomol_gpu_fock_rhf", "unomol_gpu_fock_uhf",
     "unomol_gpu_fock_rhf_device", "unomol_gpu_fock_uhf_device", "unomol_gpu_set_precision",
     "unomol_gpu_set_screening", "unomol_gpu_set_rys_mode", "unomol_gpu_get_stats", "unomol_gpu_destroy",
-    "unomol_gpu_last_error", "unomol_gpu_version",
+    "unomol_gpu_last_error", "unomol_gpu_version", "unomol_gpu_set_counting", "unomol_gpu_fma_peak",
+    "unomol_gpu_last_build_ms",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -40,7 +41,9 @@ class Stats(C.Structure):
     _fields_ = [("shell_quartets", C.c_int64), ("shell_quartets_fp32", C.c_int64),
                 ("shell_quartets_total", C.c_int64), ("function_quartets", C.c_int64),
                 ("primitive_quartets", C.c_int64), ("ms_eri", C.c_double), ("ms_total", C.c_double),
-                ("nbf", C.c_int), ("npairs", C.c_int), ("kernel_launches", C.c_int)]
+                ("nbf", C.c_int), ("npairs", C.c_int), ("kernel_launches", C.c_int), ("pad_", C.c_int),
+                ("primitive_quartets_computed", C.c_int64), ("eri_flops", C.c_double),
+                ("eri_flops_fp32", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -71,6 +74,9 @@ def lib() -> C.CDLL:
     L.unomol_gpu_set_precision.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.unomol_gpu_set_screening.argtypes = [C.c_void_p, C.c_double]
     L.unomol_gpu_set_rys_mode.argtypes = [C.c_void_p, C.c_int]
+    L.unomol_gpu_set_counting.argtypes = [C.c_void_p, C.c_int]
+    L.unomol_gpu_last_build_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.unomol_gpu_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.unomol_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.unomol_gpu_destroy.argtypes = [C.c_void_p]
     L.unomol_gpu_destroy.restype = None
@@ -165,6 +171,15 @@ class TwoElectronInts:
         """RYS_REFERENCE (default, the reference's two-root fit) or RYS_EXACT (exact quadrature)."""
         _check(lib().unomol_gpu_set_rys_mode(self._h, int(mode)), self._h)
 
+    def last_build_ms(self):
+        """(ms of the ERI + J/K kernels, ms of the whole build) of the last build, device events."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().unomol_gpu_last_build_ms(self._h, C.byref(a), C.byref(b)), self._h)
+        return a.value, b.value
+
+    def set_counting(self, on: bool):
+        _check(lib().unomol_gpu_set_counting(self._h, 1 if on else 0), self._h)
+
     def set_screening(self, cutoff: float):
         _check(lib().unomol_gpu_set_screening(self._h, float(cutoff)), self._h)
 
@@ -183,6 +198,13 @@ class TwoElectronInts:
             self.close()
         except Exception:
             pass
+
+
+def fma_peak(fp64: bool = True) -> float:
+    """TFLOP/s of the FP64 (or FP32) FMA pipe of the current device (library microbenchmark)."""
+    v = C.c_double()
+    _check(lib().unomol_gpu_fma_peak(1 if fp64 else 0, C.byref(v)))
+    return v.value
 
 
 def _c(a):
