@@ -122,7 +122,7 @@ def patin_text(atoms, basis: str, charge: int = 0, maxits: int = 300, eps: float
     for e, x in atoms:
         out.append(f"{float(Z[e.upper()]):15.10f}" + "".join(f"{v / BOHR:20.12f}" for v in x))
     for l, prims, c in shells:
-        out.append(f"{len(prims):3d}{l:3d}{c:3d}")
+        out.append(f"{len(prims):4d}{l:4d}{c:6d}")  # whitespace separated for any centre index
         for a, cc in prims:
             out.append(f"{a:20.10f}{cc:20.10f}")
     return "\n".join(out) + "\n"
