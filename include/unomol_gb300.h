@@ -136,6 +136,19 @@ int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total);
  * kernels, which are bound by the FP64 (or FP32) pipe. */
 int unomol_gpu_fma_peak(int fp64, double* tflops);
 
+/* Allocation-free RHF Fock build.  No counterpart in the reference (its Fock build runs on the host).
+ * Same contract as unomol_gpu_fock_rhf_device (device pointers, packed P in, packed G added into,
+ * NULL stream = the context's stream), for callers that must not trigger cudaMalloc once they run:
+ * a host framework that owns every device allocation after start-up, or an iteration loop that must
+ * not take cudaMalloc's implicit device synchronisation.  Create the context during start-up; this
+ * call then allocates nothing: its per-build scratch (dense P and the N x N accumulator) lives in a
+ * 16 MiB static device array of the library, which every GPU that loads the library's kernels holds
+ * until exit.  Limits: at most 1024 basis functions (larger bases return UNOMOL_EINVAL with a
+ * message) and the FP64 precision mode only.  The first call on a device looks up the array's device
+ * address; make that first call before any stream capture.  Every call shares the one array, so calls
+ * that overlap on the GPU (other streams, other host threads) race; serialise them. */
+int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, double* dG, void* stream);
+
 void unomol_gpu_destroy(UnomolCtx* ctx);
 
 /* Last error of this context (ctx may be NULL for errors raised before a context existed). */

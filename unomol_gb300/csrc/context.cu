@@ -9,6 +9,7 @@
 // launch one kernel per quartet class, fold G += T + T^T into packed storage.
 #include <algorithm>
 #include <memory>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -738,3 +739,88 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free RHF Fock build.
+//
+// The regular build keeps its per-build scratch (the dense copy of P and the N x N accumulator T) in
+// device buffers that it allocates on first use.  Some callers cannot let a library call cudaMalloc
+// once they are running: a host framework that owns every device allocation after start-up (fixed
+// budget, its own pool), or an iteration loop that must not take cudaMalloc's implicit device
+// synchronisation.  For them this build keeps that scratch in one file-scope device array instead.
+// The array is part of the library's device image, so every GPU on which the library's kernels are
+// loaded holds it (NOALLOC_SCRATCH_BYTES) until the process exits.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int NOALLOC_MAX_NBF = 1024;  // largest basis the static scratch holds
+constexpr size_t NOALLOC_SCRATCH_DOUBLES = 2ull * NOALLOC_MAX_NBF * NOALLOC_MAX_NBF;  // 16 MiB
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};  // device address of the array, per device
+std::mutex g_noalloc_mu;
+
+}  // namespace
+
+extern "C" int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, double* dG, void* stream) {
+    if (!ctx || !dP || !dG) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    const int n = ctx->nbf;
+    if (n > NOALLOC_MAX_NBF)
+        return fail(ctx, UNOMOL_EINVAL,
+                    "unomol_gpu_fock_rhf_noalloc: " + std::to_string(n) + " basis functions exceed the " +
+                        std::to_string(NOALLOC_MAX_NBF) + " that its static scratch holds");
+    if (ctx->prec_mode != UNOMOL_PREC_FP64)
+        return fail(ctx, UNOMOL_EINVAL, "unomol_gpu_fock_rhf_noalloc runs the FP64 build only");
+    int dev = -1;
+    CU(cudaGetDevice(&dev));
+    if (dev != ctx->dev) return fail(ctx, UNOMOL_EINVAL, "unomol_gpu_fock_rhf_noalloc: current device is not the context's");
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(ctx, UNOMOL_EINVAL, "device index out of range");
+    double* scratch = nullptr;
+    {
+        // once per device, with that device current: the host-side name of the array is only a
+        // stand-in, the kernels need its device address
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess)
+                return fail(ctx, UNOMOL_ECUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+            g_noalloc_ptr[dev] = static_cast<double*>(p);
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    const long long n2 = (long long)n * n, np = (long long)n * (n + 1) / 2;
+    double* Pfull = scratch;
+    double* T = scratch + n2;
+    expand_packed<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(dP, Pfull, n);
+    CU(cudaGetLastError());
+    CU(cudaMemsetAsync(T, 0, n2 * sizeof(double), s));  // the array keeps the previous call's sums
+    FockArgs A{};
+    A.pairs = ctx->d_pairs;
+    A.prims = ctx->d_prims;
+    A.prims32 = ctx->d_prims32;
+    A.nbf = n;
+    A.Pa = Pfull;
+    A.Pb = nullptr;
+    A.Ta = T;
+    A.Tb = nullptr;
+    A.thr_int = STORE_CUT;
+    A.prim_cut = PRIM_CUT;
+    A.nshell = ctx->nshell;
+    A.rys_compat = ctx->rys_mode == UNOMOL_RYS_REFERENCE;
+    A.counters = nullptr;
+    A.mode = 0;
+    for (const ClassLaunch& L : ctx->launches) {
+        A.bps = ctx->d_bps + L.bp_begin;
+        A.prefix = ctx->d_prefix;
+        A.nbp = L.nbp;
+        A.nwork = L.nwork;
+        CU(launch_fock_fp64(L.bc, L.kc, false, A, ctx->nt, ctx->d_rys, s));
+    }
+    fold_packed<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(T, dG, n);
+    CU(cudaGetLastError());
+    return UNOMOL_OK;
+}
