@@ -151,6 +151,53 @@ int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, double* dG, vo
 
 void unomol_gpu_destroy(UnomolCtx* ctx);
 
+/* ---- SCF layer (the callers of the Fock build) ---- */
+
+/* One-electron integrals S, T and H = T + V, packed (the data of OneElectronInts, OneElectronInts.cpp:
+ * 6-202; computed on the host).  charges: [ncen] nuclear charges. */
+int unomol_one_electron(const UnomolBasisDesc* basis, const double* charges, double* S, double* T, double* H);
+
+typedef struct UnomolScfInput {
+    int norb;            /* basis functions */
+    int nelec;           /* electrons: even -> RHF, odd -> UHF (Unomol.cc:13-24) */
+    double nucrep;       /* nuclear repulsion energy */
+    const double* S;     /* packed overlap */
+    const double* H;     /* packed core Hamiltonian */
+} UnomolScfInput;
+
+#define UNOMOL_SCF_DAMPED 0 /* the reference's averaging (RHF.hpp:536-569); flag 1 behaves the same */
+#define UNOMOL_SCF_DIIS 2   /* Pulay DIIS on F (new) */
+
+typedef struct UnomolScfOptions {
+    int maxits;          /* iteration cap (patin.dat maxits) */
+    double eps;          /* convergence threshold (Basis::scf_eps) */
+    int conv_type;       /* scf_flag[0]: 0 energy, 1 density, 2 both (RHF.hpp:390-402) */
+    int accel;           /* UNOMOL_SCF_DAMPED or UNOMOL_SCF_DIIS */
+    int guess;           /* 0 core Hamiltonian (RHF.hpp:205-211), 1 the P passed in (PMATRIX.DAT form) */
+    int diis_size;       /* DIIS subspace (default 8) */
+    double diis_tol;     /* DIIS: max |X^T (FPS - SPF) X| at convergence */
+} UnomolScfOptions;
+
+typedef struct UnomolScfResult {
+    int status;
+    char message[256];
+    double energy;        /* final total energy (electronic + nuclear repulsion) */
+    double e_electronic;
+    double init_energy;   /* energy of the first iteration (short.gs.out line 1) */
+    double ediff, pdiff, diis_error;
+    double seconds;       /* wall time of the SCF */
+    int iterations, converged, fock_builds;
+    double* energies;     /* optional [energies_cap]: total energy after every update */
+    int energies_cap;
+} UnomolScfResult;
+
+/* SCF on the GPU: the loop of RestrictedHartreeFock / UnRestrictedHartreeFock::findEnergy (RHF.hpp:
+ * 114-176, UHF.hpp:137-177) with every Fock build on this context and the FP64 linear algebra in
+ * cuSOLVER (syevd) / cuBLAS.  P_io: [no2] (RHF) or [2*no2] (UHF: Pa then Pb) -- the guess when
+ * options->guess == 1, the final density on return.  orbital_energies: optional [norb] (UHF: 2*norb). */
+int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* input, const UnomolScfOptions* options, UnomolScfResult* result,
+               double* P_io, double* orbital_energies);
+
 /* Last error of this context (ctx may be NULL for errors raised before a context existed). */
 const char* unomol_gpu_last_error(const UnomolCtx* ctx);
 

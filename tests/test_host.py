@@ -1,0 +1,111 @@
+"""CPU tests of the host side: library exports, basis reader, one-electron integrals, molecules."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, basis_of, golden_cases, load_golden
+
+
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "unomol_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(unomol_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from unomol_gb300 import native
+    L = native.lib()
+    syms = _header_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(L, s), f"{s} declared in include/unomol_gb300.h but not exported"
+    for s in native.EXPORTS:
+        assert s in syms
+
+
+def test_version_string():
+    from unomol_gb300 import native
+    assert b"sm_103a" in native.lib().unomol_gpu_version()
+
+
+def test_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from unomol_gb300 import native
+    g = load_golden("h2o_sto3g_c0")
+    with pytest.raises(native.UnomolError, match="no CUDA device"):
+        native.TwoElectronInts(basis_of(g))
+
+
+def test_bad_basis_rejected_before_device_use():
+    from unomol_gb300 import native
+    L = native.lib()
+    L.unomol_gpu_create.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    h = C.c_void_p()
+    assert L.unomol_gpu_create(None, 0, C.byref(h)) == -1
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_one_electron_matches_reference(name):
+    from unomol_gb300 import native
+    g = load_golden(name)
+    S, T, H = native.one_electron(basis_of(g))
+    assert np.abs(S - g["S"]).max() < 1e-12
+    assert np.abs(T - g["T"]).max() < 1e-12
+    assert np.abs(H - g["H"]).max() < 1e-12
+
+
+def test_basis_reader_normalisation_matches_reference_export():
+    """Shell::normalize restated (Basis.hpp:56-75): coefficients within 2 ulp of the reference's."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refh
+    if not refh.available():
+        pytest.skip("reference build not present (oracle/_ref)")
+    from unomol_gb300.basis import Basis
+    for tag in ("631.h2o", "dh95.co2", "3g.ch4"):
+        path = f"/root/reference/test/patin.dat.{tag}"
+        rb = refh.RefBasis(path)
+        info, a, c, cen = rb.export()
+        b = Basis(path)
+        assert np.abs(b.coef - c).max() <= 4 * np.finfo(float).eps * np.abs(c).max()
+        assert (np.array(b.shell_offset) == info[:, 3]).all()
+
+
+def test_molecule_generators():
+    from unomol_gb300 import molecules
+    from unomol_gb300.basis import Basis
+    dec = molecules.alkane(10)
+    assert len(dec) == 32
+    C = np.array([x for e, x in dec if e == "C"])
+    H = np.array([x for e, x in dec if e == "H"])
+    d = np.linalg.norm(C[1:] - C[:-1], axis=1)
+    assert np.allclose(d, 1.54)
+    # every H at 1.09 A from its nearest carbon, every angle at a carbon 109.47 deg
+    for h in H:
+        assert abs(np.min(np.linalg.norm(C - h, axis=1)) - 1.09) < 1e-9
+    for i, c in enumerate(C):
+        nb = [x for x in np.vstack([C, H]) if 0.1 < np.linalg.norm(x - c) < 1.6]
+        assert len(nb) == 4
+        for a in range(4):
+            for bb in range(a):
+                u, v = nb[a] - c, nb[bb] - c
+                ang = np.degrees(np.arccos(u @ v / np.linalg.norm(u) / np.linalg.norm(v)))
+                assert abs(ang - 109.47) < 0.01  # a tetrahedron's angle is 109.4712 deg
+    b = Basis(text=molecules.patin_text(dec, "6-31G"))
+    assert b.norb == 134 and b.nshell == 94
+    w = molecules.water_cluster(32, 0)
+    O = np.array([x for e, x in w if e == "O"])
+    dm = np.linalg.norm(O[:, None] - O[None], axis=2) + np.eye(32) * 10
+    assert dm.min() >= 2.7 and O.min() >= 0 and O.max() <= 10.0 + 1.0
+    b = Basis(text=molecules.patin_text(w, "6-31G"))
+    assert b.norb == 416 and b.nshell == 288
+
+
+def test_oracle_port_builds_without_reference():
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

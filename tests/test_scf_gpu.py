@@ -1,0 +1,65 @@
+"""SCF energies on the GPU (unomol_scf) against the reference's own RHF/UHF runs (golden fixtures).
+
+Parity mode: the reference's damped loop (RHF.hpp / UHF.hpp) with the reference-compatible Rys mode and
+the reference's own S and H; the final total energy must agree within 1e-10 Eh with the stock
+reference run (and with the published energy of test/scfout.dat.* where there is one).  The exact Rys
+mode is checked against the reference with an exact two-root quadrature, and the library's own
+one-electron integrals against the fixture S and H.
+"""
+import numpy as np
+import pytest
+
+from conftest import basis_of, golden_cases, load_golden
+
+TOL_E = 1e-10
+SCF_CASES = [c for c in golden_cases() if "scf_energy" in load_golden(c)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", SCF_CASES)
+def test_scf_energy_parity(gpu, name):
+    from unomol_gb300 import native
+    g = load_golden(name)
+    b = basis_of(g)
+    t = native.TwoElectronInts(b)
+    r = native.scf(t, b, S=g["S"], H=g["H"])
+    assert abs(r["energy"] - float(g["scf_energy"])) <= TOL_E, (r["energy"], float(g["scf_energy"]), r["iterations"])
+    if "golden_energy" in g:
+        assert abs(r["energy"] - float(g["golden_energy"])) <= TOL_E
+    assert abs(r["init_energy"] - float(g["scf_init_energy"])) <= 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_631g", "ref_631_co", "ref_431_n2", "propane_cation_sto3g", "ref_dh95_h2"])
+def test_scf_energy_exact_mode(gpu, name):
+    from unomol_gb300 import native
+    g = load_golden(name)
+    b = basis_of(g)
+    t = native.TwoElectronInts(b)
+    t.set_rys_mode(native.RYS_EXACT)
+    r = native.scf(t, b, S=g["S"], H=g["H"])
+    assert abs(r["energy"] - float(g["scf_energy_exact"])) <= TOL_E
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_sto3g_c0", "ref_631_h2o", "ref_n_dhdz", "water3_631g"])
+def test_scf_with_own_one_electron(gpu, name):
+    from unomol_gb300 import native
+    g = load_golden(name)
+    b = basis_of(g)
+    t = native.TwoElectronInts(b)
+    r = native.scf(t, b)  # S, H from unomol_one_electron
+    assert abs(r["energy"] - float(g["scf_energy"])) <= TOL_E
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_631g", "ethane_631g", "ref_b_dhdz", "propane_cation_sto3g"])
+def test_diis_reaches_same_energy(gpu, name):
+    """DIIS (new accelerator) converges to the same SCF solution as the reference's damped loop."""
+    from unomol_gb300 import native
+    g = load_golden(name)
+    b = basis_of(g)
+    t = native.TwoElectronInts(b)
+    r = native.scf(t, b, S=g["S"], H=g["H"], accel=native.SCF_DIIS, eps=1e-12, diis_tol=1e-8)
+    assert r["converged"]
+    assert abs(r["energy"] - float(g["scf_energy"])) <= 1e-9

@@ -22,7 +22,7 @@ OBJDIR = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-DUGB_MAX_PAIRCLASS=6",
                   "-I" + os.path.join(ROOT, "include")]
-UNITS = ["fock_fp64.cu", "fock_fp32.cu", "context.cu", "peak.cu"]
+UNITS = ["fock_fp64.cu", "fock_fp32.cu", "context.cu", "peak.cu", "scf.cu", "one_electron.cpp"]
 
 
 def nvcc() -> str:
@@ -34,7 +34,7 @@ def nvcc() -> str:
 
 def _compile(unit: str) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(OBJDIR, unit.replace(".cu", ".o"))
+    obj = os.path.join(OBJDIR, os.path.splitext(unit)[0] + ".o")
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".inc", ".h"))]
     deps.append(os.path.join(ROOT, "include", "unomol_gb300.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):

@@ -1,0 +1,455 @@
+// SCF driver on the GPU: the loop of RestrictedHartreeFock / UnRestrictedHartreeFock::findEnergy
+// (RHF.hpp:114-176, UHF.hpp:137-177) with every Fock build on the GPU and the linear algebra in FP64
+// on the GPU (cuSOLVER syevd for S^{-1/2} and the Fock eigenproblem, cuBLAS for X^T F X, C and P).
+//
+// Parity mode (accel 0/1) follows the reference step by step: update() (RHF.hpp:87-112), the damping
+// of scf_converger() (RHF.hpp:536-569; the "Anderson" branch is dead in the serial reference because
+// `extrap` stays 0, so only the averaging runs), is_converged() on the signed ediff and/or pdiff
+// (RHF.hpp:390-402), canonical X = U s^{-1/2} (RHF.hpp:214-233) and the core-Hamiltonian guess
+// (RHF.hpp:205-211).  DIIS (accel 2) is new: Pulay extrapolation of F on the orthonormal-basis error
+// X^T (F P S - S P F) X, for systems on which the damped loop oscillates.
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/unomol_gb300.h"
+
+namespace {
+
+struct Dev {
+    int n = 0;
+    cudaStream_t s = nullptr;
+    cublasHandle_t cb = nullptr;
+    cusolverDnHandle_t cs = nullptr;
+    double *X = nullptr, *F = nullptr, *W = nullptr, *C = nullptr, *T1 = nullptr, *ev = nullptr, *work = nullptr;
+    int* info = nullptr;
+    int lwork = 0;
+    std::string err;
+    ~Dev() {
+        for (double* p : {X, F, W, C, T1, ev, work})
+            if (p) cudaFree(p);
+        if (info) cudaFree(info);
+        if (cb) cublasDestroy(cb);
+        if (cs) cusolverDnDestroy(cs);
+    }
+};
+
+#define CK(call, code)                                                         \
+    do {                                                                       \
+        if ((call) != 0) {                                                     \
+            d.err = std::string(#call) + " failed";                            \
+            return code;                                                       \
+        }                                                                      \
+    } while (0)
+
+int dev_init(Dev& d, int n, cudaStream_t s) {
+    d.n = n;
+    d.s = s;
+    const size_t n2 = (size_t)n * n * sizeof(double);
+    CK(cublasCreate(&d.cb), UNOMOL_ECUDA);
+    CK(cublasSetStream(d.cb, s), UNOMOL_ECUDA);
+    CK(cusolverDnCreate(&d.cs), UNOMOL_ECUDA);
+    CK(cusolverDnSetStream(d.cs, s), UNOMOL_ECUDA);
+    for (double** p : {&d.X, &d.F, &d.W, &d.C, &d.T1}) CK(cudaMalloc(p, n2), UNOMOL_ENOMEM);
+    CK(cudaMalloc(&d.ev, n * sizeof(double)), UNOMOL_ENOMEM);
+    CK(cudaMalloc(&d.info, sizeof(int)), UNOMOL_ENOMEM);
+    CK(cusolverDnDsyevd_bufferSize(d.cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, d.F, n, d.ev, &d.lwork), UNOMOL_ECUDA);
+    CK(cudaMalloc(&d.work, (size_t)d.lwork * sizeof(double)), UNOMOL_ENOMEM);
+    return UNOMOL_OK;
+}
+
+// symmetric eigen-decomposition of A (n x n, in place -> eigenvectors in columns), eigenvalues in ev
+int syevd(Dev& d, double* A) {
+    CK(cusolverDnDsyevd(d.cs, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d.n, A, d.n, d.ev, d.work, d.lwork, d.info),
+       UNOMOL_ECUDA);
+    int info = 0;
+    CK(cudaMemcpyAsync(&info, d.info, sizeof(int), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    if (info != 0) {
+        d.err = "syevd did not converge (info " + std::to_string(info) + ")";
+        return UNOMOL_ESCF;
+    }
+    return UNOMOL_OK;
+}
+
+__global__ void k_unpack(const double* __restrict__ pk, double* __restrict__ full, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    const int i = (int)(t / n), j = (int)(t % n);
+    const int hi = i > j ? i : j, lo = i > j ? j : i;
+    full[t] = pk[(long long)hi * (hi + 1) / 2 + lo];
+}
+__global__ void k_pack(const double* __restrict__ full, double* __restrict__ pk, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long np = (long long)n * (n + 1) / 2;
+    if (t >= np) return;
+    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)i * (i + 1) / 2 > t) --i;
+    while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+    const int j = (int)(t - (long long)i * (i + 1) / 2);
+    pk[t] = full[(long long)j * n + i];  // column-major (symmetric: either)
+}
+// X[:, j] = U[:, j] * sv[j]  (column-major)
+__global__ void k_scale_cols(const double* __restrict__ U, const double* __restrict__ sv, double* __restrict__ X, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    X[t] = U[t] * sv[t / n];
+}
+
+unsigned blocks(long long n) { return (unsigned)((n + 255) / 256); }
+
+// packed trace of SymmPack::TraceSymmPackProduct (SymmPack.cpp:7-18): sum_{i>j} 2 a b + sum_i a b
+double trace_packed(const std::vector<double>& a, const std::vector<double>& b, int n) {
+    double sum = 0.0;
+    size_t ij = 0;
+    for (int i = 0; i < n; ++ij, ++i) {
+        for (int j = 0; j < i; ++ij, ++j) sum += a[ij] * b[ij];
+        sum += 0.5 * a[ij] * b[ij];
+    }
+    return sum + sum;
+}
+// SymmPack::SymmPackDiffNorm (SymmPack.cpp:20-36)
+double diffnorm_packed(const std::vector<double>& a, const std::vector<double>& b, int n) {
+    double sum = 0.0;
+    size_t ij = 0;
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < i; ++ij, ++j) {
+            double t = a[ij] - b[ij];
+            sum += t * t;
+        }
+        double t = a[ij] - b[ij];
+        sum += 0.5 * t * t;
+        ++ij;
+    }
+    sum += sum;
+    return std::sqrt(sum) / n;
+}
+
+// X = U s^{-1/2} from the overlap (RHF.hpp:214-233)
+int form_x(Dev& d, const std::vector<double>& S, double* d_pk) {
+    const int n = d.n;
+    CK(cudaMemcpyAsync(d_pk, S.data(), S.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, d.F, n);
+    int rc = syevd(d, d.F);
+    if (rc) return rc;
+    std::vector<double> ev(n);
+    CK(cudaMemcpy(ev.data(), d.ev, n * sizeof(double), cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
+    for (int i = 0; i < n; ++i) {
+        double f = ev[i];
+        if (std::fabs(f) < 1.e-7 && f < 0.0) f = -f;
+        if (f == 0.0) { d.err = "Zero Eigenvalue in Overlap Matrix"; return UNOMOL_ESCF; }
+        if (f < 0.0) { d.err = "Negative Eigenvalue in Overlap Matrix"; return UNOMOL_ESCF; }
+        ev[i] = 1.0 / std::sqrt(f);
+    }
+    CK(cudaMemcpy(d.ev, ev.data(), n * sizeof(double), cudaMemcpyHostToDevice), UNOMOL_ECUDA);
+    k_scale_cols<<<blocks((long long)n * n), 256, 0, d.s>>>(d.F, d.ev, d.X, n);
+    return UNOMOL_OK;
+}
+
+// F (packed, host) -> eigenvalues and C = X W on the device, then P = C_occ C_occ^T packed (host)
+int diag_density(Dev& d, const std::vector<double>& Fpk, double* d_pk, int nocc, std::vector<double>& P,
+                 std::vector<double>& evals, std::vector<double>* Cout) {
+    const int n = d.n;
+    const double one = 1.0, zero = 0.0;
+    CK(cudaMemcpyAsync(d_pk, Fpk.data(), Fpk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, d.F, n);
+    // T1 = F X ; W = X^T T1
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.F, n, d.X, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, d.X, n, d.T1, n, &zero, d.W, n), UNOMOL_ECUDA);
+    int rc = syevd(d, d.W);
+    if (rc) return rc;
+    evals.resize(n);
+    CK(cudaMemcpyAsync(evals.data(), d.ev, n * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    // C = X W
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.X, n, d.W, n, &zero, d.C, n), UNOMOL_ECUDA);
+    // P = C_occ C_occ^T
+    if (nocc > 0)
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &one, d.C, n, d.C, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    else
+        CK(cudaMemsetAsync(d.T1, 0, (size_t)n * n * sizeof(double), d.s), UNOMOL_ECUDA);
+    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(d.T1, d_pk, n);
+    P.resize((size_t)n * (n + 1) / 2);
+    CK(cudaMemcpyAsync(P.data(), d_pk, P.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    if (Cout) {
+        Cout->resize((size_t)n * n);
+        CK(cudaMemcpyAsync(Cout->data(), d.C, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    }
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    return UNOMOL_OK;
+}
+
+// ---- DIIS (Pulay) on the packed Fock matrices ----
+struct Diis {
+    int maxv = 8;
+    std::vector<std::vector<double>> F, E;
+    void push(const std::vector<double>& f, const std::vector<double>& e) {
+        if ((int)F.size() == maxv) {
+            F.erase(F.begin());
+            E.erase(E.begin());
+        }
+        F.push_back(f);
+        E.push_back(e);
+    }
+    bool extrapolate(std::vector<double>& out) {
+        const int m = (int)F.size();
+        if (m < 2) return false;
+        std::vector<double> B((m + 1) * (m + 1), 0.0), rhs(m + 1, 0.0);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j <= i; ++j) {
+                double s = 0.0;
+                for (size_t k = 0; k < E[i].size(); ++k) s += E[i][k] * E[j][k];
+                B[i * (m + 1) + j] = B[j * (m + 1) + i] = s;
+            }
+        for (int i = 0; i < m; ++i) B[i * (m + 1) + m] = B[m * (m + 1) + i] = -1.0;
+        rhs[m] = -1.0;
+        // Gaussian elimination with partial pivoting
+        const int N = m + 1;
+        std::vector<int> piv(N);
+        for (int c = 0; c < N; ++c) {
+            int p = c;
+            for (int r = c + 1; r < N; ++r)
+                if (std::fabs(B[r * N + c]) > std::fabs(B[p * N + c])) p = r;
+            if (std::fabs(B[p * N + c]) < 1e-300) return false;
+            if (p != c) {
+                for (int k = 0; k < N; ++k) std::swap(B[c * N + k], B[p * N + k]);
+                std::swap(rhs[c], rhs[p]);
+            }
+            for (int r = c + 1; r < N; ++r) {
+                const double f = B[r * N + c] / B[c * N + c];
+                for (int k = c; k < N; ++k) B[r * N + k] -= f * B[c * N + k];
+                rhs[r] -= f * rhs[c];
+            }
+        }
+        std::vector<double> x(N);
+        for (int r = N - 1; r >= 0; --r) {
+            double s = rhs[r];
+            for (int k = r + 1; k < N; ++k) s -= B[r * N + k] * x[k];
+            x[r] = s / B[r * N + r];
+        }
+        out.assign(F[0].size(), 0.0);
+        for (int i = 0; i < m; ++i)
+            for (size_t k = 0; k < out.size(); ++k) out[k] += x[i] * F[i][k];
+        return true;
+    }
+};
+
+// Error vector X^T (F P S - S P F) X, packed (antisymmetric: strict lower triangle is enough)
+int diis_error(Dev& d, const std::vector<double>& Fpk, const std::vector<double>& Ppk, const double* d_S,
+               double* d_pk, std::vector<double>& err) {
+    const int n = d.n;
+    const double one = 1.0, zero = 0.0, mone = -1.0;
+    double *dF = d.F, *dP = d.W, *t = d.T1, *u = d.C;  // W and C are free between diagonalisations
+    CK(cudaMemcpyAsync(d_pk, Fpk.data(), Fpk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, dF, n);
+    CK(cudaMemcpyAsync(d_pk, Ppk.data(), Ppk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, dP, n);
+    // t = F P ; u = t S = F P S ; u -= (F P S)^T  (S P F = (F P S)^T)
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, dF, n, dP, n, &zero, t, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, t, n, d_S, n, &zero, u, n), UNOMOL_ECUDA);
+    CK(cublasDgeam(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, &one, u, n, &mone, u, n, t, n), UNOMOL_ECUDA);
+    // u = X^T t X
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, t, n, d.X, n, &zero, dP, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, d.X, n, dP, n, &zero, u, n), UNOMOL_ECUDA);
+    std::vector<double> full((size_t)n * n);
+    CK(cudaMemcpyAsync(full.data(), u, full.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    err.resize((size_t)n * (n - 1) / 2);
+    size_t k = 0;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j) err[k++] = full[(size_t)j * n + i];
+    return UNOMOL_OK;
+}
+
+double maxabs(const std::vector<double>& v) {
+    double m = 0.0;
+    for (double x : v) m = std::max(m, std::fabs(x));
+    return m;
+}
+
+}  // namespace
+
+extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const UnomolScfOptions* opt, UnomolScfResult* res,
+                          double* P_io, double* orbital_energies) {
+    if (!ctx || !in || !opt || !res || !P_io || !in->S || !in->H) return UNOMOL_EINVAL;
+    const int n = in->norb;
+    const size_t no2 = (size_t)n * (n + 1) / 2;
+    const bool uhf = in->nelec % 2 != 0;
+    const int noccA = uhf ? in->nelec - in->nelec / 2 : in->nelec / 2;
+    const int noccB = in->nelec / 2;
+    auto t0 = std::chrono::steady_clock::now();
+    Dev d;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return UNOMOL_ECUDA;
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
+    } sg{s};
+    int rc = dev_init(d, n, s);
+    double *d_pk = nullptr, *d_P = nullptr, *d_G = nullptr, *d_Pb = nullptr, *d_Gb = nullptr, *d_S = nullptr;
+    struct Bufs {
+        double** p[6];
+        ~Bufs() { for (auto q : p) if (*q) cudaFree(*q); }
+    } bufs{{&d_pk, &d_P, &d_G, &d_Pb, &d_Gb, &d_S}};
+    auto fail = [&](int code) {
+        res->status = code;
+        std::snprintf(res->message, sizeof(res->message), "%s", d.err.c_str());
+        return code;
+    };
+    if (rc) return fail(rc);
+    if (cudaMalloc(&d_pk, no2 * sizeof(double)) || cudaMalloc(&d_P, no2 * sizeof(double)) ||
+        cudaMalloc(&d_G, no2 * sizeof(double)) || cudaMalloc(&d_Pb, no2 * sizeof(double)) ||
+        cudaMalloc(&d_Gb, no2 * sizeof(double)) || cudaMalloc(&d_S, (size_t)n * n * sizeof(double))) {
+        d.err = "device allocation failed";
+        return fail(UNOMOL_ENOMEM);
+    }
+    std::vector<double> S(in->S, in->S + no2), H(in->H, in->H + no2);
+    rc = form_x(d, S, d_pk);
+    if (rc) return fail(rc);
+    cudaMemcpyAsync(d_pk, S.data(), no2 * sizeof(double), cudaMemcpyHostToDevice, s);
+    k_unpack<<<blocks((long long)n * n), 256, 0, s>>>(d_pk, d_S, n);
+    std::vector<double> Pa(no2), Pb(no2), Ga(no2), Gb(no2), Fa(no2), Fb(no2), PoldA(no2), PoldB(no2), PoldA2(no2),
+        PoldB2(no2), evA, evB, tmp;
+    // guess: caller's P (RHF.hpp:120-123) or core Hamiltonian (RHF.hpp:205-211; UHF.hpp:487-496)
+    if (opt->guess == 1) {
+        std::memcpy(Pa.data(), P_io, no2 * sizeof(double));
+        if (uhf) std::memcpy(Pb.data(), P_io + no2, no2 * sizeof(double));
+    } else {
+        rc = diag_density(d, H, d_pk, noccA, Pa, evA, nullptr);
+        if (rc) return fail(rc);
+        if (uhf) {
+            rc = diag_density(d, H, d_pk, noccB, Pb, evB, nullptr);
+            if (rc) return fail(rc);
+        }
+    }
+    const int maxits = opt->maxits > 0 ? opt->maxits : 300;
+    const double eps = opt->eps;
+    const int cflag = opt->conv_type;
+    double eold = 0.0, energy = 0.0, ediff = 10.0, pdiff = 10.0, init_energy = 0.0;
+    int iteration = 0, builds = 0;
+    Diis diisA, diisB;
+    diisA.maxv = diisB.maxv = opt->diis_size > 1 ? opt->diis_size : 8;
+    double diis_err = 0.0;
+    // update(): RHF.hpp:87-112 / UHF.hpp:101-134
+    auto update = [&]() -> int {
+        std::fill(Ga.begin(), Ga.end(), 0.0);
+        cudaMemcpyAsync(d_P, Pa.data(), no2 * sizeof(double), cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(d_G, 0, no2 * sizeof(double), s);
+        int r;
+        if (!uhf) {
+            r = unomol_gpu_fock_rhf_device(ctx, d_P, d_G, s);
+        } else {
+            cudaMemcpyAsync(d_Pb, Pb.data(), no2 * sizeof(double), cudaMemcpyHostToDevice, s);
+            cudaMemsetAsync(d_Gb, 0, no2 * sizeof(double), s);
+            r = unomol_gpu_fock_uhf_device(ctx, d_P, d_Pb, d_G, d_Gb, s);
+        }
+        if (r) {
+            d.err = unomol_gpu_last_error(ctx);
+            return r;
+        }
+        ++builds;
+        cudaMemcpyAsync(Ga.data(), d_G, no2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (uhf) cudaMemcpyAsync(Gb.data(), d_Gb, no2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            d.err = "Fock build failed on the device";
+            return UNOMOL_ECUDA;
+        }
+        if (!uhf) {
+            energy = 2.0 * trace_packed(Pa, H, n) + trace_packed(Pa, Ga, n);
+        } else {
+            energy = trace_packed(Pa, H, n) + trace_packed(Pb, H, n) + 0.5 * (trace_packed(Pa, Ga, n) + trace_packed(Pb, Gb, n));
+        }
+        ediff = energy - eold;
+        eold = energy;
+        for (size_t k = 0; k < no2; ++k) Fa[k] = H[k] + Ga[k];
+        if (uhf)
+            for (size_t k = 0; k < no2; ++k) Fb[k] = H[k] + Gb[k];
+        if (opt->accel == 2) {  // DIIS on F
+            std::vector<double> e;
+            r = diis_error(d, Fa, Pa, d_S, d_pk, e);
+            if (r) return r;
+            diis_err = maxabs(e);
+            diisA.push(Fa, e);
+            diisA.extrapolate(Fa);
+            if (uhf) {
+                r = diis_error(d, Fb, Pb, d_S, d_pk, e);
+                if (r) return r;
+                diis_err = std::max(diis_err, maxabs(e));
+                diisB.push(Fb, e);
+                diisB.extrapolate(Fb);
+            }
+        }
+        PoldA2 = PoldA;
+        PoldA = Pa;
+        r = diag_density(d, Fa, d_pk, noccA, Pa, evA, nullptr);
+        if (r) return r;
+        pdiff = diffnorm_packed(Pa, PoldA, n);
+        if (uhf) {
+            PoldB2 = PoldB;
+            PoldB = Pb;
+            r = diag_density(d, Fb, d_pk, noccB, Pb, evB, nullptr);
+            if (r) return r;
+            pdiff += diffnorm_packed(Pb, PoldB, n);
+        }
+        if (res->energies && iteration < res->energies_cap) res->energies[iteration] = energy + in->nucrep;
+        ++iteration;
+        return UNOMOL_OK;
+    };
+    // scf_converger(): RHF.hpp:536-569 (averaging; skipped when the energy went down)
+    auto converger = [&]() {
+        if (opt->accel == 2) return;
+        if (ediff < 0.0) return;
+        for (size_t k = 0; k < no2; ++k) Pa[k] = (Pa[k] + PoldA[k]) * 0.5;
+        if (uhf)
+            for (size_t k = 0; k < no2; ++k) Pb[k] = (Pb[k] + PoldB[k]) * 0.5;
+    };
+    // is_converged(): RHF.hpp:390-402 (signed ediff); DIIS: |ediff| < eps and max|error| < diis_tol
+    auto converged = [&]() {
+        if (opt->accel == 2) return std::fabs(ediff) < eps && diis_err < opt->diis_tol;
+        switch (cflag) {
+            case 0: return ediff < eps;
+            case 1: return pdiff < eps;
+            default: return pdiff < eps && ediff < eps;
+        }
+    };
+    eold = 0.0;
+    if ((rc = update())) return fail(rc);
+    init_energy = energy + in->nucrep;
+    iteration = 1;
+    if (uhf) eold = 0.0;  // UHF.hpp:158-160 resets eold before the second update, RHF does not
+    if ((rc = update())) return fail(rc);
+    iteration = 2;
+    bool conv = false;
+    while (iteration < maxits) {
+        converger();
+        if ((rc = update())) return fail(rc);
+        if (converged()) {
+            conv = true;
+            break;
+        }
+    }
+    std::memcpy(P_io, Pa.data(), no2 * sizeof(double));
+    if (uhf) std::memcpy(P_io + no2, Pb.data(), no2 * sizeof(double));
+    if (orbital_energies) {
+        std::memcpy(orbital_energies, evA.data(), n * sizeof(double));
+        if (uhf) std::memcpy(orbital_energies + n, evB.data(), n * sizeof(double));
+    }
+    res->status = UNOMOL_OK;
+    res->message[0] = 0;
+    res->energy = energy + in->nucrep;
+    res->e_electronic = energy;
+    res->init_energy = init_energy;
+    res->ediff = ediff;
+    res->pdiff = pdiff;
+    res->iterations = iteration;
+    res->converged = conv ? 1 : 0;
+    res->fock_builds = builds;
+    res->diis_error = diis_err;
+    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return UNOMOL_OK;
+}

@@ -200,6 +200,76 @@ class TwoElectronInts:
             pass
 
 
+class ScfInput(C.Structure):
+    _fields_ = [("norb", C.c_int), ("nelec", C.c_int), ("nucrep", C.c_double),
+                ("S", C.POINTER(C.c_double)), ("H", C.POINTER(C.c_double))]
+
+
+class ScfOptions(C.Structure):
+    _fields_ = [("maxits", C.c_int), ("eps", C.c_double), ("conv_type", C.c_int), ("accel", C.c_int),
+                ("guess", C.c_int), ("diis_size", C.c_int), ("diis_tol", C.c_double)]
+
+
+class ScfResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("message", C.c_char * 256), ("energy", C.c_double),
+                ("e_electronic", C.c_double), ("init_energy", C.c_double), ("ediff", C.c_double),
+                ("pdiff", C.c_double), ("diis_error", C.c_double), ("seconds", C.c_double),
+                ("iterations", C.c_int), ("converged", C.c_int), ("fock_builds", C.c_int),
+                ("energies", C.POINTER(C.c_double)), ("energies_cap", C.c_int)]
+
+
+SCF_DAMPED = 0
+SCF_DIIS = 2
+
+
+def one_electron(b: Basis):
+    """S, T, H (packed) of the basis: unomol_one_electron (host code of the library)."""
+    L = lib()
+    L.unomol_one_electron.argtypes = [C.POINTER(BasisDesc), _dp, _dp, _dp, _dp]
+    d, keep = basis_desc(b)
+    S, T, H = np.zeros(b.no2), np.zeros(b.no2), np.zeros(b.no2)
+    _check(L.unomol_one_electron(C.byref(d), np.ascontiguousarray(b.charges, np.float64), S, T, H))
+    return S, T, H
+
+
+def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPED, guess_P=None,
+        maxits: int | None = None, eps: float | None = None, conv_type: int | None = None,
+        diis_size: int = 8, diis_tol: float = 1e-6, record: int = 0):
+    """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ..."""
+    L = lib()
+    L.unomol_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.POINTER(ScfOptions), C.POINTER(ScfResult),
+                             _dp, C.c_void_p]
+    if S is None or H is None:
+        S, _, H = one_electron(b)
+    S = np.ascontiguousarray(S, np.float64)
+    H = np.ascontiguousarray(H, np.float64)
+    dp = C.POINTER(C.c_double)
+    inp = ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), S.ctypes.data_as(dp), H.ctypes.data_as(dp))
+    opt = ScfOptions(maxits if maxits is not None else b.maxits, eps if eps is not None else b.eps,
+                     conv_type if conv_type is not None else b.scf_flag[0], accel, 0 if guess_P is None else 1,
+                     diis_size, diis_tol)
+    uhf = b.nelec % 2 == 1
+    P = np.zeros(b.no2 * (2 if uhf else 1))
+    if guess_P is not None:
+        P[:] = guess_P
+    eps_orb = np.zeros(b.norb * (2 if uhf else 1))
+    res = ScfResult()
+    energies = np.zeros(max(record, 1))
+    if record:
+        res.energies = energies.ctypes.data_as(dp)
+        res.energies_cap = record
+    rc = L.unomol_scf(ctx._h, C.byref(inp), C.byref(opt), C.byref(res), P, eps_orb.ctypes.data)
+    if rc != 0:
+        raise UnomolError(f"unomol_scf error {rc}: {res.message.decode(errors='replace')}")
+    out = {k: getattr(res, k) for k in ("energy", "e_electronic", "init_energy", "ediff", "pdiff", "diis_error",
+                                        "seconds", "iterations", "converged", "fock_builds")}
+    out["P"] = P
+    out["orbital_energies"] = eps_orb
+    if record:
+        out["energies"] = energies[:min(record, res.iterations)].copy()
+    return out
+
+
 def fma_peak(fp64: bool = True) -> float:
     """TFLOP/s of the FP64 (or FP32) FMA pipe of the current device (library microbenchmark)."""
     v = C.c_double()
