@@ -1,23 +1,30 @@
 #!/usr/bin/env python
 """Benchmark of the direct two-electron Fock build on the 32-water 6-31G cluster.
 
-One step = one Fock build G(P) (RHF, packed P in, packed G out) of a cluster of 32 rigid waters in
-6-31G (416 basis functions; oxygens uniform in a 10 A cube with O-O >= 2.7 A, random orientations,
-numpy default_rng(0)), the precision workload of the reference's headline metric.  Synthetic data:
-the geometry is generated, the density is a fixed synthetic symmetric matrix (RHF form P = C C^T of
-random orthonormal occupied orbitals, 160 doubly occupied), since the reference measures on no public
-dataset.
+Workload: 32 rigid waters in 6-31G (416 basis functions; oxygens uniform in a 10 A cube with O-O >= 2.7 A,
+random orientations, numpy default_rng(0)), RHF -- the precision workload on which the reference's
+headline metric is quoted.  Synthetic data: the geometry is generated (there is no public dataset).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|mixed] [--impl ours|reference]
+Untimed set-up: one-electron integrals, the superposition-of-fragments guess, and two SCFs to
+convergence (DIIS, 1e-10 Eh): the plain FP64 path (full FP64 builds) and the precision form
+(incremental builds G(P_k) = G(P_k-1) + G(P_k - P_k-1), FP32 for quartets with Schwarz bound x max|dP|
+below the cutoff, full rebuild every 8 builds).  Their energy difference is |dE|.
 
-value: Fock builds/s with P and G resident in HBM (device entry point), device time from CUDA events
-on the build's stream, L2 flushed (256 MiB write) between timed builds.  e2e: the same metric through
-the host entry point (unomol_gpu_fock_rhf: pinned host P in, host G out, copies inside the timing).
-roofline: the ERI + J/K kernels (every class instance of the launch) against the FP64 FMA peak measured
-by the library's own microbenchmark (the kernels are bound by the FP64 pipe, not by HBM or tensor
-cores).  cpu_baseline: the C restatement of the reference algorithm (oracle/) on the host cores, on a
-strided sample of the shell quartets.  --impl reference: that CPU implementation as the reference arm.
-Multi-GPU: replicas only (every rank builds its own Fock matrix; value sums over ranks).
+One step = one Fock build of the precision form's own SCF sequence (the k-th build: full density at
+k = 0, 8, ..., else the density change), cycled for K steps.
+  value    Fock builds/s, P and G resident in HBM, device time from CUDA events on the build's stream,
+           L2 flushed (256 MiB write) before every timed build;
+  e2e      the same builds through the host entry point (unomol_gpu_fock_rhf: pinned host P and G in,
+           G out, copies inside the timing);
+  plain_fp64   the plain FP64 path on the same densities (full builds), device-timed the same way;
+  roofline the ERI + J/K kernels of one build against the FP64 and FP32 FMA peaks measured by the
+           library's own microbenchmark (the kernels are bound by those pipes, not by HBM or tensor
+           cores): peak = flops / (flops64/peak64 + flops32/peak32);
+  cpu_baseline the C restatement of the reference algorithm (oracle/) on the host cores, on a strided
+           sample of the shell quartets of one full build.
+--impl reference: that CPU implementation as the reference arm (same metric and workload).
+--form fp64: the plain FP64 path as the measured form.
+Multi-GPU: replicas only (every rank runs the whole workload; value sums over ranks).
 """
 from __future__ import annotations
 
@@ -34,29 +41,22 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Fock builds/sec (32-water 6-31G RHF Fock build)"
+METRIC = "Fock builds/sec (32-water 6-31G RHF SCF Fock builds)"
 UNIT = "Fock builds/s"
-WORKLOAD = "32-water cluster, 6-31G, RHF Fock build G(P), 416 basis functions (seed 0)"
+WORKLOAD = "32-water cluster, 6-31G, RHF, 416 basis functions (seed 0): Fock builds of the converging SCF"
 CPU_STRIDE = 64
+FP32_CUTOFF = 1e-4
+REBUILD = 8
 
 
-def workload():
+def basis():
     from unomol_gb300 import molecules
     from unomol_gb300.basis import Basis
-    b = Basis(text=molecules.patin_text(molecules.water_cluster(32, 0), "6-31G"))
-    n, nocc = b.norb, b.nelec // 2
-    rng = np.random.default_rng(1234)
-    q, _ = np.linalg.qr(rng.normal(size=(n, nocc)))
-    C = q * 0.9
-    P = C @ C.T
-    return b, np.ascontiguousarray(P[np.tril_indices(n)])
+    return Basis(text=molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10))
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
 class Clocks:
@@ -103,8 +103,13 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def ensure_oracle():
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_build", "libunomol_oracle.so")):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+
+
 def cpu_port_rate(b, P, stride, threads):
-    """Fock builds/s of the C restatement on a 1/stride sample (extrapolated)."""
+    """Fock builds/s of the C restatement on a 1/stride sample of one full build (extrapolated)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import orc
     t0 = time.perf_counter()
@@ -113,10 +118,11 @@ def cpu_port_rate(b, P, stride, threads):
     return 1.0 / (dt * stride), dt
 
 
-def ensure_oracle():
-    lib = os.path.join(ROOT, "oracle", "_build", "libunomol_oracle.so")
-    if not os.path.exists(lib):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+def synthetic_density(b):
+    n, nocc = b.norb, b.nelec // 2
+    q, _ = np.linalg.qr(np.random.default_rng(1234).normal(size=(n, nocc)))
+    P = 0.81 * q @ q.T
+    return np.ascontiguousarray(P[np.tril_indices(n)])
 
 
 def run_reference(args):
@@ -124,20 +130,22 @@ def run_reference(args):
     if rank != 0:
         return 0
     ensure_oracle()
-    b, P = workload()
+    b = basis()
+    P = synthetic_density(b)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_port_rate(b, P, CPU_STRIDE * 4, threads)
     times = []
     for _ in range(args.steps):
-        r, dt = cpu_port_rate(b, P, CPU_STRIDE, threads)
+        _, dt = cpu_port_rate(b, P, CPU_STRIDE, threads)
         times.append(dt * CPU_STRIDE)
     value = len(times) / sum(times)
-    sample = f"every {CPU_STRIDE}th canonical shell quartet per step ({100.0 / CPU_STRIDE:.2f}% of the build), extrapolated"
+    sample = (f"C restatement of the reference algorithm (full FP64 build), every {CPU_STRIDE}th canonical shell "
+              f"quartet per step ({100.0 / CPU_STRIDE:.2f}% of a build), extrapolated")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "form": "reference algorithm (C restatement), FP64"},
+            "config": {"workload": WORKLOAD, "form": "reference algorithm (CPU), full FP64 builds"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -145,7 +153,6 @@ def run_reference(args):
 
 
 def profile_traffic(form):
-    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", f"fock_{form}_water32_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
@@ -153,84 +160,141 @@ def profile_traffic(form):
     return None
 
 
+def step_inputs(dens):
+    """Per build of the sequence: (is_full, density or density change), rebuilding every REBUILD builds."""
+    out = []
+    for k, D in enumerate(dens):
+        if k % REBUILD == 0:
+            out.append((True, D))
+        else:
+            out.append((False, D - dens[k - 1]))
+    return out
+
+
+def timed_builds(ctx, inputs, steps, dev, stream, flush):
+    """Device-resident builds: per step an L2 flush, then the build between two events."""
+    import torch
+    sp = stream.cuda_stream
+    dIn = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for _, x in inputs]
+    dG = torch.zeros_like(dIn[0])
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    eri = []
+    for k in range(steps):
+        full, _ = inputs[k % len(inputs)]
+        flush.fill_(k & 0xFF)
+        if full:
+            dG.zero_()
+        ev[k][0].record(stream)
+        ctx.fock_device(dIn[k % len(inputs)].data_ptr(), dG.data_ptr(), sp)
+        ev[k][1].record(stream)
+        eri.append(ctx.last_build_ms()[0])
+    torch.cuda.synchronize(dev)
+    return [a.elapsed_time(b_) for a, b_ in ev], eri
+
+
+def counted_flops(ctx, inputs, dev, stream):
+    """Algorithmic flops (FP64, FP32) and launches of every build of the sequence (untimed)."""
+    import torch
+    ctx.set_counting(True)
+    dG = None
+    f64, f32, launches, q32, q = [], [], [], [], []
+    for full, x in inputs:
+        dx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+        if full or dG is None:
+            dG = torch.zeros_like(dx)
+        ctx.fock_device(dx.data_ptr(), dG.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        st = ctx.stats()
+        f64.append(st["eri_flops"] - st["eri_flops_fp32"])
+        f32.append(st["eri_flops_fp32"])
+        launches.append(st["kernel_launches"])
+        q.append(st["shell_quartets"])
+        q32.append(st["shell_quartets_fp32"])
+    ctx.set_counting(False)
+    return f64, f32, launches, q, q32
+
+
 def run_ours(args):
     import torch
+
+    from unomol_gb300 import guess, native
     ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    from unomol_gb300 import native
-    b, P = workload()
-    ctx = native.TwoElectronInts(b)
-    if args.form == "mixed":
-        ctx.set_precision(native.PREC_MIXED, args.fp32_cutoff)
-    # a dedicated stream: the library maps a NULL stream handle to its own context stream, so the
-    # builds and the timing events must share a non-default torch stream
-    stream = torch.cuda.Stream(dev)
+    stream = torch.cuda.Stream(dev)  # non-default: a NULL handle would mean the library's own stream
     torch.cuda.set_stream(stream)
-    sp = stream.cuda_stream
-    assert sp != 0
-    dP = torch.from_numpy(P).to(dev)
-    dG = torch.zeros_like(dP)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(args.warmup):
-        dG.zero_()
-        ctx.fock_device(dP.data_ptr(), dG.data_ptr(), sp)
+    b = basis()
+    S, T, H = native.one_electron(b)
+    t0 = time.perf_counter()
+    P0 = guess.fragment_density(b)
+    t_guess = time.perf_counter() - t0
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, maxits=100, eps=1e-10, diis_tol=1e-7, guess_P=P0, keep_densities=64)
+    plain = native.TwoElectronInts(b)
+    r64 = native.scf(plain, b, **kw)
+    mixed = native.TwoElectronInts(b)
+    if args.form == "mixed":
+        mixed.set_precision(native.PREC_MIXED, args.fp32_cutoff)
+        mixed.set_density_screening(1e-12)
+        rm = native.scf(mixed, b, incremental=True, rebuild_every=REBUILD, **kw)
+        inputs = step_inputs(rm["densities"])
+    else:
+        rm = r64
+        inputs = [(True, D) for D in r64["densities"]]
     if args.profile:
-        # profiling mode (for ncu): `steps` device builds after the warm-up, nothing else
-        for _ in range(args.steps):
-            dG.zero_()
-            ctx.fock_device(dP.data_ptr(), dG.data_ptr(), sp)
+        dG = torch.zeros(b.no2, dtype=torch.float64, device=dev)
+        for k in range(args.warmup + args.steps):
+            full, x = inputs[k % len(inputs)]
+            dx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+            if full:
+                dG.zero_()
+            mixed.fock_device(dx.data_ptr(), dG.data_ptr(), stream.cuda_stream)
         torch.cuda.synchronize(dev)
-        print(json.dumps({"profile_builds": args.steps, "form": args.form}), flush=True)
+        print(json.dumps({"profile_builds": args.warmup + args.steps, "form": args.form}), flush=True)
         return 0
-    # one counted build (untimed) for the algorithmic flops of the ERI kernels
-    ctx.set_counting(True)
-    dG.zero_()
-    ctx.fock_device(dP.data_ptr(), dG.data_ptr(), sp)
-    torch.cuda.synchronize(dev)
-    st = ctx.stats()
-    ctx.set_counting(False)
-    launches_per_build = st["kernel_launches"]
-    # timed region: K builds, L2 flushed before each
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    # warm-up, then the counted (untimed) pass for the algorithmic flops
+    timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
+    f64, f32, launches, nq, nq32 = counted_flops(mixed, inputs, dev, stream)
+    # timed region
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     clocks = Clocks(local)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    eri_ms = []
-    for k in range(args.steps):
-        flush.fill_(k & 0xFF)
-        dG.zero_()
-        ev[k][0].record(stream)
-        ctx.fock_device(dP.data_ptr(), dG.data_ptr(), sp)
-        ev[k][1].record(stream)
-        eri_ms.append(ctx.last_build_ms()[0])
+    step_ms, eri_ms = timed_builds(mixed, inputs, args.steps, dev, stream, flush)
     torch.cuda.synchronize(dev)
     if ws > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b_) for a, b_ in ev]
     total_s = sum(step_ms) / 1e3
     if ws > 1:
         t = torch.tensor([total_s], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_s = float(t.item())
     value = ws * args.steps / total_s
+    # the plain FP64 path on the same densities (full builds)
+    plain_inputs = [(True, D) for D in rm["densities"]]
+    timed_builds(plain, plain_inputs, 2, dev, stream, flush)
+    p_ms, p_eri = timed_builds(plain, plain_inputs, min(args.steps, len(plain_inputs)), dev, stream, flush)
+    plain_rate = len(p_ms) / (sum(p_ms) / 1e3)
     # end to end through the host entry point, pinned host buffers
-    Ph = torch.from_numpy(P).pin_memory()
-    Gh = torch.zeros(len(P), dtype=torch.float64).pin_memory()
-    Pn, Gn = Ph.numpy(), Gh.numpy()
-    for _ in range(max(1, args.warmup // 2)):
-        Gn[:] = 0.0
-        ctx.formGmatrix(Pn, Gn)
+    pin_in = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for _, x in inputs]
+    Gh = torch.zeros(b.no2, dtype=torch.float64).pin_memory()
+    Gn = Gh.numpy()
+
+    def e2e_steps(n):
+        for k in range(n):
+            full, _ = inputs[k % len(inputs)]
+            if full:
+                Gn[:] = 0.0
+            mixed.formGmatrix(pin_in[k % len(inputs)].numpy(), Gn)
+
+    e2e_steps(3)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        Gn[:] = 0.0
-        ctx.formGmatrix(Pn, Gn)
+    e2e_steps(args.steps)
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
     if ws > 1:
@@ -238,41 +302,47 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = ws * args.steps / e2e_s
-    # roofline of the ERI + J/K kernels
+    # roofline of the ERI + J/K kernels over the timed steps
     peak64 = native.fma_peak(True)
     peak32 = native.fma_peak(False)
-    eri_s = statistics.mean(eri_ms) / 1e3
-    flops = st["eri_flops"]
-    achieved = flops / eri_s / 1e12
-    if args.form == "mixed":
-        # FP32 and FP64 parts share the launch: time-weighted peak is not separable; report against FP64
-        pass
+    fl64 = sum(f64[k % len(inputs)] for k in range(args.steps))
+    fl32 = sum(f32[k % len(inputs)] for k in range(args.steps))
+    eri_s = sum(eri_ms) / 1e3
+    achieved = (fl64 + fl32) / eri_s / 1e12
+    peak = (fl64 + fl32) / (fl64 / peak64 + fl32 / peak32) if (fl64 + fl32) > 0 else peak64
+    launches_total = sum(launches[k % len(inputs)] for k in range(args.steps))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else "f64+f32",
-            "data": "synthetic (generated 32-water geometry, synthetic RHF density)",
-            "config": {"workload": WORKLOAD, "form": args.form, "rys_mode": "reference-compatible",
-                       "schwarz_cutoff": 1e-14, "l2": "flushed: 256 MiB write before every timed build",
-                       "nbf": b.norb, "shell_quartets": st["shell_quartets"],
-                       "shell_quartets_unscreened": st["shell_quartets_total"],
-                       "primitive_quartets_computed": st["primitive_quartets_computed"],
-                       "parallelism": f"replicas x{ws}"},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * len(P), "d2h_bytes_per_step": 8 * len(P)},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                         "frac": achieved / peak64, "traffic": profile_traffic(args.form),
-                         "kernel": "fock_jk_kernel (all class instances of one build)",
-                         "flops_per_launch": flops, "kernel_ms": eri_s * 1e3,
-                         "peak_source": "FP64 FMA microbenchmark of this library (unomol_gpu_fma_peak), measured in this run",
-                         "fp32_peak": peak32},
-            "clocks": clk, "gpu_launches": launches_per_build * args.steps,
-            "eri_flops_per_build": flops}
+            "warmup": max(args.warmup, 3), "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if args.form == "mixed" else "f64",
+            "data": "synthetic (generated 32-water geometry; densities of its own SCF)",
+            "config": {"workload": WORKLOAD, "form": args.form, "fp32_cutoff": args.fp32_cutoff if args.form == "mixed" else None,
+                       "density_skip_cutoff": 1e-12 if args.form == "mixed" else None, "rebuild_every": REBUILD,
+                       "rys_mode": "reference-compatible", "schwarz_cutoff": 1e-14,
+                       "l2": "flushed: 256 MiB write before every timed build", "nbf": b.norb,
+                       "builds_in_sequence": len(inputs), "parallelism": f"replicas x{ws}",
+                       "shell_quartets_per_build": [int(x) for x in nq], "fp32_shell_quartets_per_build": [int(x) for x in nq32]},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * b.no2, "d2h_bytes_per_step": 8 * b.no2},
+            "roofline": {"bound": "fp64+fp32 pipes", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": profile_traffic(args.form),
+                         "kernel": "fock_jk_kernel (all class instances and both precisions of a build)",
+                         "flops_fp64": fl64 / args.steps, "flops_fp32": fl32 / args.steps, "kernel_ms": 1e3 * eri_s / args.steps,
+                         "peak_fp64": peak64, "peak_fp32": peak32,
+                         "peak_source": "FMA microbenchmark of this library (unomol_gpu_fma_peak), this run"},
+            "plain_fp64": {"value": plain_rate, "unit": UNIT, "ms_per_build": statistics.mean(p_ms),
+                           "kernel_ms": statistics.mean(p_eri), "speedup_of_value": value / plain_rate},
+            "scf": {"energy_plain_fp64": r64["energy"], "energy_form": rm["energy"],
+                    "abs_dE": abs(rm["energy"] - r64["energy"]), "iterations_plain": r64["iterations"],
+                    "iterations_form": rm["iterations"], "converged": bool(r64["converged"] and rm["converged"]),
+                    "scf_wall_s_plain_fp64": r64["seconds"], "scf_wall_s_form": rm["seconds"],
+                    "fock_ms_plain_fp64": r64["fock_ms"], "fock_ms_form": rm["fock_ms"], "guess_s": t_guess},
+            "clocks": clk, "gpu_launches": launches_total}
     if rank == 0 and ws == 1:
         ensure_oracle()
         threads = os.cpu_count() or 1
-        rate, dt = cpu_port_rate(b, P, CPU_STRIDE, threads)
+        rate, dt = cpu_port_rate(b, synthetic_density(b), CPU_STRIDE, threads)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"C restatement of the reference algorithm, every {CPU_STRIDE}th canonical "
-                                          f"shell quartet ({dt:.1f} s), extrapolated to one build"}
+                                "sample": f"C restatement of the reference algorithm, full FP64 build, every {CPU_STRIDE}th "
+                                          f"canonical shell quartet ({dt:.1f} s), extrapolated to one build"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -286,12 +356,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--fp32-cutoff", type=float, default=1e-9)
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp32-cutoff", type=float, default=FP32_CUTOFF)
     ap.add_argument("--profile", action="store_true", help="device builds only (for ncu captures)")
     args = ap.parse_args()
-    if args.impl == "ours" and not args.profile:
-        args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

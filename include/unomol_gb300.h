@@ -100,10 +100,19 @@ int unomol_gpu_fock_rhf_device(UnomolCtx* ctx, const double* dP, double* dG, voi
 int unomol_gpu_fock_uhf_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa,
                                double* dGb, void* stream);
 
-/* Precision form: UNOMOL_PREC_FP64 (default) or UNOMOL_PREC_MIXED with the FP32 cutoff on
- * (Schwarz bound of the quartet) x (max |P| over the quartet's density blocks).  No reference
- * counterpart (the reference is FP64 only). */
+/* Precision form (no reference counterpart; the reference is FP64 only).
+ * UNOMOL_PREC_FP64 (default): every quartet that passes the integral Schwarz cut, in FP64.
+ * UNOMOL_PREC_MIXED: density-screened build made per call on the device.  With b = sqrt((ab|ab))
+ *   sqrt((cd|cd)) and D = max |P| over the density passed in: quartets with b*D >= fp32_cutoff run in
+ *   FP64, quartets with skip_cut <= b*D < fp32_cutoff in FP32 (Rys fits, recurrences and contraction in
+ *   FP32; density contraction and the Fock accumulation in FP64), the rest (and quartets whose six
+ *   density blocks are all small) are skipped.  Meant for incremental builds G(P) = G(P_old) + G(dP),
+ *   where |dP| shrinks as the SCF converges.  fp32_cutoff <= skip_cut gives a density-screened FP64
+ *   build. */
 int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cutoff);
+
+/* skip_cut of the density-screened build (default 1e-12). */
+int unomol_gpu_set_density_screening(UnomolCtx* ctx, double skip_cut);
 
 /* Rys quadrature of the two-root classes (unomol_gpu_set_rys_mode).
  * UNOMOL_RYS_REFERENCE (default): for 15 < T <= 40 the two-root nodes and weights follow the
@@ -176,6 +185,11 @@ typedef struct UnomolScfOptions {
     int guess;           /* 0 core Hamiltonian (RHF.hpp:205-211), 1 the P passed in (PMATRIX.DAT form) */
     int diis_size;       /* DIIS subspace (default 8) */
     double diis_tol;     /* DIIS: max |X^T (FPS - SPF) X| at convergence */
+    double diis_start;   /* DIIS: extrapolate once the error is below this (<= 0: from the start) */
+    double level_shift;  /* DIIS: virtual-orbital shift sigma (0: none) ... */
+    double level_shift_until; /* ... applied while the DIIS error is above this */
+    int incremental;     /* 1: G(P) = G(P_prev) + G(P - P_prev) between full builds (new) */
+    int rebuild_every;   /* incremental: a full build every this many builds (<= 0: 8) */
 } UnomolScfOptions;
 
 typedef struct UnomolScfResult {
@@ -189,6 +203,9 @@ typedef struct UnomolScfResult {
     int iterations, converged, fock_builds;
     double* energies;     /* optional [energies_cap]: total energy after every update */
     int energies_cap;
+    double fock_ms;       /* device time of all Fock builds (CUDA events) */
+    double* densities;    /* optional [densities_cap][no2 (UHF: 2*no2)]: the density of every build */
+    int densities_cap;
 } UnomolScfResult;
 
 /* SCF on the GPU: the loop of RestrictedHartreeFock / UnRestrictedHartreeFock::findEnergy (RHF.hpp:

@@ -49,7 +49,14 @@ struct UnomolCtx {
     std::vector<char> block_new;
     std::vector<BlockPair> bps;
     std::vector<long long> prefix;
+    std::vector<int> row_bp;
     std::vector<ClassLaunch> launches;
+    // per-build work lists of the density-screened / mixed-precision build
+    int *d_rowbp = nullptr, *d_mseg = nullptr;
+    long long *d_c64 = nullptr, *d_c32 = nullptr, *d_pre64 = nullptr, *d_pre32 = nullptr;
+    long long *d_cnt64 = nullptr, *d_cnt32 = nullptr;
+    float* d_dmax = nullptr;
+    double skip_cut = 1e-12;
     // device buffers
     ShellPair* d_pairs = nullptr;
     PrimPair* d_prims = nullptr;
@@ -267,11 +274,28 @@ int build_worklists(UnomolCtx* ctx) {
     ctx->stats.function_quartets = fq;
     dfree(ctx->d_bps);
     dfree(ctx->d_prefix);
+    for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
+    dfree(ctx->d_rowbp);
+    dfree(ctx->d_mseg);
     if (!ctx->bps.empty()) {
         CU(cudaMalloc(&ctx->d_bps, sizeof(BlockPair) * ctx->bps.size()));
         CU(cudaMemcpyAsync(ctx->d_bps, ctx->bps.data(), sizeof(BlockPair) * ctx->bps.size(), cudaMemcpyHostToDevice, ctx->stream));
         CU(cudaMalloc(&ctx->d_prefix, sizeof(long long) * ctx->prefix.size()));
         CU(cudaMemcpyAsync(ctx->d_prefix, ctx->prefix.data(), sizeof(long long) * ctx->prefix.size(), cudaMemcpyHostToDevice, ctx->stream));
+        // row -> block pair map and the per-build work-list buffers of the density-screened build
+        ctx->row_bp.assign(ctx->prefix.size(), -1);
+        for (size_t k = 0; k < ctx->bps.size(); ++k)
+            for (int i = 0; i < ctx->bps[k].bra_count; ++i) ctx->row_bp[ctx->bps[k].prefix_off + i] = (int)k;
+        const size_t nr = ctx->prefix.size(), nbp = ctx->bps.size();
+        CU(cudaMalloc(&ctx->d_rowbp, sizeof(int) * nr));
+        CU(cudaMemcpyAsync(ctx->d_rowbp, ctx->row_bp.data(), sizeof(int) * nr, cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMalloc(&ctx->d_mseg, sizeof(int) * nr));
+        for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32}) CU(cudaMalloc(p, sizeof(long long) * nr));
+        CU(cudaMalloc(&ctx->d_cnt64, sizeof(long long) * nbp));
+        CU(cudaMalloc(&ctx->d_cnt32, sizeof(long long) * nbp));
+        CU(cudaMemsetAsync(ctx->d_c64, 0, sizeof(long long) * nr, ctx->stream));
+        CU(cudaMemsetAsync(ctx->d_c32, 0, sizeof(long long) * nr, ctx->stream));
+        CU(cudaMemsetAsync(ctx->d_mseg, 0, sizeof(int) * nr, ctx->stream));
     }
     CU(cudaStreamSynchronize(ctx->stream));
     return UNOMOL_OK;
@@ -379,9 +403,9 @@ __global__ void fold_packed(const double* __restrict__ T, double* __restrict__ G
     G[t] += T[(long long)i * n + j] + T[(long long)j * n + i];
 }
 
-// max |P| over every shell pair block, for density-weighted screening
+// max |P| over every shell pair block (and over all blocks into dmax[0]), for density screening
 __global__ void shell_pmax(const double* __restrict__ Pa, const double* __restrict__ Pb, const int* __restrict__ soff,
-                           const int* __restrict__ sl, int nshell, int n, float* __restrict__ out) {
+                           const int* __restrict__ sl, int nshell, int n, float* __restrict__ out, float* dmax) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nshell * nshell) return;
     const int a = t / nshell, b = t % nshell;
@@ -394,7 +418,107 @@ __global__ void shell_pmax(const double* __restrict__ Pa, const double* __restri
             if (Pb) v = fmax(v, fabs(Pb[ix]));
             m = fmax(m, v);
         }
-    out[t] = (float)m;
+    // round up so that the float bound never undercuts the double one
+    const float mf = __double2float_ru(m);
+    out[t] = mf;
+    atomicMax(reinterpret_cast<unsigned*>(dmax), __float_as_uint(mf));  // non-negative floats order as uints
+}
+
+// Per bra row of every block pair: lengths of the FP64 segment (bound * max|P| >= cut64) and of the
+// FP32 segment (>= skip) of the row's Schwarz staircase, for this build's density.
+__global__ void split_rows(const ShellPair* __restrict__ pairs, const BlockPair* __restrict__ bps,
+                           const int* __restrict__ row_bp, const long long* __restrict__ prefix, long long nrows,
+                           const float* __restrict__ dmax, double cut64, double skip, long long* __restrict__ c64,
+                           long long* __restrict__ c32, int* __restrict__ mseg) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nrows) return;
+    const int bpi = row_bp[t];
+    if (bpi < 0) return;  // end-of-block-pair sentinel
+    const BlockPair bp = bps[bpi];
+    const int i = (int)(t - bp.prefix_off);
+    const int nstat = (int)(prefix[t + 1] - prefix[t]);  // static (integral-bound) staircase of the row
+    const double qd = pairs[bp.bra_begin + i].q * (double)dmax[0];
+    const ShellPair* kp = pairs + bp.ket_begin;
+    auto count = [&](double cut) {  // ket pairs j < nstat with q_i q_j max|P| >= cut (q descending)
+        if (!(qd > 0.0)) return 0;
+        const double thr = cut / qd;
+        int lo = 0, hi = nstat;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (kp[mid].q >= thr) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+    };
+    const int n64 = count(cut64);
+    const int nall = cut64 <= skip ? n64 : count(skip);
+    c64[t] = n64;
+    c32[t] = nall - n64;
+    mseg[t] = n64;
+}
+
+// Exclusive scan of the two row counts within every block pair (one CUDA block per block pair).
+__global__ void __launch_bounds__(1024) scan_rows(const BlockPair* __restrict__ bps, const long long* __restrict__ c64,
+                                                  const long long* __restrict__ c32, long long* __restrict__ p64,
+                                                  long long* __restrict__ p32, long long* __restrict__ n64,
+                                                  long long* __restrict__ n32) {
+    __shared__ long long warp_a[32], warp_b[32];
+    __shared__ long long run_a, run_b;
+    const BlockPair bp = bps[blockIdx.x];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        run_a = 0;
+        run_b = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < bp.bra_count; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const long long va = i < bp.bra_count ? c64[bp.prefix_off + i] : 0;
+        const long long vb = i < bp.bra_count ? c32[bp.prefix_off + i] : 0;
+        long long sa = va, sb = vb;  // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
+            if (lane >= o) {
+                sa += xa;
+                sb += xb;
+            }
+        }
+        if (lane == 31) {
+            warp_a[wid] = sa;
+            warp_b[wid] = sb;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            const int nw = blockDim.x >> 5;
+            long long ta = lane < nw ? warp_a[lane] : 0, tb = lane < nw ? warp_b[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long xa = __shfl_up_sync(0xffffffffu, ta, o), xb = __shfl_up_sync(0xffffffffu, tb, o);
+                if (lane >= o) {
+                    ta += xa;
+                    tb += xb;
+                }
+            }
+            if (lane < nw) {
+                warp_a[lane] = ta;  // inclusive sums of the warps
+                warp_b[lane] = tb;
+            }
+        }
+        __syncthreads();
+        const long long wa = wid > 0 ? warp_a[wid - 1] : 0, wb = wid > 0 ? warp_b[wid - 1] : 0;
+        if (i < bp.bra_count) {
+            p64[bp.prefix_off + i] = run_a + wa + sa - va;
+            p32[bp.prefix_off + i] = run_b + wb + sb - vb;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            run_a += warp_a[(blockDim.x >> 5) - 1];
+            run_b += warp_b[(blockDim.x >> 5) - 1];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        n64[blockIdx.x] = run_a;
+        n32[blockIdx.x] = run_b;
+    }
 }
 
 int ensure_density_buffers(UnomolCtx* ctx, bool uhf) {
@@ -451,13 +575,27 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     A.pmax = ctx->d_pmax;
     A.status = ctx->d_status;
     const bool mixed = ctx->prec_mode == UNOMOL_PREC_MIXED;
-    if (mixed) {
+    if (mixed && !ctx->bps.empty()) {
+        // this build's work lists: density bound per shell-pair block, split of every staircase row
+        // into FP64 / FP32 / skipped segments, scan per block pair (all on the device, no host sync)
         if (!ctx->d_pmax) CU(cudaMalloc(&ctx->d_pmax, sizeof(float) * ctx->nshell * ctx->nshell));
+        if (!ctx->d_dmax) CU(cudaMalloc(&ctx->d_dmax, sizeof(float)));
         A.pmax = ctx->d_pmax;
         const int ns2 = ctx->nshell * ctx->nshell;
-        shell_pmax<<<(ns2 + 255) / 256, 256, 0, s>>>(ctx->d_Pa, A.Pb, ctx->d_soff, ctx->d_sl, ctx->nshell, n, ctx->d_pmax);
+        CU(cudaMemsetAsync(ctx->d_dmax, 0, sizeof(float), s));
+        shell_pmax<<<(ns2 + 255) / 256, 256, 0, s>>>(ctx->d_Pa, A.Pb, ctx->d_soff, ctx->d_sl, ctx->nshell, n, ctx->d_pmax,
+                                                     ctx->d_dmax);
+        const long long nr = (long long)ctx->prefix.size();
+        split_rows<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(ctx->d_pairs, ctx->d_bps, ctx->d_rowbp, ctx->d_prefix, nr,
+                                                                ctx->d_dmax, std::max(ctx->fp32_cut, ctx->skip_cut),
+                                                                ctx->skip_cut, ctx->d_c64, ctx->d_c32, ctx->d_mseg);
+        scan_rows<<<(unsigned)ctx->bps.size(), 512, 0, s>>>(ctx->d_bps, ctx->d_c64, ctx->d_c32, ctx->d_pre64, ctx->d_pre32,
+                                                             ctx->d_cnt64, ctx->d_cnt32);
         CU(cudaGetLastError());
-        ++launches;
+        launches += 3;
+        A.dmax = ctx->d_dmax;
+        A.skip_cut = ctx->skip_cut;
+        A.dyn_mseg = ctx->d_mseg;
     }
     const int ncls = NPAIRCLASS * NPAIRCLASS;
     A.counters = nullptr;
@@ -478,11 +616,18 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             ++launches;
         } else {
             A.mode = 1;
+            A.dyn_prefix = ctx->d_pre64;
+            A.dyn_count = ctx->d_cnt64 + L.bp_begin;
             CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
-            A.mode = 2;
-            A.counter_base += ncls * 32;
-            CU(launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s));
-            launches += 2;
+            if (ctx->fp32_cut > ctx->skip_cut) {
+                A.mode = 2;
+                A.dyn_prefix = ctx->d_pre32;
+                A.dyn_count = ctx->d_cnt32 + L.bp_begin;
+                A.counter_base += ncls * 32;
+                CU(launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s));
+                ++launches;
+            }
+            ++launches;
         }
     }
     CU(cudaEventRecord(ctx->ev[2], s));
@@ -517,6 +662,18 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         ctx->stats.primitive_quartets_computed = prims;
         ctx->stats.eri_flops = fl + fl32;
         ctx->stats.eri_flops_fp32 = fl32;
+        if (mixed && !ctx->bps.empty()) {
+            std::vector<long long> a(ctx->bps.size()), b(ctx->bps.size());
+            CU(cudaMemcpy(a.data(), ctx->d_cnt64, sizeof(long long) * a.size(), cudaMemcpyDeviceToHost));
+            CU(cudaMemcpy(b.data(), ctx->d_cnt32, sizeof(long long) * b.size(), cudaMemcpyDeviceToHost));
+            long long s64 = 0, s32 = 0;
+            for (size_t k = 0; k < a.size(); ++k) {
+                s64 += a[k];
+                s32 += ctx->fp32_cut > ctx->skip_cut ? b[k] : 0;
+            }
+            ctx->stats.shell_quartets = s64 + s32;
+            ctx->stats.shell_quartets_fp32 = s32;
+        }
     }
     return UNOMOL_OK;
 }
@@ -641,6 +798,12 @@ int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cut) {
     return UNOMOL_OK;
 }
 
+int unomol_gpu_set_density_screening(UnomolCtx* ctx, double skip_cut) {
+    if (!ctx || !(skip_cut >= 0.0)) return fail(ctx, UNOMOL_EINVAL, "bad density screening cutoff");
+    ctx->skip_cut = skip_cut;
+    return UNOMOL_OK;
+}
+
 int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode) {
     if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
     if (mode != UNOMOL_RYS_REFERENCE && mode != UNOMOL_RYS_EXACT) return fail(ctx, UNOMOL_EINVAL, "unknown Rys mode");
@@ -732,6 +895,10 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
     dfree(ctx->d_counters);
     dfree(ctx->d_soff);
     dfree(ctx->d_sl);
+    for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
+    dfree(ctx->d_rowbp);
+    dfree(ctx->d_mseg);
+    dfree(ctx->d_dmax);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

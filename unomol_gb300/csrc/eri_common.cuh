@@ -91,6 +91,13 @@ struct FockArgs {
     int rys_compat;             // reference-compatible two-root Rys regime (FP64 only)
     unsigned long long* counters;  // optional: primitive quartets past the prefactor cut, 32 slots per launch
     int counter_base;           // first slot of this launch (class id * 32)
+    // density-screened / mixed-precision builds (mode 1 = FP64 part, mode 2 = FP32 part): per-build
+    // work lists made on the device (split_rows + scan_rows)
+    const long long* dyn_prefix;  // per bra row, exclusive prefix of this part's quartets (prefix layout)
+    const long long* dyn_count;   // per block pair of this launch: quartets of this part
+    const int* dyn_mseg;          // per bra row: length of its FP64 segment (the FP32 segment follows it)
+    const float* dmax;            // [0]: max |P| over all shell-pair blocks
+    double skip_cut;              // quartets with bound * max|P| below this are skipped
     int* status;                // device error flag
 };
 

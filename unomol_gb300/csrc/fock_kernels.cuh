@@ -242,6 +242,42 @@ __device__ __forceinline__ bool decode_work(const FockArgs& A, long long g, int&
     return true;
 }
 
+// Decode for the per-build work lists of the density-screened / mixed-precision build: the launch
+// covers the static staircase of every block pair; this part (FP64: mode 1, FP32: mode 2) uses the
+// first dyn_count quartets of it.  Bra row i's FP64 segment is ket [0, mseg_i), its FP32 segment
+// ket [mseg_i, mseg_i + n32_i).
+__device__ __forceinline__ bool decode_work_dyn(const FockArgs& A, long long g, int& bra_idx, int& ket_idx) {
+    if (g >= A.nwork) return false;
+    int lo = 0, hi = A.nbp - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (A.bps[mid].work_begin <= g) lo = mid; else hi = mid - 1;
+    }
+    const BlockPair& bp = A.bps[lo];
+    const long long w = g - bp.work_begin;
+    if (w >= A.dyn_count[lo]) return false;
+    const long long* pre = A.dyn_prefix + bp.prefix_off;
+    int a = 0, b = bp.bra_count - 1;
+    while (a < b) {
+        int mid = (a + b + 1) >> 1;
+        if (pre[mid] <= w) a = mid; else b = mid - 1;
+    }
+    bra_idx = bp.bra_begin + a;
+    int j = (int)(w - pre[a]);
+    if (A.mode == 2) j += A.dyn_mseg[bp.prefix_off + a];
+    ket_idx = bp.ket_begin + j;
+    return true;
+}
+
+// Density screening of one quartet: Schwarz bound times the largest |P| of the six shell-pair blocks
+// the quartet contracts with (J: ab, cd; K: ac, ad, bc, bd).
+__device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellPair& bra, const ShellPair& ket) {
+    const int a = bra.ish, b = bra.jsh, c = ket.ish, d = ket.jsh, n = A.nshell;
+    float m = fmaxf(fmaxf(A.pmax[a * n + b], A.pmax[c * n + d]), fmaxf(A.pmax[a * n + c], A.pmax[a * n + d]));
+    m = fmaxf(m, fmaxf(A.pmax[b * n + c], A.pmax[b * n + d]));
+    return (float)(bra.q * ket.q) * m < (float)A.skip_cut;
+}
+
 // Density contraction of one shell quartet and scatter into T (G = T + T^T):
 //   T[a][b] += 4 v' P_cd   T[c][d] += 4 v' P_ab   (2J)
 //   T[a][c] -= v' P_bd  T[b][c] -= v' P_ad  T[a][d] -= v' P_bc  T[b][d] -= v' P_ac   (K)
@@ -379,21 +415,10 @@ __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const No
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bi, ki;
     unsigned npass = 0;
-    if (!decode_work(A, g, bi, ki)) {
-        if (A.counters) count_flush(A, 0u);
-        return;
-    }
+    if (!(A.mode == 0 ? decode_work(A, g, bi, ki) : decode_work_dyn(A, g, bi, ki))) return;
     const ShellPair bra = A.pairs[bi];
     const ShellPair ket = A.pairs[ki];
-    if (A.mode != 0) {
-        // mixed precision: the FP64 launch (mode 1) takes quartets whose bound * max|P| is at or
-        // above the cutoff, the FP32 launch (mode 2) the rest
-        const double pm = (double)A.pmax[bra.ish * A.nshell + bra.jsh] + 0.0;
-        const double pk = (double)A.pmax[ket.ish * A.nshell + ket.jsh];
-        const double big = bra.q * ket.q * fmax(pm, pk);
-        const bool is_big = big >= A.fp32_cut;
-        if ((A.mode == 1) != is_big) return;
-    }
+    if (A.mode != 0 && quartet_screened(A, bra, ket)) return;
     R acc[Q::NF];
     if constexpr (sizeof(R) == 8)
         shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.rys_compat != 0, acc,
@@ -491,13 +516,10 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bi, ki;
     unsigned npass = 0;
-    if (!decode_work(A, g, bi, ki)) return;
+    if (!(A.mode == 0 ? decode_work(A, g, bi, ki) : decode_work_dyn(A, g, bi, ki))) return;
     const ShellPair bra = A.pairs[bi];
     const ShellPair ket = A.pairs[ki];
-    if (A.mode != 0) {
-        const double pm = fmax((double)A.pmax[bra.ish * A.nshell + bra.jsh], (double)A.pmax[ket.ish * A.nshell + ket.jsh]);
-        if ((A.mode == 1) != (bra.q * ket.q * pm >= A.fp32_cut)) return;
-    }
+    if (A.mode != 0 && quartet_screened(A, bra, ket)) return;
     const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
     const int NF = NA * NB * NC * ND;
     const int nr = (la + lb + lc + ld) / 2 + 1;

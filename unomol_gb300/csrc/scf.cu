@@ -272,6 +272,27 @@ double maxabs(const std::vector<double>& v) {
     return m;
 }
 
+// Level shift sigma (S - S P S), packed: raises the virtual orbital energies by sigma and leaves the
+// occupied ones (P = C_occ C_occ^T, C^T S C = 1), damping the occupied/virtual rotations of early
+// iterations.
+int level_shift(Dev& d, const std::vector<double>& Ppk, const double* d_S, double* d_pk, double sigma,
+                std::vector<double>& shift) {
+    const int n = d.n;
+    const double one = 1.0, zero = 0.0, ms = -sigma;
+    double *dP = d.W, *t = d.T1, *u = d.C;
+    CK(cudaMemcpyAsync(d_pk, Ppk.data(), Ppk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, dP, n);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d_S, n, dP, n, &zero, t, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, t, n, d_S, n, &zero, u, n), UNOMOL_ECUDA);
+    // t = sigma S - sigma S P S
+    CK(cublasDgeam(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &sigma, d_S, n, &ms, u, n, t, n), UNOMOL_ECUDA);
+    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(t, d_pk, n);
+    shift.resize(Ppk.size());
+    CK(cudaMemcpyAsync(shift.data(), d_pk, shift.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    return UNOMOL_OK;
+}
+
 }  // namespace
 
 extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const UnomolScfOptions* opt, UnomolScfResult* res,
@@ -332,20 +353,47 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     const int cflag = opt->conv_type;
     double eold = 0.0, energy = 0.0, ediff = 10.0, pdiff = 10.0, init_energy = 0.0;
     int iteration = 0, builds = 0;
-    Diis diisA, diisB;
-    diisA.maxv = diisB.maxv = opt->diis_size > 1 ? opt->diis_size : 8;
+    Diis diisA;
+    diisA.maxv = opt->diis_size > 1 ? opt->diis_size : 8;
+    const double diis_start = opt->diis_start > 0.0 ? opt->diis_start : 1e30;
     double diis_err = 0.0;
     // update(): RHF.hpp:87-112 / UHF.hpp:101-134
+    // incremental builds: d_G / d_Gb keep G(P_prev); a build adds G(P - P_prev) (G is linear in P)
+    const int rebuild_every = opt->rebuild_every > 0 ? opt->rebuild_every : 8;
+    double fock_ms = 0.0;
+    int since_full = 1 << 30;
+    std::vector<double> PprevA, PprevB, dPa(no2), dPb(no2);
     auto update = [&]() -> int {
         std::fill(Ga.begin(), Ga.end(), 0.0);
-        cudaMemcpyAsync(d_P, Pa.data(), no2 * sizeof(double), cudaMemcpyHostToDevice, s);
-        cudaMemsetAsync(d_G, 0, no2 * sizeof(double), s);
+        const bool full = !opt->incremental || since_full >= rebuild_every;
+        const double* srcA = Pa.data();
+        const double* srcB = Pb.data();
+        if (!full) {
+            for (size_t k = 0; k < no2; ++k) dPa[k] = Pa[k] - PprevA[k];
+            srcA = dPa.data();
+            if (uhf) {
+                for (size_t k = 0; k < no2; ++k) dPb[k] = Pb[k] - PprevB[k];
+                srcB = dPb.data();
+            }
+            ++since_full;
+        } else {
+            since_full = 1;
+            cudaMemsetAsync(d_G, 0, no2 * sizeof(double), s);
+            if (uhf) cudaMemsetAsync(d_Gb, 0, no2 * sizeof(double), s);
+        }
+        if (res->densities && builds < res->densities_cap) {
+            double* dst = res->densities + (size_t)builds * no2 * (uhf ? 2 : 1);
+            std::memcpy(dst, Pa.data(), no2 * sizeof(double));
+            if (uhf) std::memcpy(dst + no2, Pb.data(), no2 * sizeof(double));
+        }
+        PprevA = Pa;
+        if (uhf) PprevB = Pb;
+        cudaMemcpyAsync(d_P, srcA, no2 * sizeof(double), cudaMemcpyHostToDevice, s);
         int r;
         if (!uhf) {
             r = unomol_gpu_fock_rhf_device(ctx, d_P, d_G, s);
         } else {
-            cudaMemcpyAsync(d_Pb, Pb.data(), no2 * sizeof(double), cudaMemcpyHostToDevice, s);
-            cudaMemsetAsync(d_Gb, 0, no2 * sizeof(double), s);
+            cudaMemcpyAsync(d_Pb, srcB, no2 * sizeof(double), cudaMemcpyHostToDevice, s);
             r = unomol_gpu_fock_uhf_device(ctx, d_P, d_Pb, d_G, d_Gb, s);
         }
         if (r) {
@@ -353,6 +401,10 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
             return r;
         }
         ++builds;
+        {
+            double me = 0.0, mt = 0.0;
+            if (unomol_gpu_last_build_ms(ctx, &me, &mt) == UNOMOL_OK) fock_ms += mt;
+        }
         cudaMemcpyAsync(Ga.data(), d_G, no2 * sizeof(double), cudaMemcpyDeviceToHost, s);
         if (uhf) cudaMemcpyAsync(Gb.data(), d_Gb, no2 * sizeof(double), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) {
@@ -369,19 +421,36 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
         for (size_t k = 0; k < no2; ++k) Fa[k] = H[k] + Ga[k];
         if (uhf)
             for (size_t k = 0; k < no2; ++k) Fb[k] = H[k] + Gb[k];
-        if (opt->accel == 2) {  // DIIS on F
-            std::vector<double> e;
+        if (opt->accel == 2) {
+            // DIIS on F; for UHF one set of coefficients for both spins (errors and Fock matrices of
+            // the two spins concatenated), extrapolation only once the error is below diis_start
+            std::vector<double> e, eb;
             r = diis_error(d, Fa, Pa, d_S, d_pk, e);
             if (r) return r;
             diis_err = maxabs(e);
-            diisA.push(Fa, e);
-            diisA.extrapolate(Fa);
+            std::vector<double> fcat = Fa;
             if (uhf) {
-                r = diis_error(d, Fb, Pb, d_S, d_pk, e);
+                r = diis_error(d, Fb, Pb, d_S, d_pk, eb);
                 if (r) return r;
-                diis_err = std::max(diis_err, maxabs(e));
-                diisB.push(Fb, e);
-                diisB.extrapolate(Fb);
+                diis_err = std::max(diis_err, maxabs(eb));
+                e.insert(e.end(), eb.begin(), eb.end());
+                fcat.insert(fcat.end(), Fb.begin(), Fb.end());
+            }
+            diisA.push(fcat, e);
+            if (diis_err < diis_start && diisA.extrapolate(fcat)) {
+                std::copy(fcat.begin(), fcat.begin() + no2, Fa.begin());
+                if (uhf) std::copy(fcat.begin() + no2, fcat.end(), Fb.begin());
+            }
+            if (opt->level_shift > 0.0 && diis_err > opt->level_shift_until) {
+                std::vector<double> sh;
+                r = level_shift(d, Pa, d_S, d_pk, opt->level_shift, sh);
+                if (r) return r;
+                for (size_t k = 0; k < no2; ++k) Fa[k] += sh[k];
+                if (uhf) {
+                    r = level_shift(d, Pb, d_S, d_pk, opt->level_shift, sh);
+                    if (r) return r;
+                    for (size_t k = 0; k < no2; ++k) Fb[k] += sh[k];
+                }
             }
         }
         PoldA2 = PoldA;
@@ -449,6 +518,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     res->iterations = iteration;
     res->converged = conv ? 1 : 0;
     res->fock_builds = builds;
+    res->fock_ms = fock_ms;
     res->diis_error = diis_err;
     res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return UNOMOL_OK;

@@ -23,7 +23,8 @@ EXPORTS = [
     "unomol_gpu_fock_rhf_device", "unomol_gpu_fock_uhf_device", "unomol_gpu_set_precision",
     "unomol_gpu_set_screening", "unomol_gpu_set_rys_mode", "unomol_gpu_get_stats", "unomol_gpu_destroy",
     "unomol_gpu_last_error", "unomol_gpu_version", "unomol_gpu_set_counting", "unomol_gpu_fma_peak",
-    "unomol_gpu_last_build_ms",
+    "unomol_gpu_last_build_ms", "unomol_gpu_set_density_screening", "unomol_gpu_fock_rhf_noalloc",
+    "unomol_one_electron", "unomol_scf",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -177,6 +178,10 @@ class TwoElectronInts:
         _check(lib().unomol_gpu_last_build_ms(self._h, C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
 
+    def set_density_screening(self, skip_cut: float):
+        lib().unomol_gpu_set_density_screening.argtypes = [C.c_void_p, C.c_double]
+        _check(lib().unomol_gpu_set_density_screening(self._h, float(skip_cut)), self._h)
+
     def set_counting(self, on: bool):
         _check(lib().unomol_gpu_set_counting(self._h, 1 if on else 0), self._h)
 
@@ -207,7 +212,9 @@ class ScfInput(C.Structure):
 
 class ScfOptions(C.Structure):
     _fields_ = [("maxits", C.c_int), ("eps", C.c_double), ("conv_type", C.c_int), ("accel", C.c_int),
-                ("guess", C.c_int), ("diis_size", C.c_int), ("diis_tol", C.c_double)]
+                ("guess", C.c_int), ("diis_size", C.c_int), ("diis_tol", C.c_double),
+                ("diis_start", C.c_double), ("level_shift", C.c_double), ("level_shift_until", C.c_double),
+                ("incremental", C.c_int), ("rebuild_every", C.c_int)]
 
 
 class ScfResult(C.Structure):
@@ -215,7 +222,8 @@ class ScfResult(C.Structure):
                 ("e_electronic", C.c_double), ("init_energy", C.c_double), ("ediff", C.c_double),
                 ("pdiff", C.c_double), ("diis_error", C.c_double), ("seconds", C.c_double),
                 ("iterations", C.c_int), ("converged", C.c_int), ("fock_builds", C.c_int),
-                ("energies", C.POINTER(C.c_double)), ("energies_cap", C.c_int)]
+                ("energies", C.POINTER(C.c_double)), ("energies_cap", C.c_int), ("fock_ms", C.c_double),
+                ("densities", C.POINTER(C.c_double)), ("densities_cap", C.c_int)]
 
 
 SCF_DAMPED = 0
@@ -234,7 +242,9 @@ def one_electron(b: Basis):
 
 def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPED, guess_P=None,
         maxits: int | None = None, eps: float | None = None, conv_type: int | None = None,
-        diis_size: int = 8, diis_tol: float = 1e-6, record: int = 0):
+        diis_size: int = 8, diis_tol: float = 1e-6, record: int = 0, diis_start: float = 0.0,
+        level_shift: float = 0.0, level_shift_until: float = 0.05, incremental: bool = False,
+        rebuild_every: int = 8, keep_densities: int = 0):
     """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ..."""
     L = lib()
     L.unomol_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.POINTER(ScfOptions), C.POINTER(ScfResult),
@@ -247,7 +257,8 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
     inp = ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), S.ctypes.data_as(dp), H.ctypes.data_as(dp))
     opt = ScfOptions(maxits if maxits is not None else b.maxits, eps if eps is not None else b.eps,
                      conv_type if conv_type is not None else b.scf_flag[0], accel, 0 if guess_P is None else 1,
-                     diis_size, diis_tol)
+                     diis_size, diis_tol, diis_start, level_shift, level_shift_until, 1 if incremental else 0,
+                     rebuild_every)
     uhf = b.nelec % 2 == 1
     P = np.zeros(b.no2 * (2 if uhf else 1))
     if guess_P is not None:
@@ -258,15 +269,21 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
     if record:
         res.energies = energies.ctypes.data_as(dp)
         res.energies_cap = record
+    dens = np.zeros((max(keep_densities, 1), len(P)))
+    if keep_densities:
+        res.densities = dens.ctypes.data_as(dp)
+        res.densities_cap = keep_densities
     rc = L.unomol_scf(ctx._h, C.byref(inp), C.byref(opt), C.byref(res), P, eps_orb.ctypes.data)
     if rc != 0:
         raise UnomolError(f"unomol_scf error {rc}: {res.message.decode(errors='replace')}")
     out = {k: getattr(res, k) for k in ("energy", "e_electronic", "init_energy", "ediff", "pdiff", "diis_error",
-                                        "seconds", "iterations", "converged", "fock_builds")}
+                                        "seconds", "iterations", "converged", "fock_builds", "fock_ms")}
     out["P"] = P
     out["orbital_energies"] = eps_orb
     if record:
         out["energies"] = energies[:min(record, res.iterations)].copy()
+    if keep_densities:
+        out["densities"] = dens[:min(keep_densities, res.fock_builds)].copy()
     return out
 
 
