@@ -69,6 +69,7 @@ struct UnomolCtx {
     double *d_Pa = nullptr, *d_Pb = nullptr, *d_Ta = nullptr, *d_Tb = nullptr;
     double *d_Ga = nullptr, *d_Gb = nullptr, *d_pk_a = nullptr, *d_pk_b = nullptr;
     float* d_pmax = nullptr;
+    float *d_Pa32 = nullptr, *d_Pb32 = nullptr;
     int *d_soff = nullptr, *d_sl = nullptr;
     int* d_status = nullptr;
     unsigned long long* d_counters = nullptr;
@@ -390,6 +391,12 @@ __global__ void expand_packed(const double* __restrict__ pk, double* __restrict_
     full[t] = pk[(long long)hi * (hi + 1) / 2 + lo];
 }
 
+// FP32 copy of a dense density (the FP32 kernels contract with it)
+__global__ void to_float(const double* __restrict__ full, float* __restrict__ f32, long long n2) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n2) f32[t] = (float)full[t];
+}
+
 // G_packed[ij] += T[i][j] + T[j][i]
 __global__ void fold_packed(const double* __restrict__ T, double* __restrict__ G, int n) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -536,6 +543,10 @@ int ensure_density_buffers(UnomolCtx* ctx, bool uhf) {
         CU(cudaMalloc(&ctx->d_Gb, np * sizeof(double)));
         CU(cudaMalloc(&ctx->d_pk_b, np * sizeof(double)));
     }
+    if (ctx->prec_mode == UNOMOL_PREC_MIXED) {
+        if (!ctx->d_Pa32) CU(cudaMalloc(&ctx->d_Pa32, n2 * sizeof(float)));
+        if (uhf && !ctx->d_Pb32) CU(cudaMalloc(&ctx->d_Pb32, n2 * sizeof(float)));
+    }
     return UNOMOL_OK;
 }
 
@@ -596,6 +607,13 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         A.dmax = ctx->d_dmax;
         A.skip_cut = ctx->skip_cut;
         A.dyn_mseg = ctx->d_mseg;
+        to_float<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(ctx->d_Pa, ctx->d_Pa32, n2);
+        A.Pa32 = ctx->d_Pa32;
+        if (uhf) {
+            to_float<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(ctx->d_Pb, ctx->d_Pb32, n2);
+            A.Pb32 = ctx->d_Pb32;
+        }
+        CU(cudaGetLastError());
     }
     const int ncls = NPAIRCLASS * NPAIRCLASS;
     A.counters = nullptr;
@@ -899,6 +917,8 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
     dfree(ctx->d_rowbp);
     dfree(ctx->d_mseg);
     dfree(ctx->d_dmax);
+    dfree(ctx->d_Pa32);
+    dfree(ctx->d_Pb32);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -80,6 +80,8 @@ struct FockArgs {
     int nbf;
     const double* Pa;           // full N x N density (RHF: P; UHF: Pa)
     const double* Pb;           // UHF: Pb; RHF: nullptr
+    const float* Pa32;          // FP32 copies of Pa / Pb for the FP32 kernels' density contraction
+    const float* Pb32;
     const float* pmax;          // shell-pair max |P| (nshell x nshell), for density screening
     double* Ta;                 // N x N accumulators; G = T + T^T
     double* Tb;                 // UHF beta accumulator

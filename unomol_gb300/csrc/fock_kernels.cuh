@@ -31,6 +31,14 @@ __host__ __device__ constexpr int rys_off(int n, int deg) {
 // Size of a device table: polynomial blocks, then hermite x[5][5] and w[5][5].
 __host__ __device__ constexpr int rys_table_len(int deg) { return rys_off(RYS_NMAX + 1, deg) + 50; }
 
+// |v| > cut (cut >= 0) compared as IEEE bit patterns: integer pipe, no FP64 compare
+__device__ __forceinline__ bool above_cut(double v, double cut) {
+    return (__double_as_longlong(v) & 0x7fffffffffffffffLL) > __double_as_longlong(cut);
+}
+__device__ __forceinline__ bool above_cut(float v, double cut) {
+    return (__float_as_int(v) & 0x7fffffff) > __float_as_int((float)cut);
+}
+
 // Reference-compatible two-root regime.  For 15 < T <= 40 the reference's Rys::root2 evaluates a
 // large-T form with fitted e^{-T} corrections (Rys.cpp:611-623) that departs from the exact
 // quadrature by up to 3.5e-4 relative at T = 15 (below 1e-12 from T ~ 31 on); the golden energies of
@@ -180,9 +188,12 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
         const R PAx = pb[ib].PA[0], PAy = pb[ib].PA[1], PAz = pb[ib].PA[2];
         for (int ik = 0; ik < nk; ++ik) {
             const R q = pk[ik].p, rq = pk[ik].rp, Ecd = pk[ik].E, ccd = pk[ik].cc;
-            const R rpq = R(1) / (p + q);
-            R sr = R(SRTERM) * Eab * Ecd * sqrt(rpq);
-            if (sr < prim_cut) continue;  // TwoElectronInts.cpp:478-479 (before the coefficients)
+            // one reciprocal square root gives both 1/sqrt(p+q) and 1/(p+q) (the FP64 pipe of this
+            // GPU is 1/64 of the FP32 one: a division and a square root cost twice as much)
+            const R rs = rsqrt(p + q);
+            R sr = R(SRTERM) * Eab * Ecd * rs;
+            if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
+            const R rpq = rs * rs;
             sr *= cab * ccd;
             if (npass) ++*npass;
             const R QCx = pk[ik].PA[0], QCy = pk[ik].PA[1], QCz = pk[ik].PA[2];
@@ -289,37 +300,49 @@ template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& bra, const ShellPair& ket,
                                           bool same_pair, const R (&acc)[QClass<LA, LB, LC, LD>::NF],
                                           const double (&nrm)[LMAX + 1][6]) {
+    // The density contraction runs in the kernel's own type R (FP32 in the FP32 kernels, on an FP32
+    // copy of P); only the partial sums reach the FP64 accumulator T.  The degeneracy factor is applied
+    // to those sums, and the storage cut compares magnitudes as integers (no FP64 compare).
     using Q = QClass<LA, LB, LC, LD>;
+    constexpr bool UNIT_NORMS = LA < 2 && LB < 2 && LC < 2 && LD < 2;  // all component factors are 1
     const int N = A.nbf;
-    double deg = 1.0;
-    if (bra.same) deg *= 0.5;
-    if (ket.same) deg *= 0.5;
-    if (same_pair) deg *= 0.5;
-    const double* __restrict__ Pa = A.Pa;
-    const double* __restrict__ Pb = A.Pb;
-    double jcd[Q::NC * Q::ND];
-    double kbc[Q::NB * Q::NC], kbd[Q::NB * Q::ND];
-    double kbcB[UHF ? Q::NB * Q::NC : 1], kbdB[UHF ? Q::NB * Q::ND : 1];
+    R deg = R(1);
+    if (bra.same) deg *= R(0.5);
+    if (ket.same) deg *= R(0.5);
+    if (same_pair) deg *= R(0.5);
+    const R* __restrict__ Pa;
+    const R* __restrict__ Pb;
+    if constexpr (sizeof(R) == 8) {
+        Pa = reinterpret_cast<const R*>(A.Pa);
+        Pb = reinterpret_cast<const R*>(A.Pb);
+    } else {
+        Pa = reinterpret_cast<const R*>(A.Pa32);
+        Pb = reinterpret_cast<const R*>(A.Pb32);
+    }
+    const R jf = UHF ? R(2) : R(4);
+    R jcd[Q::NC * Q::ND];
+    R kbc[Q::NB * Q::NC], kbd[Q::NB * Q::ND];
+    R kbcB[UHF ? Q::NB * Q::NC : 1], kbdB[UHF ? Q::NB * Q::ND : 1];
 #pragma unroll
-    for (int i = 0; i < Q::NC * Q::ND; ++i) jcd[i] = 0.0;
+    for (int i = 0; i < Q::NC * Q::ND; ++i) jcd[i] = R(0);
 #pragma unroll
-    for (int i = 0; i < Q::NB * Q::NC; ++i) { kbc[i] = 0.0; if constexpr (UHF) kbcB[i] = 0.0; }
+    for (int i = 0; i < Q::NB * Q::NC; ++i) { kbc[i] = R(0); if constexpr (UHF) kbcB[i] = R(0); }
 #pragma unroll
-    for (int i = 0; i < Q::NB * Q::ND; ++i) { kbd[i] = 0.0; if constexpr (UHF) kbdB[i] = 0.0; }
+    for (int i = 0; i < Q::NB * Q::ND; ++i) { kbd[i] = R(0); if constexpr (UHF) kbdB[i] = R(0); }
 #pragma unroll
     for (int ia = 0; ia < Q::NA; ++ia) {
         const int a = bra.a_off + ia;
-        double kac[Q::NC], kad[Q::ND], kacB[UHF ? Q::NC : 1], kadB[UHF ? Q::ND : 1];
+        R kac[Q::NC], kad[Q::ND], kacB[UHF ? Q::NC : 1], kadB[UHF ? Q::ND : 1];
 #pragma unroll
-        for (int i = 0; i < Q::NC; ++i) { kac[i] = 0.0; if constexpr (UHF) kacB[i] = 0.0; }
+        for (int i = 0; i < Q::NC; ++i) { kac[i] = R(0); if constexpr (UHF) kacB[i] = R(0); }
 #pragma unroll
-        for (int i = 0; i < Q::ND; ++i) { kad[i] = 0.0; if constexpr (UHF) kadB[i] = 0.0; }
+        for (int i = 0; i < Q::ND; ++i) { kad[i] = R(0); if constexpr (UHF) kadB[i] = R(0); }
 #pragma unroll
         for (int ib = 0; ib < Q::NB; ++ib) {
             const int b = bra.b_off + ib;
-            double Pab = __ldg(Pa + a * N + b);
+            R Pab = __ldg(Pa + a * N + b);
             if constexpr (UHF) Pab += __ldg(Pb + a * N + b);
-            double jab = 0.0;
+            R jab = R(0);
 #pragma unroll
             for (int ic = 0; ic < Q::NC; ++ic) {
                 const int c = ket.a_off + ic;
@@ -327,10 +350,10 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
                 for (int id = 0; id < Q::ND; ++id) {
                     const int d = ket.b_off + id;
                     const int f = ((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id;
-                    double v = double(acc[f]) * (nrm[LA][ia] * nrm[LB][ib] * nrm[LC][ic] * nrm[LD][id]);
-                    if (!(fabs(v) > A.thr_int)) continue;  // TwoElectronInts.cpp:668
-                    v *= deg;
-                    double Pcd = __ldg(Pa + c * N + d);
+                    R v = acc[f];
+                    if constexpr (!UNIT_NORMS) v *= R(nrm[LA][ia] * nrm[LB][ib] * nrm[LC][ic] * nrm[LD][id]);
+                    if (!above_cut(v, A.thr_int)) continue;  // TwoElectronInts.cpp:668
+                    R Pcd = __ldg(Pa + c * N + d);
                     if constexpr (UHF) Pcd += __ldg(Pb + c * N + d);
                     jab = fma(v, Pcd, jab);
                     jcd[ic * Q::ND + id] = fma(v, Pab, jcd[ic * Q::ND + id]);
@@ -346,24 +369,21 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
                     }
                 }
             }
-            if constexpr (UHF) {
-                atomicAdd(A.Ta + a * N + b, 2.0 * jab);
-                atomicAdd(A.Tb + a * N + b, 2.0 * jab);
-            } else {
-                atomicAdd(A.Ta + a * N + b, 4.0 * jab);
-            }
+            const double j = double(jf * deg * jab);
+            atomicAdd(A.Ta + a * N + b, j);
+            if constexpr (UHF) atomicAdd(A.Tb + a * N + b, j);
         }
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic) {
             const int c = ket.a_off + ic;
-            atomicAdd(A.Ta + a * N + c, -kac[ic]);
-            if constexpr (UHF) atomicAdd(A.Tb + a * N + c, -kacB[ic]);
+            atomicAdd(A.Ta + a * N + c, double(-deg * kac[ic]));
+            if constexpr (UHF) atomicAdd(A.Tb + a * N + c, double(-deg * kacB[ic]));
         }
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int d = ket.b_off + id;
-            atomicAdd(A.Ta + a * N + d, -kad[id]);
-            if constexpr (UHF) atomicAdd(A.Tb + a * N + d, -kadB[id]);
+            atomicAdd(A.Ta + a * N + d, double(-deg * kad[id]));
+            if constexpr (UHF) atomicAdd(A.Tb + a * N + d, double(-deg * kadB[id]));
         }
     }
 #pragma unroll
@@ -371,12 +391,9 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int c = ket.a_off + ic, d = ket.b_off + id;
-            if constexpr (UHF) {
-                atomicAdd(A.Ta + c * N + d, 2.0 * jcd[ic * Q::ND + id]);
-                atomicAdd(A.Tb + c * N + d, 2.0 * jcd[ic * Q::ND + id]);
-            } else {
-                atomicAdd(A.Ta + c * N + d, 4.0 * jcd[ic * Q::ND + id]);
-            }
+            const double j = double(jf * deg * jcd[ic * Q::ND + id]);
+            atomicAdd(A.Ta + c * N + d, j);
+            if constexpr (UHF) atomicAdd(A.Tb + c * N + d, j);
         }
 #pragma unroll
     for (int ib = 0; ib < Q::NB; ++ib) {
@@ -384,14 +401,14 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic) {
             const int c = ket.a_off + ic;
-            atomicAdd(A.Ta + b * N + c, -kbc[ib * Q::NC + ic]);
-            if constexpr (UHF) atomicAdd(A.Tb + b * N + c, -kbcB[ib * Q::NC + ic]);
+            atomicAdd(A.Ta + b * N + c, double(-deg * kbc[ib * Q::NC + ic]));
+            if constexpr (UHF) atomicAdd(A.Tb + b * N + c, double(-deg * kbcB[ib * Q::NC + ic]));
         }
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int d = ket.b_off + id;
-            atomicAdd(A.Ta + b * N + d, -kbd[ib * Q::ND + id]);
-            if constexpr (UHF) atomicAdd(A.Tb + b * N + d, -kbdB[ib * Q::ND + id]);
+            atomicAdd(A.Ta + b * N + d, double(-deg * kbd[ib * Q::ND + id]));
+            if constexpr (UHF) atomicAdd(A.Tb + b * N + d, double(-deg * kbdB[ib * Q::ND + id]));
         }
     }
 }
