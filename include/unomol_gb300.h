@@ -124,6 +124,15 @@ int unomol_gpu_set_density_screening(UnomolCtx* ctx, double skip_cut);
 #define UNOMOL_RYS_EXACT 1
 int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode);
 
+/* Integral method (unomol_gpu_set_eri_method).
+ * UNOMOL_ERI_REFERENCE (default): Rys quadrature for la+lb+lc+ld <= 8 and McMurchie-Davidson above,
+ *   as the reference's default build (TwoElectronInts.cpp:658-666).
+ * UNOMOL_ERI_MD: McMurchie-Davidson for every quartet, as the reference built with -DUNOMOL_MD_INTS.
+ * The MD integrals use the reference's Boys evaluation (MD_Rfunction.hpp:2185-2206). */
+#define UNOMOL_ERI_REFERENCE 0
+#define UNOMOL_ERI_MD 1
+int unomol_gpu_set_eri_method(UnomolCtx* ctx, int method);
+
 /* Schwarz cutoff on sqrt((ab|ab)) sqrt((cd|cd)).  Default 1e-14: the reference drops stored
  * integrals with |v| <= 1e-14 (TwoElectronInts.cpp:668), so quartets whose bound is below that
  * contribute nothing there either.  Rebuilds the work lists. */

@@ -85,6 +85,31 @@ def make_case(name: str, patin: str, scf: bool, golden_energy: float | None, dum
     print(name, "nbf", n, "stored", len(vals), "E" if scf else "", out.get("scf_energy", ""), file=sys.stderr)
 
 
+def pbas_patin(atoms_bohr, key: str, nelec: int, eps: float = 1e-10) -> str:
+    """patin.dat text for atoms [(Z, (x, y, z) bohr)] with basis `key` of the reference's pbas.lib
+    (used for the f-shell cases: the basis_sets.json of the package holds the light bases only)."""
+    lines = open(os.path.join(REF, "pbas.lib")).read().split("\n")
+    i = lines.index(key)
+    nsh = int(lines[i + 1].split()[0])
+    j = i + 2
+    shells = []
+    for _ in range(nsh):
+        npr, l = map(int, lines[j].split()[:2])
+        shells.append((l, [lines[j + 1 + k].split()[:2] for k in range(npr)]))
+        j += npr + 1
+    out_s, norb, maxl = [], 0, 0
+    for c in range(len(atoms_bohr)):
+        for l, prims in shells:
+            out_s.append(f"{len(prims):4d}{l:4d}{c:6d}")
+            out_s += [f"{a} {k}" for a, k in prims]
+            norb += (l + 1) * (l + 2) // 2
+            maxl = max(maxl, l)
+    head = [f"{len(shells) * len(atoms_bohr):7d}{norb:7d}{len(atoms_bohr):7d}{maxl:3d}", f"{nelec:7d}{299:7d}",
+            f"{eps:24.16e}", " 0 0", " 2 1 0", " 0 0 0"]
+    cen = [f"{float(z):15.10f}" + "".join(f"{v:20.12f}" for v in x) for z, x in atoms_bohr]
+    return "\n".join(head + cen + out_s) + "\n"
+
+
 def published_energy(tag: str) -> float:
     with open(os.path.join(REF, "test", f"scfout.dat.{tag}")) as f:
         for line in f:
@@ -119,6 +144,10 @@ def main():
     cases.append(("ethane_631g", molecules.patin_text(molecules.alkane(2), "6-31G", eps=1e-10), True, None, False))
     cases.append(("propane_cation_sto3g", molecules.patin_text(molecules.alkane(3), "STO-3G", charge=1, eps=1e-10), True, None, False))
     cases.append(("water3_631g", molecules.patin_text(molecules.water_cluster(3, 7), "6-31G", eps=1e-10), True, None, False))
+    # f shells (He cc-pVQZ of pbas.lib): classes with la+lb+lc+ld > 8 run the reference's MD path
+    fcases = [("he_ccpvqz", pbas_patin([(2, (0.0, 0.0, 0.0))], "HE:CC-PVQZU", 2), True, None, False),
+              ("he2_ccpvqz", pbas_patin([(2, (0.0, 0.0, 0.0)), (2, (0.0, 0.0, 3.0))], "HE:CC-PVQZU", 4), False, None, False)]
+    cases += fcases
     if a.big:
         cases.append(("decane_631g", molecules.patin_text(molecules.alkane(10), "6-31G", eps=1e-10), False, None, False))
         cases.append(("water32_631g", molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10), False, None, False))
@@ -126,10 +155,11 @@ def main():
         if a.only and a.only not in c[0]:
             continue
         make_case(*c)
-    # MD-only reference build on a few cases (parity target of an MD kernel)
-    if not a.only:
-        for c in cases[:2]:
-            make_case(c[0], c[1], False, None, False, md=True)
+    # MD-only reference build on a few cases (parity target of the MD mode)
+    for c in cases[:2] + fcases:
+        if a.only and a.only not in c[0]:
+            continue
+        make_case(c[0], c[1], False, None, False, md=True)
 
 
 if __name__ == "__main__":

@@ -57,3 +57,21 @@ def test_g_adds_into_caller_array(gpu):
     G = np.full(len(g["G_rand"]), 1.5)
     t.formGmatrix(g["P_rand"], G)
     assert np.abs(G - 1.5 - g["G_rand"]).max() <= TOL_G
+
+
+MD_CASES = golden_cases("*_md.npz", exclude_md=False)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", MD_CASES)
+def test_md_mode_matches_md_reference(gpu, name):
+    """MD for every quartet against the reference built with -DUNOMOL_MD_INTS (f-shell cases included)."""
+    from unomol_gb300.native import ERI_MD, TwoElectronInts
+    g = load_golden(name)
+    t = TwoElectronInts(basis_of(g))
+    t.set_eri_method(ERI_MD)
+    G = t.form_g(g["P_rand"])
+    err = np.abs(G - g["G_rand"]).max()
+    assert err <= TOL_G, f"{name}: max|dG| = {err:.3e}"
+    Ga, Gb = t.form_g_uhf(g["Pa"], g["Pb"])
+    assert max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max()) <= TOL_G

@@ -14,7 +14,7 @@ sys.path.insert(0, ROOT + "/oracle")
 
 TOL_G = 1e-10
 # d-shell and large cases are slow for the single-pass C oracle; they are covered on the GPU
-FAST = [c for c in golden_cases() if not any(s in c for s in ("tzp", "dh95_co2", "dh95_h2"))]
+FAST = [c for c in golden_cases() if not any(s in c for s in ("tzp", "dh95_co2", "dh95_h2", "ccpvqz"))]
 
 
 @pytest.mark.parametrize("name", FAST)

@@ -78,6 +78,8 @@ struct UnomolCtx {
     double schwarz_cut = STORE_CUT;
     int prec_mode = UNOMOL_PREC_FP64;
     int rys_mode = UNOMOL_RYS_REFERENCE;
+    int eri_method = UNOMOL_ERI_REFERENCE;
+    unsigned long long* d_qbits = nullptr;
     int counting = 0;
     double fp32_cut = 1e-10;
     UnomolStats stats{};
@@ -194,6 +196,7 @@ void free_setup(UnomolCtx* c) {
     dfree(c->d_bps);
     dfree(c->d_prefix);
     dfree(c->d_q);
+    dfree(c->d_qbits);
 }
 
 // Work lists for the current Schwarz cutoff (host side; O(npairs * nblocks log npairs)).
@@ -335,7 +338,14 @@ int build_setup(UnomolCtx* ctx) {
             const int cls = pair_class(raw[i].la, raw[i].lb);
             size_t j = i;
             while (j < raw.size() && pair_class(raw[j].la, raw[j].lb) == cls) ++j;
-            CU(launch_schwarz(cls, ctx->d_pairs, ctx->d_prims, (int)i, (int)(j - i), ctx->nt, ctx->d_rys, ctx->d_q, ctx->stream));
+            if (cls < NTMPLCLASS) {
+                CU(launch_schwarz(cls, ctx->d_pairs, ctx->d_prims, (int)i, (int)(j - i), ctx->nt, ctx->d_rys, ctx->d_q,
+                                  ctx->stream));
+            } else {
+                if (!ctx->d_qbits) CU(cudaMalloc(&ctx->d_qbits, sizeof(unsigned long long) * raw.size()));
+                CU(launch_schwarz_high(pc_la(cls), pc_lb(cls), ctx->d_pairs, ctx->d_prims, (int)i, (int)(j - i), ctx->nt,
+                                       ctx->d_rys, ctx->d_q, ctx->d_qbits, ctx->stream));
+            }
             i = j;
         }
     }
@@ -622,6 +632,16 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         CU(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 2 * ncls * 32, s));
         A.counters = ctx->d_counters;
     }
+    // one class: the reference's integral method (Rys for la+lb+lc+ld <= 8, MD above:
+    // TwoElectronInts.cpp:658-666; MD everywhere in the MD mode), templated kernels for s/p/d
+    auto launch_class = [&](const ClassLaunch& L, bool fp32) -> cudaError_t {
+        const int la = pc_la(L.bc), lb = pc_lb(L.bc), lc = pc_la(L.kc), ld = pc_lb(L.kc);
+        if (ctx->eri_method == UNOMOL_ERI_MD || la + lb + lc + ld > 8) return launch_fock_md(la, lb, lc, ld, uhf, A, ctx->nt, s);
+        if (L.bc < NTMPLCLASS && L.kc < NTMPLCLASS)
+            return fp32 ? launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s)
+                        : launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s);
+        return launch_fock_generic(la, lb, lc, ld, uhf, fp32, A, ctx->nt, ctx->d_rys, ctx->d_rys32, s);
+    };
     for (const ClassLaunch& L : ctx->launches) {
         A.bps = ctx->d_bps + L.bp_begin;
         A.prefix = ctx->d_prefix;
@@ -630,19 +650,19 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         A.counter_base = (L.bc * NPAIRCLASS + L.kc) * 32;  // FP32 launches use the second half
         if (!mixed) {
             A.mode = 0;
-            CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
+            CU(launch_class(L, false));
             ++launches;
         } else {
             A.mode = 1;
             A.dyn_prefix = ctx->d_pre64;
             A.dyn_count = ctx->d_cnt64 + L.bp_begin;
-            CU(launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s));
+            CU(launch_class(L, false));
             if (ctx->fp32_cut > ctx->skip_cut) {
                 A.mode = 2;
                 A.dyn_prefix = ctx->d_pre32;
                 A.dyn_count = ctx->d_cnt32 + L.bp_begin;
                 A.counter_base += ncls * 32;
-                CU(launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s));
+                CU(launch_class(L, true));
                 ++launches;
             }
             ++launches;
@@ -737,7 +757,7 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
     int np = 0, off = 0;
     for (int i = 0; i < b->nshell; ++i) {
         const int l = b->shell_l[i];
-        if (l < 0 || l > LMAX) return fail(nullptr, UNOMOL_EINVAL, "shell angular momentum above 2 is not supported by this build");
+        if (l < 0 || l > LMAX) return fail(nullptr, UNOMOL_EINVAL, "shell angular momentum above 4 (g) is not supported (Basis.hpp:222)");
         if (b->shell_nprim[i] <= 0) return fail(nullptr, UNOMOL_EINVAL, "shell with no primitives");
         if (b->shell_center[i] < 0 || b->shell_center[i] >= b->ncen) return fail(nullptr, UNOMOL_EINVAL, "shell centre out of range");
         if (b->shell_offset[i] != off) return fail(nullptr, UNOMOL_EINVAL, "shell offsets must follow shell order");
@@ -819,6 +839,13 @@ int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cut) {
 int unomol_gpu_set_density_screening(UnomolCtx* ctx, double skip_cut) {
     if (!ctx || !(skip_cut >= 0.0)) return fail(ctx, UNOMOL_EINVAL, "bad density screening cutoff");
     ctx->skip_cut = skip_cut;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_set_eri_method(UnomolCtx* ctx, int method) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    if (method != UNOMOL_ERI_REFERENCE && method != UNOMOL_ERI_MD) return fail(ctx, UNOMOL_EINVAL, "unknown ERI method");
+    ctx->eri_method = method;
     return UNOMOL_OK;
 }
 

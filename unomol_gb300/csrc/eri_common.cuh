@@ -6,8 +6,10 @@
 
 namespace ugb {
 
-constexpr int LMAX = 2;                 // angular momentum handled by the templated Rys kernels
+constexpr int LMAX = 4;                 // largest shell angular momentum (g; Basis.hpp:222)
+constexpr int LTMPL = 2;                // shells up to d have class-templated Rys kernels
 constexpr int NPAIRCLASS = (LMAX + 1) * (LMAX + 2) / 2;  // (la >= lb) pair classes
+constexpr int NTMPLCLASS = (LTMPL + 1) * (LTMPL + 2) / 2;
 constexpr double SRTERM = 34.9868366552497250;  // 2 pi^{5/2} (TwoElectronInts.cpp:427)
 constexpr double PRIM_CUT = 1.e-12;     // primitive prefactor cut (TwoElectronInts.cpp:428,478-479)
 constexpr double STORE_CUT = 1.e-14;    // integral storage cut (TwoElectronInts.cpp:517,668)

@@ -299,7 +299,7 @@ __device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellP
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& bra, const ShellPair& ket,
                                           bool same_pair, const R (&acc)[QClass<LA, LB, LC, LD>::NF],
-                                          const double (&nrm)[LMAX + 1][6]) {
+                                          const double (&nrm)[LMAX + 1][15]) {
     // The density contraction runs in the kernel's own type R (FP32 in the FP32 kernels, on an FP32
     // copy of P); only the partial sums reach the FP64 accumulator T.  The degeneracy factor is applied
     // to those sums, and the storage cut compares magnitudes as integers (no FP64 compare).
@@ -414,7 +414,7 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
 }
 
 struct NormTable {
-    double v[LMAX + 1][6];
+    double v[LMAX + 1][15];
 };
 
 // Optional work counter: primitive quartets past the prefactor cut, summed over the converged lanes of
@@ -479,16 +479,17 @@ namespace ugb {
 // Generic path for the classes with more than 81 function quartets (d shells): the same
 // arithmetic with runtime angular momenta and loops, the integrals in thread-local memory.
 // ---------------------------------------------------------------------------------------------
-constexpr int GEN_LMAX = 2;
+constexpr int GEN_LMAX = LMAX;  // shells up to g, classes with la+lb+lc+ld <= 8 (the Rys domain)
+constexpr int GEN_L2 = 8;       // largest la+lb (or lc+ld) of such a class
 constexpr int GEN_NC = (GEN_LMAX + 1) * (GEN_LMAX + 2) / 2;
-constexpr int GEN_NF = GEN_NC * GEN_NC * GEN_NC * GEN_NC;
-constexpr int GEN_NI = (GEN_LMAX + 1) * (GEN_LMAX + 1) * (GEN_LMAX + 1) * (GEN_LMAX + 1);
+constexpr int GEN_NF = 1296;    // most function quartets of a class with la+lb+lc+ld <= 8: (dd|dd)
+constexpr int GEN_NI = 81;      // most 1D transfer values (la+1)(lb+1)(lc+1)(ld+1) of such a class
 
 template <typename R>
 __device__ void rys_axis_rt(int la, int lb, int lc, int ld, R g00, R C, R Cp, R B00, R B1, R B1p, R AB,
                             R CD, R* I) {
     const int L12 = la + lb, L34 = lc + ld;
-    R G[2 * GEN_LMAX + 1][2 * GEN_LMAX + 1];
+    R G[GEN_L2 + 1][GEN_L2 + 1];
     G[0][0] = g00;
     if (L12 > 0) G[1][0] = C * g00;
     for (int i = 1; i < L12; ++i) G[i + 1][0] = C * G[i][0] + R(i) * B1 * G[i - 1][0];
@@ -499,7 +500,7 @@ __device__ void rys_axis_rt(int la, int lb, int lc, int ld, R g00, R C, R Cp, R 
             if (i > 0) v = fma(R(i) * B00, G[i - 1][j], v);
             G[i][j + 1] = v;
         }
-    R X[GEN_LMAX + 1][2 * GEN_LMAX + 1][2 * GEN_LMAX + 1];
+    R X[GEN_LMAX + 1][GEN_L2 + 1][GEN_L2 + 1];
     for (int a = 0; a <= L12; ++a)
         for (int j = 0; j <= L34; ++j) X[0][a][j] = G[a][j];
     for (int b = 1; b <= lb; ++b)
@@ -507,7 +508,7 @@ __device__ void rys_axis_rt(int la, int lb, int lc, int ld, R g00, R C, R Cp, R 
             for (int j = 0; j <= L34; ++j) X[b][a][j] = fma(AB, X[b - 1][a][j], X[b - 1][a + 1][j]);
     for (int a = 0; a <= la; ++a)
         for (int b = 0; b <= lb; ++b) {
-            R Y[GEN_LMAX + 1][2 * GEN_LMAX + 1];
+            R Y[GEN_LMAX + 1][GEN_L2 + 1];
             for (int c = 0; c <= L34; ++c) Y[0][c] = X[b][a][c];
             for (int d = 1; d <= ld; ++d)
                 for (int c = 0; c <= L34 - d; ++c) Y[d][c] = fma(CD, Y[d - 1][c], Y[d - 1][c + 1]);

@@ -24,10 +24,12 @@ EXPORTS = [
     "unomol_gpu_set_screening", "unomol_gpu_set_rys_mode", "unomol_gpu_get_stats", "unomol_gpu_destroy",
     "unomol_gpu_last_error", "unomol_gpu_version", "unomol_gpu_set_counting", "unomol_gpu_fma_peak",
     "unomol_gpu_last_build_ms", "unomol_gpu_set_density_screening", "unomol_gpu_fock_rhf_noalloc",
-    "unomol_one_electron", "unomol_scf",
+    "unomol_one_electron", "unomol_scf", "unomol_gpu_set_eri_method",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
+ERI_REFERENCE = 0
+ERI_MD = 1
 
 
 class BasisDesc(C.Structure):
@@ -177,6 +179,11 @@ class TwoElectronInts:
         a, b = C.c_double(), C.c_double()
         _check(lib().unomol_gpu_last_build_ms(self._h, C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
+
+    def set_eri_method(self, method: int):
+        """ERI_REFERENCE (Rys for la+lb+lc+ld <= 8, MD above; default) or ERI_MD (MD everywhere)."""
+        lib().unomol_gpu_set_eri_method.argtypes = [C.c_void_p, C.c_int]
+        _check(lib().unomol_gpu_set_eri_method(self._h, int(method)), self._h)
 
     def set_density_screening(self, skip_cut: float):
         lib().unomol_gpu_set_density_screening.argtypes = [C.c_void_p, C.c_double]
