@@ -169,6 +169,29 @@ int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, double* dG, vo
 
 void unomol_gpu_destroy(UnomolCtx* ctx);
 
+/* ---- Batches of molecules (no reference counterpart: the reference handles one molecule) ----
+ * Many molecules of uneven size share one launch per quartet class: their shell pairs and Schwarz
+ * staircases are merged, and a persistent kernel per class pulls tiles of work from an atomic counter.
+ * The batch owns a packed P and a packed G buffer on the device (molecule m at packed_offsets[m]);
+ * a build writes G = G(P) for every molecule (RHF, FP64, shells up to d). */
+typedef struct UnomolBatch UnomolBatch;
+#define UNOMOL_BATCH_GRAPH 0      /* the batched build captured once as a CUDA graph, then replayed */
+#define UNOMOL_BATCH_LAUNCHES 1   /* the batched build as plain launches on the stream */
+#define UNOMOL_BATCH_SEQUENTIAL 2 /* one molecule after the other (the single-molecule path), for comparison */
+int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch** out);
+int unomol_gpu_batch_buffers(UnomolBatch* batch, double** dP, double** dG, const long long** packed_offsets,
+                             int64_t* packed_total);
+int unomol_gpu_batch_fock(UnomolBatch* batch, int mode, void* stream);
+/* Autotuner: times every (CTA size 64/128/256, CTAs per SM 1/2/4/8) per class launch on the current P
+ * and keeps the fastest; chosen (optional, 3 ints per launch): class id, CTA size, CTAs per SM.
+ * Returns the number of launches (>= 0) or an error code. */
+int unomol_gpu_batch_autotune(UnomolBatch* batch, int reps, int* chosen);
+/* host copies of the batch's packed P (in) and G (out), all molecules concatenated */
+int unomol_gpu_batch_set_density(UnomolBatch* batch, const double* P);
+int unomol_gpu_batch_get_fock(UnomolBatch* batch, double* G);
+void unomol_gpu_batch_destroy(UnomolBatch* batch);
+const char* unomol_gpu_batch_last_error(const UnomolBatch* batch);
+
 /* ---- SCF layer (the callers of the Fock build) ---- */
 
 /* One-electron integrals S, T and H = T + V, packed (the data of OneElectronInts, OneElectronInts.cpp:

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/unomol_gb300.h"
+#include "ctx_view.h"
 #include "fock_dispatch.cuh"
 #include "fock_kernels.cuh"
 
@@ -728,6 +729,26 @@ int finish_timing(UnomolCtx* ctx, cudaStream_t s) {
 }
 
 }  // namespace
+
+namespace ugb {
+
+CtxView ctx_view(const UnomolCtx* c) {
+    CtxView v;
+    v.nbf = c->nbf;
+    v.nshell = c->nshell;
+    v.rys_compat = c->rys_mode == UNOMOL_RYS_REFERENCE;
+    v.eri_method = c->eri_method;
+    v.pairs = &c->pairs;
+    v.prims = &c->prims;
+    v.bps = &c->bps;
+    v.prefix = &c->prefix;
+    for (const ClassLaunch& L : c->launches) v.launches.push_back({L.bc, L.kc, L.bp_begin, L.nbp, L.nwork, L.quartets});
+    v.nt = c->nt;
+    v.d_rys = c->d_rys;
+    return v;
+}
+
+}  // namespace ugb
 
 extern "C" {
 

@@ -102,6 +102,11 @@ struct FockArgs {
     const int* dyn_mseg;          // per bra row: length of its FP64 segment (the FP32 segment follows it)
     const float* dmax;            // [0]: max |P| over all shell-pair blocks
     double skip_cut;              // quartets with bound * max|P| below this are skipped
+    // batches of molecules: ShellPair::pad holds the molecule; its dense P / T start at mol_base and
+    // have mol_nbf rows (nullptr: one molecule, A.nbf rows at offset 0)
+    const int* mol_nbf;
+    const long long* mol_base;
+    unsigned long long* tile_counter;  // persistent launches: next tile of this launch
     int* status;                // device error flag
 };
 

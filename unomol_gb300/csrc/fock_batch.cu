@@ -1,0 +1,430 @@
+// Batched Fock build over many molecules (the batching form): merged work lists, one persistent kernel
+// per quartet class pulling tiles from an atomic counter, the whole build captured as a CUDA graph,
+// and an autotuner choosing the CTA size (quartets per tile) and the CTAs per SM of every class.
+// FP64, RHF, shells up to d (the batch workload is s/p).
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/unomol_gb300.h"
+#include "ctx_view.h"
+#include "fock_dispatch.cuh"
+
+using namespace ugb;
+
+namespace {
+
+template <int BC, int KC>
+cudaError_t persistent_one(const FockArgs& A, const NormTable& nt, const double* rys, int grid, int block, cudaStream_t s) {
+    constexpr int LA = pc_la(BC), LB = pc_lb(BC), LC = pc_la(KC), LD = pc_lb(KC);
+    if constexpr (QClass<LA, LB, LC, LD>::NF <= 81) {
+        fock_jk_persistent<LA, LB, LC, LD, false, double><<<grid, block, 0, s>>>(A, nt, rys);
+    } else {
+        // large classes: one item per thread over the whole launch
+        fock_jk_generic<false, double, PrimPair><<<(unsigned)((A.nwork + 63) / 64), 64, 0, s>>>(A, nt, rys, A.prims, LA, LB, LC, LD);
+    }
+    return cudaGetLastError();
+}
+
+#define UGB_CASE(BC, KC) \
+    case (BC) * 8 + (KC): \
+        return persistent_one<BC, KC>(A, nt, rys, grid, block, s);
+
+cudaError_t launch_persistent(int bc, int kc, const FockArgs& A, const NormTable& nt, const double* rys, int grid,
+                              int block, cudaStream_t s) {
+    switch (bc * 8 + kc) {
+#include "fock_cases.inc"
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+#undef UGB_CASE
+
+// dense <- packed for every molecule of the batch
+__global__ void batch_expand(const double* __restrict__ pk, const long long* __restrict__ poff, double* __restrict__ full,
+                             const long long* __restrict__ doff, const int* __restrict__ nbf, int nmol, long long total) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    int lo = 0, hi = nmol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (doff[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const int n = nbf[lo];
+    const long long r = t - doff[lo];
+    const int i = (int)(r / n), j = (int)(r % n);
+    const int a = i > j ? i : j, b = i > j ? j : i;
+    full[t] = pk[poff[lo] + (long long)a * (a + 1) / 2 + b];
+}
+
+// packed G = T + T^T for every molecule
+__global__ void batch_fold(const double* __restrict__ T, const long long* __restrict__ doff, double* __restrict__ G,
+                           const long long* __restrict__ poff, const int* __restrict__ nbf, int nmol, long long total) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    int lo = 0, hi = nmol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (poff[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const int n = nbf[lo];
+    const long long r = t - poff[lo];
+    int i = (int)((sqrt(8.0 * (double)r + 1.0) - 1.0) * 0.5);
+    while ((long long)i * (i + 1) / 2 > r) --i;
+    while ((long long)(i + 1) * (i + 2) / 2 <= r) ++i;
+    const int j = (int)(r - (long long)i * (i + 1) / 2);
+    const double* Tm = T + doff[lo];
+    G[t] = Tm[(long long)i * n + j] + Tm[(long long)j * n + i];
+}
+
+struct BLaunch {
+    int bc, kc, bp_begin, nbp;
+    long long nwork;
+    int block = 128, ctas_per_sm = 4;
+};
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+thread_local std::string g_batch_err;
+
+}  // namespace
+
+struct UnomolBatch {
+    std::vector<UnomolCtx*> mols;
+    std::vector<int> nbf;
+    std::vector<long long> doff, poff;  // dense / packed offsets per molecule (+ total at the end)
+    long long dense_total = 0, packed_total = 0;
+    ShellPair* d_pairs = nullptr;
+    PrimPair* d_prims = nullptr;
+    BlockPair* d_bps = nullptr;
+    long long* d_prefix = nullptr;
+    int* d_nbf = nullptr;
+    long long *d_doff = nullptr, *d_poff = nullptr;
+    double *d_P = nullptr, *d_G = nullptr, *d_Pfull = nullptr, *d_T = nullptr;
+    unsigned long long* d_tiles = nullptr;
+    std::vector<BLaunch> launches;
+    NormTable nt{};
+    const double* rys = nullptr;
+    int rys_compat = 1;
+    int nsm = 152;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    std::string err;
+};
+
+namespace {
+
+int bfail(UnomolBatch* b, int code, const std::string& m) {
+    if (b) b->err = m;
+    g_batch_err = m;
+    return code;
+}
+
+#define BCU(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return bfail(b, e_ == cudaErrorMemoryAllocation ? UNOMOL_ENOMEM : UNOMOL_ECUDA,       \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+    } while (0)
+
+FockArgs batch_args(UnomolBatch* b, const BLaunch& L, int k) {
+    FockArgs A{};
+    A.pairs = b->d_pairs;
+    A.prims = b->d_prims;
+    A.bps = b->d_bps + L.bp_begin;
+    A.prefix = b->d_prefix;
+    A.nbp = L.nbp;
+    A.nwork = L.nwork;
+    A.nbf = 0;
+    A.Pa = b->d_Pfull;
+    A.Ta = b->d_T;
+    A.thr_int = STORE_CUT;
+    A.prim_cut = PRIM_CUT;
+    A.rys_compat = b->rys_compat;
+    A.mol_nbf = b->d_nbf;
+    A.mol_base = b->d_doff;
+    A.tile_counter = b->d_tiles + k;
+    A.mode = 0;
+    return A;
+}
+
+// the batched build on stream s (persistent launches); G = G(P) for every molecule
+int batch_build(UnomolBatch* b, cudaStream_t s) {
+    const int nmol = (int)b->mols.size();
+    batch_expand<<<(unsigned)((b->dense_total + 255) / 256), 256, 0, s>>>(b->d_P, b->d_poff, b->d_Pfull, b->d_doff, b->d_nbf,
+                                                                          nmol, b->dense_total);
+    BCU(cudaGetLastError());
+    BCU(cudaMemsetAsync(b->d_T, 0, sizeof(double) * b->dense_total, s));
+    BCU(cudaMemsetAsync(b->d_tiles, 0, sizeof(unsigned long long) * std::max<size_t>(1, b->launches.size()), s));
+    for (size_t k = 0; k < b->launches.size(); ++k) {
+        const BLaunch& L = b->launches[k];
+        const FockArgs A = batch_args(b, L, (int)k);
+        BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, s));
+    }
+    batch_fold<<<(unsigned)((b->packed_total + 255) / 256), 256, 0, s>>>(b->d_T, b->d_doff, b->d_G, b->d_poff, b->d_nbf,
+                                                                         nmol, b->packed_total);
+    BCU(cudaGetLastError());
+    return UNOMOL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch** out) {
+    UnomolBatch* b = nullptr;
+    if (!bases || nmol <= 0 || !out) return bfail(nullptr, UNOMOL_EINVAL, "bad batch arguments");
+    *out = nullptr;
+    b = new UnomolBatch();
+    auto cleanup = [&](int rc) {
+        unomol_gpu_batch_destroy(b);
+        return rc;
+    };
+    std::vector<ShellPair> pairs;
+    std::vector<PrimPair> prims;
+    std::vector<long long> prefix;
+    std::vector<std::vector<BlockPair>> per_class(NTMPLCLASS * NTMPLCLASS);
+    long long dense = 0, packed = 0;
+    for (int m = 0; m < nmol; ++m) {
+        UnomolCtx* c = nullptr;
+        int rc = unomol_gpu_create(&bases[m], 0, &c);
+        if (rc) {
+            bfail(b, rc, std::string("molecule ") + std::to_string(m) + ": " + unomol_gpu_last_error(nullptr));
+            return cleanup(rc);
+        }
+        b->mols.push_back(c);
+        const CtxView v = ctx_view(c);
+        if (m == 0) {
+            b->nt = v.nt;
+            b->rys = v.d_rys;
+            b->rys_compat = v.rys_compat;
+        }
+        const int pair0 = (int)pairs.size(), prim0 = (int)prims.size(), pre0 = (int)prefix.size();
+        for (ShellPair sp : *v.pairs) {
+            sp.prim_begin += prim0;
+            sp.pad = m;
+            pairs.push_back(sp);
+        }
+        prims.insert(prims.end(), v.prims->begin(), v.prims->end());
+        prefix.insert(prefix.end(), v.prefix->begin(), v.prefix->end());
+        for (const ClassLaunchInfo& L : v.launches) {
+            if (L.bc >= NTMPLCLASS || L.kc >= NTMPLCLASS) {
+                bfail(b, UNOMOL_EINVAL, "batched build: shells above d are not supported");
+                return cleanup(UNOMOL_EINVAL);
+            }
+            for (int k = 0; k < L.nbp; ++k) {
+                BlockPair bp = (*v.bps)[L.bp_begin + k];
+                bp.bra_begin += pair0;
+                bp.ket_begin += pair0;
+                bp.prefix_off += pre0;
+                per_class[L.bc * NTMPLCLASS + L.kc].push_back(bp);
+            }
+        }
+        b->nbf.push_back(v.nbf);
+        b->doff.push_back(dense);
+        b->poff.push_back(packed);
+        dense += (long long)v.nbf * v.nbf;
+        packed += (long long)v.nbf * (v.nbf + 1) / 2;
+    }
+    b->dense_total = dense;
+    b->packed_total = packed;
+    // launches: one per class over all molecules, work ranges 32-aligned (warps never straddle)
+    std::vector<BlockPair> bps;
+    for (int cls = 0; cls < NTMPLCLASS * NTMPLCLASS; ++cls) {
+        auto& v = per_class[cls];
+        if (v.empty()) continue;
+        BLaunch L;
+        L.bc = cls / NTMPLCLASS;
+        L.kc = cls % NTMPLCLASS;
+        L.bp_begin = (int)bps.size();
+        L.nbp = (int)v.size();
+        long long w = 0;
+        for (auto& bp : v) {
+            bp.work_begin = w;
+            w += (bp.work_count + 31) / 32 * 32;
+            bps.push_back(bp);
+        }
+        L.nwork = w;
+        b->launches.push_back(L);
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
+    BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    BCU(cudaMalloc(&b->d_pairs, sizeof(ShellPair) * std::max<size_t>(1, pairs.size())));
+    BCU(cudaMalloc(&b->d_prims, sizeof(PrimPair) * std::max<size_t>(1, prims.size())));
+    BCU(cudaMalloc(&b->d_bps, sizeof(BlockPair) * std::max<size_t>(1, bps.size())));
+    BCU(cudaMalloc(&b->d_prefix, sizeof(long long) * std::max<size_t>(1, prefix.size())));
+    BCU(cudaMalloc(&b->d_nbf, sizeof(int) * nmol));
+    BCU(cudaMalloc(&b->d_doff, sizeof(long long) * nmol));
+    BCU(cudaMalloc(&b->d_poff, sizeof(long long) * nmol));
+    BCU(cudaMalloc(&b->d_P, sizeof(double) * packed));
+    BCU(cudaMalloc(&b->d_G, sizeof(double) * packed));
+    BCU(cudaMalloc(&b->d_Pfull, sizeof(double) * dense));
+    BCU(cudaMalloc(&b->d_T, sizeof(double) * dense));
+    BCU(cudaMalloc(&b->d_tiles, sizeof(unsigned long long) * std::max<size_t>(1, b->launches.size())));
+    BCU(cudaMemcpy(b->d_pairs, pairs.data(), sizeof(ShellPair) * pairs.size(), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->d_prims, prims.data(), sizeof(PrimPair) * prims.size(), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->d_bps, bps.data(), sizeof(BlockPair) * bps.size(), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->d_prefix, prefix.data(), sizeof(long long) * prefix.size(), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->d_nbf, b->nbf.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->d_doff, b->doff.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->d_poff, b->poff.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice));
+    BCU(cudaMemset(b->d_P, 0, sizeof(double) * packed));
+    *out = b;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_batch_buffers(UnomolBatch* b, double** dP, double** dG, const long long** packed_offsets, int64_t* packed_total) {
+    if (!b) return bfail(b, UNOMOL_EINVAL, "null batch");
+    if (dP) *dP = b->d_P;
+    if (dG) *dG = b->d_G;
+    if (packed_offsets) *packed_offsets = b->poff.data();
+    if (packed_total) *packed_total = b->packed_total;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_batch_fock(UnomolBatch* b, int mode, void* stream) {
+    if (!b) return bfail(b, UNOMOL_EINVAL, "null batch");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    if (mode == UNOMOL_BATCH_GRAPH) {
+        if (!b->graph) {
+            cudaGraph_t g = nullptr;
+            BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = batch_build(b, b->stream);
+            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            if (rc) return rc;
+            BCU(e);
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            BCU(e);
+        }
+        if (s != b->stream) {  // order the graph after the caller's stream and back
+            cudaEvent_t ev;
+            BCU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            BCU(cudaEventRecord(ev, s));
+            BCU(cudaStreamWaitEvent(b->stream, ev, 0));
+            BCU(cudaGraphLaunch(b->graph, b->stream));
+            BCU(cudaEventRecord(ev, b->stream));
+            BCU(cudaStreamWaitEvent(s, ev, 0));
+            cudaEventDestroy(ev);
+            return UNOMOL_OK;
+        }
+        BCU(cudaGraphLaunch(b->graph, b->stream));
+        return UNOMOL_OK;
+    }
+    if (mode == UNOMOL_BATCH_LAUNCHES) return batch_build(b, s);
+    if (mode == UNOMOL_BATCH_SEQUENTIAL) {  // one molecule after the other through the single-molecule path
+        BCU(cudaMemsetAsync(b->d_G, 0, sizeof(double) * b->packed_total, s));
+        for (size_t m = 0; m < b->mols.size(); ++m) {
+            int rc = unomol_gpu_fock_rhf_device(b->mols[m], b->d_P + b->poff[m], b->d_G + b->poff[m], s);
+            if (rc) return bfail(b, rc, unomol_gpu_last_error(b->mols[m]));
+        }
+        return UNOMOL_OK;
+    }
+    return bfail(b, UNOMOL_EINVAL, "unknown batch mode");
+}
+
+// Autotuner: for every class launch, time each (CTA size, CTAs per SM) and keep the fastest; the
+// CUDA graph is rebuilt on the next graph launch.  Uses the densities currently in the P buffer.
+int unomol_gpu_batch_autotune(UnomolBatch* b, int reps, int* chosen) {
+    if (!b) return bfail(b, UNOMOL_EINVAL, "null batch");
+    if (reps <= 0) reps = 2;
+    const int blocks[3] = {64, 128, 256};
+    const int ctas[4] = {1, 2, 4, 8};
+    cudaStream_t s = b->stream;
+    int rc = batch_build(b, s);  // dense P in place
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    BCU(cudaEventCreate(&e0));
+    BCU(cudaEventCreate(&e1));
+    for (size_t k = 0; k < b->launches.size(); ++k) {
+        BLaunch& L = b->launches[k];
+        float best = 1e30f;
+        int bb = L.block, bc = L.ctas_per_sm;
+        for (int blk : blocks)
+            for (int c : ctas) {
+                float tot = 0.f;
+                for (int r = 0; r < reps; ++r) {
+                    BCU(cudaMemsetAsync(b->d_tiles + k, 0, sizeof(unsigned long long), s));
+                    FockArgs A = batch_args(b, L, (int)k);
+                    BCU(cudaEventRecord(e0, s));
+                    BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * c, blk, s));
+                    BCU(cudaEventRecord(e1, s));
+                    BCU(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    tot += ms;
+                }
+                if (tot < best) {
+                    best = tot;
+                    bb = blk;
+                    bc = c;
+                }
+            }
+        L.block = bb;
+        L.ctas_per_sm = bc;
+        if (chosen) {
+            chosen[3 * k + 0] = L.bc * NTMPLCLASS + L.kc;
+            chosen[3 * k + 1] = bb;
+            chosen[3 * k + 2] = bc;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    BCU(cudaMemsetAsync(b->d_T, 0, sizeof(double) * b->dense_total, s));  // leave no partial sums
+    BCU(cudaStreamSynchronize(s));
+    return (int)b->launches.size();
+}
+
+int unomol_gpu_batch_set_density(UnomolBatch* b, const double* P) {
+    if (!b || !P) return bfail(b, UNOMOL_EINVAL, "null argument");
+    BCU(cudaMemcpyAsync(b->d_P, P, sizeof(double) * b->packed_total, cudaMemcpyHostToDevice, b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_batch_get_fock(UnomolBatch* b, double* G) {
+    if (!b || !G) return bfail(b, UNOMOL_EINVAL, "null argument");
+    BCU(cudaDeviceSynchronize());
+    BCU(cudaMemcpy(G, b->d_G, sizeof(double) * b->packed_total, cudaMemcpyDeviceToHost));
+    return UNOMOL_OK;
+}
+
+void unomol_gpu_batch_destroy(UnomolBatch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    dfree(b->d_pairs);
+    dfree(b->d_prims);
+    dfree(b->d_bps);
+    dfree(b->d_prefix);
+    dfree(b->d_nbf);
+    dfree(b->d_doff);
+    dfree(b->d_poff);
+    dfree(b->d_P);
+    dfree(b->d_G);
+    dfree(b->d_Pfull);
+    dfree(b->d_T);
+    dfree(b->d_tiles);
+    for (UnomolCtx* c : b->mols) unomol_gpu_destroy(c);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char* unomol_gpu_batch_last_error(const UnomolBatch* b) {
+    if (b && !b->err.empty()) return b->err.c_str();
+    return g_batch_err.c_str();
+}
+
+}  // extern "C"

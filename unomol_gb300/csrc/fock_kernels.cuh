@@ -305,7 +305,14 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
     // to those sums, and the storage cut compares magnitudes as integers (no FP64 compare).
     using Q = QClass<LA, LB, LC, LD>;
     constexpr bool UNIT_NORMS = LA < 2 && LB < 2 && LC < 2 && LD < 2;  // all component factors are 1
-    const int N = A.nbf;
+    int N = A.nbf;
+    long long base = 0;
+    if (A.mol_nbf) {  // batch of molecules: this molecule's dense matrices
+        N = A.mol_nbf[bra.pad];
+        base = A.mol_base[bra.pad];
+    }
+    double* __restrict__ Ta = A.Ta + base;
+    double* __restrict__ Tb = UHF ? A.Tb + base : nullptr;
     R deg = R(1);
     if (bra.same) deg *= R(0.5);
     if (ket.same) deg *= R(0.5);
@@ -313,11 +320,11 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
     const R* __restrict__ Pa;
     const R* __restrict__ Pb;
     if constexpr (sizeof(R) == 8) {
-        Pa = reinterpret_cast<const R*>(A.Pa);
-        Pb = reinterpret_cast<const R*>(A.Pb);
+        Pa = reinterpret_cast<const R*>(A.Pa) + base;
+        Pb = UHF ? reinterpret_cast<const R*>(A.Pb) + base : nullptr;
     } else {
-        Pa = reinterpret_cast<const R*>(A.Pa32);
-        Pb = reinterpret_cast<const R*>(A.Pb32);
+        Pa = reinterpret_cast<const R*>(A.Pa32) + base;
+        Pb = UHF ? reinterpret_cast<const R*>(A.Pb32) + base : nullptr;
     }
     const R jf = UHF ? R(2) : R(4);
     R jcd[Q::NC * Q::ND];
@@ -370,20 +377,20 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
                 }
             }
             const double j = double(jf * deg * jab);
-            atomicAdd(A.Ta + a * N + b, j);
-            if constexpr (UHF) atomicAdd(A.Tb + a * N + b, j);
+            atomicAdd(Ta +a * N + b, j);
+            if constexpr (UHF) atomicAdd(Tb +a * N + b, j);
         }
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic) {
             const int c = ket.a_off + ic;
-            atomicAdd(A.Ta + a * N + c, double(-deg * kac[ic]));
-            if constexpr (UHF) atomicAdd(A.Tb + a * N + c, double(-deg * kacB[ic]));
+            atomicAdd(Ta +a * N + c, double(-deg * kac[ic]));
+            if constexpr (UHF) atomicAdd(Tb +a * N + c, double(-deg * kacB[ic]));
         }
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int d = ket.b_off + id;
-            atomicAdd(A.Ta + a * N + d, double(-deg * kad[id]));
-            if constexpr (UHF) atomicAdd(A.Tb + a * N + d, double(-deg * kadB[id]));
+            atomicAdd(Ta +a * N + d, double(-deg * kad[id]));
+            if constexpr (UHF) atomicAdd(Tb +a * N + d, double(-deg * kadB[id]));
         }
     }
 #pragma unroll
@@ -392,8 +399,8 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
         for (int id = 0; id < Q::ND; ++id) {
             const int c = ket.a_off + ic, d = ket.b_off + id;
             const double j = double(jf * deg * jcd[ic * Q::ND + id]);
-            atomicAdd(A.Ta + c * N + d, j);
-            if constexpr (UHF) atomicAdd(A.Tb + c * N + d, j);
+            atomicAdd(Ta +c * N + d, j);
+            if constexpr (UHF) atomicAdd(Tb +c * N + d, j);
         }
 #pragma unroll
     for (int ib = 0; ib < Q::NB; ++ib) {
@@ -401,14 +408,14 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic) {
             const int c = ket.a_off + ic;
-            atomicAdd(A.Ta + b * N + c, double(-deg * kbc[ib * Q::NC + ic]));
-            if constexpr (UHF) atomicAdd(A.Tb + b * N + c, double(-deg * kbcB[ib * Q::NC + ic]));
+            atomicAdd(Ta +b * N + c, double(-deg * kbc[ib * Q::NC + ic]));
+            if constexpr (UHF) atomicAdd(Tb +b * N + c, double(-deg * kbcB[ib * Q::NC + ic]));
         }
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int d = ket.b_off + id;
-            atomicAdd(A.Ta + b * N + d, double(-deg * kbd[ib * Q::ND + id]));
-            if constexpr (UHF) atomicAdd(A.Tb + b * N + d, double(-deg * kbdB[ib * Q::ND + id]));
+            atomicAdd(Ta +b * N + d, double(-deg * kbd[ib * Q::ND + id]));
+            if constexpr (UHF) atomicAdd(Tb +b * N + d, double(-deg * kbdB[ib * Q::ND + id]));
         }
     }
 }
@@ -427,9 +434,8 @@ __device__ __forceinline__ void count_flush(const FockArgs& A, unsigned v) {
 }
 
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
-__global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
+__device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt, const R* __restrict__ rys, long long g) {
     using Q = QClass<LA, LB, LC, LD>;
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bi, ki;
     unsigned npass = 0;
     if (!(A.mode == 0 ? decode_work(A, g, bi, ki) : decode_work_dyn(A, g, bi, ki))) return;
@@ -445,6 +451,28 @@ __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const No
                                                          A.counters ? &npass : nullptr);
     digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt.v);
     if (A.counters) count_flush(A, npass);
+}
+
+template <int LA, int LB, int LC, int LD, bool UHF, typename R>
+__global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
+    fock_item<LA, LB, LC, LD, UHF, R>(A, nt, rys, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Persistent form for batches of molecules: a fixed grid of CTAs (a few per SM) pulls tiles of
+// blockDim consecutive work items from an atomic counter until the launch's work is done, so that
+// molecules of uneven size balance across the GPU in one launch per class.  Tiles follow the work
+// order (block pairs of one molecule are contiguous), which keeps a tile's warps uniform.
+template <int LA, int LB, int LC, int LD, bool UHF, typename R>
+__global__ void __launch_bounds__(256) fock_jk_persistent(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
+    __shared__ long long tile;
+    for (;;) {
+        if (threadIdx.x == 0) tile = (long long)atomicAdd(A.tile_counter, 1ull);
+        __syncthreads();
+        const long long g0 = tile * blockDim.x;
+        __syncthreads();
+        if (g0 >= A.nwork) return;
+        fock_item<LA, LB, LC, LD, UHF, R>(A, nt, rys, g0 + threadIdx.x);
+    }
 }
 
 // Schwarz diagonal: q[pair] = sqrt(max_{a,b} |(ab|ab)|) for every pair of one class (no primitive
@@ -586,13 +614,20 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
         }
     }
     // density contraction and scatter, as digest_jk with runtime sizes
-    const int N = A.nbf;
+    int N = A.nbf;
+    long long base = 0;
+    if (A.mol_nbf) {
+        N = A.mol_nbf[bra.pad];
+        base = A.mol_base[bra.pad];
+    }
+    double* __restrict__ Ta = A.Ta + base;
+    double* __restrict__ Tb = UHF ? A.Tb + base : nullptr;
     double deg = 1.0;
     if (bra.same) deg *= 0.5;
     if (ket.same) deg *= 0.5;
     if (bi == ki) deg *= 0.5;
-    const double* __restrict__ Pa = A.Pa;
-    const double* __restrict__ Pb = A.Pb;
+    const double* __restrict__ Pa = A.Pa + base;
+    const double* __restrict__ Pb = UHF ? A.Pb + base : nullptr;
     int f = 0;
     for (int ia = 0; ia < NA; ++ia) {
         const int a = bra.a_off + ia;
@@ -612,23 +647,23 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
                     if (UHF) Pcd += Pb[c * N + d];
                     jab = fma(v, Pcd, jab);
                     const double jf = UHF ? 2.0 : 4.0;
-                    atomicAdd(A.Ta + c * N + d, jf * v * Pab);
-                    atomicAdd(A.Ta + a * N + c, -v * Pa[b * N + d]);
-                    atomicAdd(A.Ta + a * N + d, -v * Pa[b * N + c]);
-                    atomicAdd(A.Ta + b * N + c, -v * Pa[a * N + d]);
-                    atomicAdd(A.Ta + b * N + d, -v * Pa[a * N + c]);
+                    atomicAdd(Ta +c * N + d, jf * v * Pab);
+                    atomicAdd(Ta +a * N + c, -v * Pa[b * N + d]);
+                    atomicAdd(Ta +a * N + d, -v * Pa[b * N + c]);
+                    atomicAdd(Ta +b * N + c, -v * Pa[a * N + d]);
+                    atomicAdd(Ta +b * N + d, -v * Pa[a * N + c]);
                     if (UHF) {
-                        atomicAdd(A.Tb + c * N + d, jf * v * Pab);
-                        atomicAdd(A.Tb + a * N + c, -v * Pb[b * N + d]);
-                        atomicAdd(A.Tb + a * N + d, -v * Pb[b * N + c]);
-                        atomicAdd(A.Tb + b * N + c, -v * Pb[a * N + d]);
-                        atomicAdd(A.Tb + b * N + d, -v * Pb[a * N + c]);
+                        atomicAdd(Tb +c * N + d, jf * v * Pab);
+                        atomicAdd(Tb +a * N + c, -v * Pb[b * N + d]);
+                        atomicAdd(Tb +a * N + d, -v * Pb[b * N + c]);
+                        atomicAdd(Tb +b * N + c, -v * Pb[a * N + d]);
+                        atomicAdd(Tb +b * N + d, -v * Pb[a * N + c]);
                     }
                 }
             }
             const double jf = UHF ? 2.0 : 4.0;
-            atomicAdd(A.Ta + a * N + b, jf * jab);
-            if (UHF) atomicAdd(A.Tb + a * N + b, jf * jab);
+            atomicAdd(Ta +a * N + b, jf * jab);
+            if (UHF) atomicAdd(Tb +a * N + b, jf * jab);
         }
     }
     if (A.counters) count_flush(A, npass);

@@ -100,6 +100,23 @@ def water_cluster(nw: int, seed: int, box: float = 10.0, dmin: float = 2.7):
     return atoms
 
 
+def batch_workload(seed: int = 0, n: int = 256):
+    """The batching workload: n molecules, half all-trans alkanes C_kH_{2k+2} with k uniform in 1..8,
+    half water clusters of 1..6 monomers (as water_cluster), each in STO-3G or 6-31G by a coin flip;
+    everything from numpy.random.default_rng(seed).  Returns [(label, patin text)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        basis = "STO-3G" if rng.integers(2) == 0 else "6-31G"
+        if i < n // 2:
+            k = int(rng.integers(1, 9))
+            out.append((f"C{k}H{2 * k + 2}/{basis}", patin_text(alkane(k), basis)))
+        else:
+            nw = int(rng.integers(1, 7))
+            out.append((f"(H2O){nw}/{basis}", patin_text(water_cluster(nw, int(rng.integers(1 << 30))), basis)))
+    return out
+
+
 def perturb(atoms, sigma: float, seed: int):
     """Isotropic Gaussian displacement of every atom (Angstrom)."""
     rng = np.random.default_rng(seed)

@@ -24,7 +24,9 @@ EXPORTS = [
     "unomol_gpu_set_screening", "unomol_gpu_set_rys_mode", "unomol_gpu_get_stats", "unomol_gpu_destroy",
     "unomol_gpu_last_error", "unomol_gpu_version", "unomol_gpu_set_counting", "unomol_gpu_fma_peak",
     "unomol_gpu_last_build_ms", "unomol_gpu_set_density_screening", "unomol_gpu_fock_rhf_noalloc",
-    "unomol_one_electron", "unomol_scf", "unomol_gpu_set_eri_method",
+    "unomol_one_electron", "unomol_scf", "unomol_gpu_set_eri_method", "unomol_gpu_batch_create",
+    "unomol_gpu_batch_buffers", "unomol_gpu_batch_fock", "unomol_gpu_batch_autotune", "unomol_gpu_batch_set_density",
+    "unomol_gpu_batch_get_fock", "unomol_gpu_batch_destroy", "unomol_gpu_batch_last_error",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -292,6 +294,78 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
     if keep_densities:
         out["densities"] = dens[:min(keep_densities, res.fock_builds)].copy()
     return out
+
+
+BATCH_GRAPH = 0
+BATCH_LAUNCHES = 1
+BATCH_SEQUENTIAL = 2
+
+
+class Batch:
+    """Many molecules in one batched Fock build (unomol_gpu_batch_*): merged work lists, persistent
+    kernels per quartet class, CUDA-graph replay, autotuned launch shapes."""
+
+    def __init__(self, bases: list):
+        L = lib()
+        L.unomol_gpu_batch_create.argtypes = [C.POINTER(BasisDesc), C.c_int, C.POINTER(C.c_void_p)]
+        L.unomol_gpu_batch_buffers.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                               C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]
+        L.unomol_gpu_batch_fock.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.unomol_gpu_batch_autotune.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.unomol_gpu_batch_set_density.argtypes = [C.c_void_p, _dp]
+        L.unomol_gpu_batch_get_fock.argtypes = [C.c_void_p, _dp]
+        L.unomol_gpu_batch_destroy.argtypes = [C.c_void_p]
+        L.unomol_gpu_batch_destroy.restype = None
+        L.unomol_gpu_batch_last_error.argtypes = [C.c_void_p]
+        L.unomol_gpu_batch_last_error.restype = C.c_char_p
+        self.bases = bases
+        descs, self._keep = [], []
+        for b in bases:
+            d, k = basis_desc(b)
+            descs.append(d)
+            self._keep.append(k)
+        arr = (BasisDesc * len(descs))(*descs)
+        self._h = C.c_void_p()
+        self._chk(L.unomol_gpu_batch_create(arr, len(descs), C.byref(self._h)))
+        dP, dG, off, tot = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_int64()
+        self._chk(L.unomol_gpu_batch_buffers(self._h, C.byref(dP), C.byref(dG), C.byref(off), C.byref(tot)))
+        self.dP, self.dG, self.total = dP.value, dG.value, tot.value
+        self.offsets = [0]
+        for b in bases[:-1]:
+            self.offsets.append(self.offsets[-1] + b.no2)
+
+    def _chk(self, rc):
+        if rc < 0:
+            msg = lib().unomol_gpu_batch_last_error(getattr(self, "_h", None) or None).decode(errors="replace")
+            raise UnomolError(f"unomol_gb300 batch error {rc}: {msg}")
+        return rc
+
+    def set_densities(self, Ps):
+        self._chk(lib().unomol_gpu_batch_set_density(self._h, np.ascontiguousarray(np.concatenate(Ps), np.float64)))
+
+    def fock(self, mode: int = BATCH_GRAPH, stream: int = 0):
+        self._chk(lib().unomol_gpu_batch_fock(self._h, int(mode), C.c_void_p(stream)))
+
+    def get_focks(self):
+        G = np.zeros(self.total)
+        self._chk(lib().unomol_gpu_batch_get_fock(self._h, G))
+        return [G[o:o + b.no2].copy() for o, b in zip(self.offsets, self.bases)]
+
+    def autotune(self, reps: int = 2):
+        chosen = np.zeros(3 * 64, np.int32)
+        n = self._chk(lib().unomol_gpu_batch_autotune(self._h, int(reps), chosen.ctypes.data))
+        return [tuple(int(x) for x in chosen[3 * k:3 * k + 3]) for k in range(n)]
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().unomol_gpu_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def fma_peak(fp64: bool = True) -> float:
