@@ -214,7 +214,9 @@ typedef struct UnomolScfOptions {
     double eps;          /* convergence threshold (Basis::scf_eps) */
     int conv_type;       /* scf_flag[0]: 0 energy, 1 density, 2 both (RHF.hpp:390-402) */
     int accel;           /* UNOMOL_SCF_DAMPED or UNOMOL_SCF_DIIS */
-    int guess;           /* 0 core Hamiltonian (RHF.hpp:205-211), 1 the P passed in (PMATRIX.DAT form) */
+    int guess;           /* 0 core Hamiltonian (RHF.hpp:205-211), 1 the P passed in (PMATRIX.DAT form),
+                            2 the P passed in, McWeeny-purified and trace-checked, core Hamiltonian if it
+                            fails (UNOMOL_GUESS_PURIFY; for the learned guess) */
     int diis_size;       /* DIIS subspace (default 8) */
     double diis_tol;     /* DIIS: max |X^T (FPS - SPF) X| at convergence */
     double diis_start;   /* DIIS: extrapolate once the error is below this (<= 0: from the start) */
@@ -238,7 +240,19 @@ typedef struct UnomolScfResult {
     double fock_ms;       /* device time of all Fock builds (CUDA events) */
     double* densities;    /* optional [densities_cap][no2 (UHF: 2*no2)]: the density of every build */
     int densities_cap;
+    int guess_used;       /* UNOMOL_GUESS_USED_*: what the SCF started from */
+    int purify_iterations;
+    double purify_error;  /* guess 2: ||Q^2 - Q||_F at the end of the purification (per spin: max) */
+    double guess_trace;   /* guess 2: tr Q after the purification (alpha spin for UHF) */
 } UnomolScfResult;
+
+#define UNOMOL_GUESS_CORE 0
+#define UNOMOL_GUESS_GIVEN 1
+#define UNOMOL_GUESS_PURIFY 2
+#define UNOMOL_GUESS_USED_CORE 0       /* core Hamiltonian (asked for) */
+#define UNOMOL_GUESS_USED_GIVEN 1      /* the caller's P as given */
+#define UNOMOL_GUESS_USED_PURIFIED 2   /* the caller's P after McWeeny purification */
+#define UNOMOL_GUESS_USED_FALLBACK 3   /* purification or trace check failed: core Hamiltonian */
 
 /* SCF on the GPU: the loop of RestrictedHartreeFock / UnRestrictedHartreeFock::findEnergy (RHF.hpp:
  * 114-176, UHF.hpp:137-177) with every Fock build on this context and the FP64 linear algebra in
@@ -246,6 +260,67 @@ typedef struct UnomolScfResult {
  * options->guess == 1, the final density on return.  orbital_energies: optional [norb] (UHF: 2*norb). */
 int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* input, const UnomolScfOptions* options, UnomolScfResult* result,
                double* P_io, double* orbital_energies);
+
+/* ---- Learned initial density (no reference counterpart; the reference starts from the core
+ * Hamiltonian, RHF.hpp:205-211, or reads PMATRIX.DAT, RHF.hpp:120-123) ----
+ * A per-atom-pair MLP maps (element of i, element of j, 16 radial basis functions of r_ij) to
+ * Slater-Koster-like coefficients of the density blocks in the bond frame; the blocks are rotated
+ * into place and summed into the RHF half density P (trace(PS) = nocc, the PMATRIX.DAT form).  Training
+ * and inference run on the GPU: BF16 GEMMs on the tensor cores with FP32 accumulation, FP32 master
+ * weights and Adam.  Bases: s and p shells, every centre of an element with the same shell list. */
+
+/* the network alone: y = W_L silu(... silu(W_0 x + b_0) ...) + b_L; parameters (fp32, host order):
+ * per linear map W [dout x din] row major, then b [dout] */
+typedef struct UnomolMlp UnomolMlp;
+int unomol_mlp_create(int n_in, int hidden, int layers, int n_out, unsigned long long seed, UnomolMlp** out);
+long long unomol_mlp_num_params(const UnomolMlp* m);
+int unomol_mlp_get_params(UnomolMlp* m, float* out);
+int unomol_mlp_set_params(UnomolMlp* m, const float* in);
+/* x: device fp32 [rows x n_in]; y: device fp32 [rows x n_out] */
+int unomol_mlp_forward(UnomolMlp* m, const float* x, int rows, float* y, void* stream);
+/* gradients of sum(dy * y) for the rows of the last forward; dy: device fp32 [rows x n_out] */
+int unomol_mlp_backward(UnomolMlp* m, const float* dy, void* stream);
+int unomol_mlp_get_grads(UnomolMlp* m, float* out);
+int unomol_mlp_adam(UnomolMlp* m, float lr, float beta1, float beta2, float eps, float weight_decay, void* stream);
+void unomol_mlp_destroy(UnomolMlp* m);
+const char* unomol_mlp_last_error(const UnomolMlp* m);
+/* C[M x N] (fp32, device) = A[M x K] . B[N x K]^T, A and B bf16 row major on the device (the tensor-core
+ * GEMM of the network); status: device int set to 1 if a bounded wait gave up. */
+int unomol_tc_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int* status, void* stream);
+
+typedef struct UnomolGuess UnomolGuess;
+typedef struct UnomolGuessConfig {
+    int hidden;                /* hidden width (<= 0: 256) */
+    int layers;                /* hidden layers (<= 0: 3) */
+    int n_rbf;                 /* radial basis functions (<= 1: 16), centres k * r_cut / (n_rbf - 1) */
+    double r_cut;              /* pair cutoff in bohr (<= 0: 15) */
+    unsigned long long seed;   /* weight initialisation */
+} UnomolGuessConfig;
+typedef struct UnomolGuessTrainOptions {
+    int first, count;          /* molecules [first, first + count) of the model's data set */
+    int epochs;
+    int batch_molecules;       /* molecules per Adam step (<= 0: 16) */
+    float lr, lr_final;        /* cosine schedule from lr to lr_final (<= 0: lr / 100) */
+    float weight_decay;
+    unsigned long long seed;   /* mini-batch order */
+} UnomolGuessTrainOptions;
+/* The model's elements and their shell lists come from this basis; charges: [ncen] nuclear charges. */
+int unomol_guess_create(const UnomolGuessConfig* cfg, const UnomolBasisDesc* basis, const int* charges,
+                        UnomolGuess** out);
+int unomol_guess_info(const UnomolGuess* g, int* n_in, int* n_out, long long* n_params, int* n_elements);
+/* append a molecule and its converged RHF density (packed, PMATRIX.DAT form) to the data set */
+int unomol_guess_add_molecule(UnomolGuess* g, const UnomolBasisDesc* basis, const int* charges, const double* P);
+int unomol_guess_num_molecules(const UnomolGuess* g);
+/* Adam on the mean over molecules of sum (P_pred - P)^2; loss_history: optional [epochs] */
+int unomol_guess_train(UnomolGuess* g, const UnomolGuessTrainOptions* opt, double* loss_history);
+/* loss of molecules [first, first + count) and, if grads != NULL, its gradient (host order) */
+int unomol_guess_loss(UnomolGuess* g, int first, int count, int batch_molecules, double* loss, float* grads);
+/* predicted P (packed) for a molecule; hand it to unomol_scf with guess = UNOMOL_GUESS_PURIFY */
+int unomol_guess_predict(UnomolGuess* g, const UnomolBasisDesc* basis, const int* charges, double* P);
+int unomol_guess_get_params(UnomolGuess* g, float* out);
+int unomol_guess_set_params(UnomolGuess* g, const float* in);
+void unomol_guess_destroy(UnomolGuess* g);
+const char* unomol_guess_last_error(const UnomolGuess* g);
 
 /* Last error of this context (ctx may be NULL for errors raised before a context existed). */
 const char* unomol_gpu_last_error(const UnomolCtx* ctx);

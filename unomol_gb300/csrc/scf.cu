@@ -293,6 +293,60 @@ int level_shift(Dev& d, const std::vector<double>& Ppk, const double* d_S, doubl
     return UNOMOL_OK;
 }
 
+// McWeeny purification of a guess density (new; for the learned guess).  In the orthonormal basis of X
+// (X^T S X = 1, so X^{-1} = X^T S) the density is Q = X^T S P S X; Q <- 3 Q^2 - 2 Q^3 drives every
+// eigenvalue of Q in (-1/2, 1/2) to 0 and in (1/2, 3/2) to 1.  Accepted when ||Q^2 - Q||_F falls
+// below 1e-10 within 60 steps and tr Q = nocc within 1e-6; then P = X Q X^T.  Otherwise (diverging
+// or non-finite values, wrong electron count) ok = false and P is left unchanged.
+int purify(Dev& d, const double* d_S, double* d_pk, std::vector<double>& P, int nocc, int& iters, double& err,
+           double& trace, bool& ok) {
+    const int n = d.n;
+    const double one = 1.0, zero = 0.0, mone = -1.0, three = 3.0, mtwo = -2.0;
+    double *Q = d.W, *t = d.T1, *u = d.C, *v = d.F;
+    ok = false;
+    iters = 0;
+    err = 0.0;
+    trace = 0.0;
+    CK(cudaMemcpyAsync(d_pk, P.data(), P.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, v, n);
+    // Q = X^T (S P S) X
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d_S, n, v, n, &zero, t, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, t, n, d_S, n, &zero, u, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, u, n, d.X, n, &zero, t, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, d.X, n, t, n, &zero, Q, n), UNOMOL_ECUDA);
+    bool conv = false;
+    for (int it = 0; it < 60; ++it) {
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, Q, n, Q, n, &zero, t, n), UNOMOL_ECUDA);  // Q^2
+        CK(cublasDgeam(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &one, t, n, &mone, Q, n, u, n), UNOMOL_ECUDA);
+        double e = 0.0;
+        CK(cublasDnrm2(d.cb, n * n, u, 1, &e), UNOMOL_ECUDA);  // host pointer mode: synchronous
+        err = e;
+        iters = it;
+        if (!(e < 1e6)) return UNOMOL_OK;  // diverging or not finite
+        if (e < 1e-10) {
+            conv = true;
+            break;
+        }
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, t, n, Q, n, &zero, u, n), UNOMOL_ECUDA);  // Q^3
+        CK(cublasDgeam(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, &three, t, n, &mtwo, u, n, Q, n), UNOMOL_ECUDA);
+        iters = it + 1;
+    }
+    if (!conv) return UNOMOL_OK;
+    std::vector<double> diag(n);
+    CK(cublasGetVectorAsync(n, sizeof(double), Q, n + 1, diag.data(), 1, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    for (double x : diag) trace += x;
+    if (!(std::fabs(trace - nocc) < 1e-6)) return UNOMOL_OK;
+    // P = X Q X^T
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.X, n, Q, n, &zero, t, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, t, n, d.X, n, &zero, u, n), UNOMOL_ECUDA);
+    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(u, d_pk, n);
+    CK(cudaMemcpyAsync(P.data(), d_pk, P.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    ok = true;
+    return UNOMOL_OK;
+}
+
 }  // namespace
 
 extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const UnomolScfOptions* opt, UnomolScfResult* res,
@@ -336,11 +390,27 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     k_unpack<<<blocks((long long)n * n), 256, 0, s>>>(d_pk, d_S, n);
     std::vector<double> Pa(no2), Pb(no2), Ga(no2), Gb(no2), Fa(no2), Fb(no2), PoldA(no2), PoldB(no2), PoldA2(no2),
         PoldB2(no2), evA, evB, tmp;
-    // guess: caller's P (RHF.hpp:120-123) or core Hamiltonian (RHF.hpp:205-211; UHF.hpp:487-496)
-    if (opt->guess == 1) {
+    // guess: caller's P (RHF.hpp:120-123), the caller's P purified (new), or core Hamiltonian
+    // (RHF.hpp:205-211; UHF.hpp:487-496)
+    int guess_used = UNOMOL_GUESS_USED_CORE, pur_it = 0;
+    double pur_err = 0.0, pur_tr = 0.0;
+    if (opt->guess == UNOMOL_GUESS_GIVEN || opt->guess == UNOMOL_GUESS_PURIFY) {
         std::memcpy(Pa.data(), P_io, no2 * sizeof(double));
         if (uhf) std::memcpy(Pb.data(), P_io + no2, no2 * sizeof(double));
-    } else {
+        guess_used = UNOMOL_GUESS_USED_GIVEN;
+    }
+    if (opt->guess == UNOMOL_GUESS_PURIFY) {
+        bool okA = false, okB = true;
+        int itB = 0;
+        double eB = 0.0, trB = 0.0;
+        rc = purify(d, d_S, d_pk, Pa, noccA, pur_it, pur_err, pur_tr, okA);
+        if (!rc && okA && uhf) rc = purify(d, d_S, d_pk, Pb, noccB, itB, eB, trB, okB);
+        if (rc) return fail(rc);
+        pur_it = std::max(pur_it, itB);
+        pur_err = std::max(pur_err, eB);
+        guess_used = okA && okB ? UNOMOL_GUESS_USED_PURIFIED : UNOMOL_GUESS_USED_FALLBACK;
+    }
+    if (guess_used == UNOMOL_GUESS_USED_CORE || guess_used == UNOMOL_GUESS_USED_FALLBACK) {
         rc = diag_density(d, H, d_pk, noccA, Pa, evA, nullptr);
         if (rc) return fail(rc);
         if (uhf) {
@@ -520,6 +590,10 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     res->fock_builds = builds;
     res->fock_ms = fock_ms;
     res->diis_error = diis_err;
+    res->guess_used = guess_used;
+    res->purify_iterations = pur_it;
+    res->purify_error = pur_err;
+    res->guess_trace = pur_tr;
     res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return UNOMOL_OK;
 }

@@ -26,7 +26,12 @@ EXPORTS = [
     "unomol_gpu_last_build_ms", "unomol_gpu_set_density_screening", "unomol_gpu_fock_rhf_noalloc",
     "unomol_one_electron", "unomol_scf", "unomol_gpu_set_eri_method", "unomol_gpu_batch_create",
     "unomol_gpu_batch_buffers", "unomol_gpu_batch_fock", "unomol_gpu_batch_autotune", "unomol_gpu_batch_set_density",
-    "unomol_gpu_batch_get_fock", "unomol_gpu_batch_destroy", "unomol_gpu_batch_last_error",
+    "unomol_gpu_batch_get_fock", "unomol_gpu_batch_destroy", "unomol_gpu_batch_last_error", "unomol_tc_gemm_bf16",
+    "unomol_mlp_create", "unomol_mlp_num_params", "unomol_mlp_get_params", "unomol_mlp_set_params",
+    "unomol_mlp_forward", "unomol_mlp_backward", "unomol_mlp_get_grads", "unomol_mlp_adam", "unomol_mlp_destroy",
+    "unomol_mlp_last_error", "unomol_guess_create", "unomol_guess_info", "unomol_guess_add_molecule",
+    "unomol_guess_num_molecules", "unomol_guess_train", "unomol_guess_loss", "unomol_guess_predict",
+    "unomol_guess_get_params", "unomol_guess_set_params", "unomol_guess_destroy", "unomol_guess_last_error",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -232,11 +237,14 @@ class ScfResult(C.Structure):
                 ("pdiff", C.c_double), ("diis_error", C.c_double), ("seconds", C.c_double),
                 ("iterations", C.c_int), ("converged", C.c_int), ("fock_builds", C.c_int),
                 ("energies", C.POINTER(C.c_double)), ("energies_cap", C.c_int), ("fock_ms", C.c_double),
-                ("densities", C.POINTER(C.c_double)), ("densities_cap", C.c_int)]
+                ("densities", C.POINTER(C.c_double)), ("densities_cap", C.c_int), ("guess_used", C.c_int),
+                ("purify_iterations", C.c_int), ("purify_error", C.c_double), ("guess_trace", C.c_double)]
 
 
 SCF_DAMPED = 0
 SCF_DIIS = 2
+GUESS_CORE, GUESS_GIVEN, GUESS_PURIFY = 0, 1, 2
+GUESS_USED = {0: "core", 1: "given", 2: "purified", 3: "fallback"}
 
 
 def one_electron(b: Basis):
@@ -253,8 +261,10 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
         maxits: int | None = None, eps: float | None = None, conv_type: int | None = None,
         diis_size: int = 8, diis_tol: float = 1e-6, record: int = 0, diis_start: float = 0.0,
         level_shift: float = 0.0, level_shift_until: float = 0.05, incremental: bool = False,
-        rebuild_every: int = 8, keep_densities: int = 0):
-    """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ..."""
+        rebuild_every: int = 8, keep_densities: int = 0, purify: bool = False):
+    """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ...
+    purify: start from guess_P after McWeeny purification and a trace check, or from the core
+    Hamiltonian when it fails them (out["guess_used"] says which)."""
     L = lib()
     L.unomol_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.POINTER(ScfOptions), C.POINTER(ScfResult),
                              _dp, C.c_void_p]
@@ -265,7 +275,8 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
     dp = C.POINTER(C.c_double)
     inp = ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), S.ctypes.data_as(dp), H.ctypes.data_as(dp))
     opt = ScfOptions(maxits if maxits is not None else b.maxits, eps if eps is not None else b.eps,
-                     conv_type if conv_type is not None else b.scf_flag[0], accel, 0 if guess_P is None else 1,
+                     conv_type if conv_type is not None else b.scf_flag[0], accel,
+                     GUESS_CORE if guess_P is None else (GUESS_PURIFY if purify else GUESS_GIVEN),
                      diis_size, diis_tol, diis_start, level_shift, level_shift_until, 1 if incremental else 0,
                      rebuild_every)
     uhf = b.nelec % 2 == 1
@@ -286,7 +297,9 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
     if rc != 0:
         raise UnomolError(f"unomol_scf error {rc}: {res.message.decode(errors='replace')}")
     out = {k: getattr(res, k) for k in ("energy", "e_electronic", "init_energy", "ediff", "pdiff", "diis_error",
-                                        "seconds", "iterations", "converged", "fock_builds", "fock_ms")}
+                                        "seconds", "iterations", "converged", "fock_builds", "fock_ms",
+                                        "purify_iterations", "purify_error", "guess_trace")}
+    out["guess_used"] = GUESS_USED.get(res.guess_used, str(res.guess_used))
     out["P"] = P
     out["orbital_energies"] = eps_orb
     if record:
