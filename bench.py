@@ -152,6 +152,24 @@ def run_reference(args):
     return 0
 
 
+def measured_hbm():
+    """HBM copy bandwidth (GB/s) from MEASURED_PEAKS.json, None when the file is absent."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    for k in ("hbm_gbs", "hbm_GBps", "hbm"):
+        v = d.get(k)
+        if isinstance(v, (int, float)):
+            return float(v)
+        if isinstance(v, dict):
+            for kk in ("value", "gbs", "burst"):
+                if isinstance(v.get(kk), (int, float)):
+                    return float(v[kk])
+    return None
+
+
 def profile_traffic(form):
     p = os.path.join(ROOT, "profiles", f"fock_{form}_water32_traffic.json")
     if os.path.exists(p):
@@ -197,7 +215,7 @@ def counted_flops(ctx, inputs, dev, stream):
     import torch
     ctx.set_counting(True)
     dG = None
-    f64, f32, launches, q32, q = [], [], [], [], []
+    f64, f32, launches, q32, q, fq = [], [], [], [], [], []
     for full, x in inputs:
         dx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
         if full or dG is None:
@@ -210,8 +228,9 @@ def counted_flops(ctx, inputs, dev, stream):
         launches.append(st["kernel_launches"])
         q.append(st["shell_quartets"])
         q32.append(st["shell_quartets_fp32"])
+        fq.append(st["function_quartets"])
     ctx.set_counting(False)
-    return f64, f32, launches, q, q32
+    return f64, f32, launches, q, q32, fq
 
 
 def run_ours(args):
@@ -263,7 +282,7 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     # warm-up, then the counted (untimed) pass for the algorithmic flops
     timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
-    f64, f32, launches, nq, nq32 = counted_flops(mixed, inputs, dev, stream)
+    f64, f32, launches, nq, nq32, nfq = counted_flops(mixed, inputs, dev, stream)
     # timed region
     if ws > 1:
         torch.distributed.barrier()
@@ -317,6 +336,12 @@ def run_ours(args):
     achieved = (fl64 + fl32) / eri_s / 1e12
     peak = (fl64 + fl32) / (fl64 / peak64 + fl32 / peak32) if (fl64 + fl32) > 0 else peak64
     launches_total = sum(launches[k % len(inputs)] for k in range(args.steps))
+    # J/K scatter: 144 algorithmic bytes per computed function quartet (6 density reads and 6 Fock
+    # read-modify-writes of 8 bytes), fused into the ERI kernels, against HBM and the L2 figures
+    l2_read, l2_atom = native.l2_peak()
+    scatter_bytes = 144.0 * sum(nfq[k % len(inputs)] for k in range(args.steps))
+    scatter_gbs = scatter_bytes / eri_s / 1e9
+    hbm = measured_hbm()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if args.form == "mixed" else "f64",
@@ -341,6 +366,11 @@ def run_ours(args):
                     "iterations_form": rm["iterations"], "converged": bool(r64["converged"] and rm["converged"]),
                     "scf_wall_s_plain_fp64": r64["seconds"], "scf_wall_s_form": rm["seconds"],
                     "fock_ms_plain_fp64": r64["fock_ms"], "fock_ms_form": rm["fock_ms"], "guess_s": t_guess},
+            "scatter": {"algorithmic_bytes_per_build": scatter_bytes / args.steps, "achieved_gbs": scatter_gbs,
+                        "hbm_gbs": hbm, "frac_of_hbm": scatter_gbs / hbm if hbm else None,
+                        "l2_read_gbs": l2_read, "frac_of_l2_read": scatter_gbs / l2_read,
+                        "l2_fp64_atomics_per_s": l2_atom * 1e9,
+                        "note": "fused into the ERI kernels (the J/K epilogue); time = ERI kernel time"},
             "clocks": clk, "gpu_launches": launches_total}
     if rank == 0 and ws == 1:
         ensure_oracle()

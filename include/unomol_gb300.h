@@ -153,6 +153,9 @@ int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total);
  * kernel over every SM, FP64 (fp64 = 1) or FP32 (fp64 = 0).  The roofline denominator of the Fock
  * kernels, which are bound by the FP64 (or FP32) pipe. */
 int unomol_gpu_fma_peak(int fp64, double* tflops);
+/* L2 figures of the J/K scatter, measured on the current device: read bandwidth of an L2-resident 32 MiB
+ * buffer (GB/s) and FP64 atomicAdd throughput on a 416 x 416 accumulator (10^9 atomics/s). */
+int unomol_gpu_l2_peak(double* read_gbs, double* atomic_gops);
 
 /* Allocation-free RHF Fock build.  No counterpart in the reference (its Fock build runs on the host).
  * Same contract as unomol_gpu_fock_rhf_device (device pointers, packed P in, packed G added into,
@@ -182,6 +185,7 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
 int unomol_gpu_batch_buffers(UnomolBatch* batch, double** dP, double** dG, const long long** packed_offsets,
                              int64_t* packed_total);
 int unomol_gpu_batch_fock(UnomolBatch* batch, int mode, void* stream);
+int unomol_gpu_batch_size(const UnomolBatch* batch);  /* molecules in the batch */
 /* Autotuner: times every (CTA size 64/128/256, CTAs per SM 1/2/4/8) per class launch on the current P
  * and keeps the fastest; chosen (optional, 3 ints per launch): class id, CTA size, CTAs per SM.
  * Returns the number of launches (>= 0) or an error code. */
@@ -197,6 +201,14 @@ const char* unomol_gpu_batch_last_error(const UnomolBatch* batch);
 /* One-electron integrals S, T and H = T + V, packed (the data of OneElectronInts, OneElectronInts.cpp:
  * 6-202; computed on the host).  charges: [ncen] nuclear charges. */
 int unomol_one_electron(const UnomolBasisDesc* basis, const double* charges, double* S, double* T, double* H);
+
+/* The same integrals on the GPU for ngeom geometries of one basis in one launch (one thread per packed
+ * element and geometry; the reference computes them on the host once per geometry,
+ * OneElectronInts.cpp:6-202).  centers: [ngeom][ncen][3] bohr (NULL: the basis's own, ngeom = 1);
+ * S, T, H: host [ngeom][no2] (T may be NULL).  Shells up to l = 4. */
+int unomol_gpu_one_electron(const UnomolBasisDesc* basis, const double* charges, int ngeom, const double* centers,
+                            double* S, double* T, double* H);
+const char* unomol_gpu_one_electron_last_error(void);
 
 typedef struct UnomolScfInput {
     int norb;            /* basis functions */
@@ -260,6 +272,21 @@ typedef struct UnomolScfResult {
  * options->guess == 1, the final density on return.  orbital_energies: optional [norb] (UHF: 2*norb). */
 int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* input, const UnomolScfOptions* options, UnomolScfResult* result,
                double* P_io, double* orbital_energies);
+
+/* RHF SCF of every molecule of the batch at once: each iteration is one batched Fock build plus the
+ * DIIS update of the single-molecule driver (F = H + G, energy, X^T (FPS - SPF) X, Pulay extrapolation,
+ * X^T F X, batched eigen-solve, P = C_occ C_occ^T) for all molecules, with converged molecules frozen;
+ * with graph != 0 the iteration is captured once as a CUDA graph and replayed (graph_used reports
+ * whether the capture succeeded; unomol_gpu_batch_scf_last_error then names what stopped it).
+ * inputs: [nmol] (S, H packed, nelec even), options: maxits, eps, diis_size, diis_tol (the DIIS
+ * criterion of unomol_scf; core-Hamiltonian guess).  P_out: optional, the batch's packed densities. */
+typedef struct UnomolBatchScfResult {
+    double energy, e_electronic, diis_error;
+    int iterations, converged;
+} UnomolBatchScfResult;
+int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* inputs, int nmol, const UnomolScfOptions* options,
+                         int graph, UnomolBatchScfResult* results, double* P_out, double* seconds, int* graph_used);
+const char* unomol_gpu_batch_scf_last_error(void);
 
 /* ---- Learned initial density (no reference counterpart; the reference starts from the core
  * Hamiltonian, RHF.hpp:205-211, or reads PMATRIX.DAT, RHF.hpp:120-123) ----

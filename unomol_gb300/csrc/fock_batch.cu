@@ -290,6 +290,8 @@ int unomol_gpu_batch_buffers(UnomolBatch* b, double** dP, double** dG, const lon
     return UNOMOL_OK;
 }
 
+int unomol_gpu_batch_size(const UnomolBatch* b) { return b ? (int)b->mols.size() : UNOMOL_EINVAL; }
+
 int unomol_gpu_batch_fock(UnomolBatch* b, int mode, void* stream) {
     if (!b) return bfail(b, UNOMOL_EINVAL, "null batch");
     cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;

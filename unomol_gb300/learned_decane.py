@@ -44,10 +44,11 @@ def run(n_geom: int = 2000, n_train: int = 1600, sigma: float = 0.05, seed: int 
     bases = [Basis(text=molecules.patin_text(a, basis, maxits=maxits, eps=eps)) for a in geoms]
     opts = dict(eps=eps, diis_tol=diis_tol, maxits=maxits, conv_type=0)
     ctx = native.TwoElectronInts(bases[0])
-    one = []
-    for b in bases:
-        S, _, H = native.one_electron(b)
-        one.append((S, H))
+    # one-electron integrals of every geometry in one GPU launch
+    t0 = time.perf_counter()
+    S_all, H_all = native.one_electron_gpu(bases[0], centers=np.stack([b.centers for b in bases]))
+    t_one = time.perf_counter() - t0
+    one = [(S_all[k], H_all[k]) for k in range(n_geom)]
     # warm-up (first launches, cuBLAS/cuSOLVER handles)
     _scf(ctx, bases[0], *one[0], opts)
     # plain SCF on the training geometries: the training targets
@@ -78,8 +79,9 @@ def run(n_geom: int = 2000, n_train: int = 1600, sigma: float = 0.05, seed: int 
         t_pred = time.perf_counter() - t0
         q = _scf(ctx, b, *one[k], opts, guess=Pg)
         rows.append(dict(k=k, plain_its=p["iterations"], plain_s=p["seconds"], plain_E=p["energy"],
-                         plain_conv=p["converged"], learned_its=q["iterations"], learned_s=q["seconds"] + t_pred,
-                         learned_E=q["energy"], learned_conv=q["converged"], guess_used=q["guess_used"],
+                         plain_conv=p["converged"], plain_fock_ms=p["fock_ms"], learned_its=q["iterations"],
+                         learned_s=q["seconds"] + t_pred, learned_E=q["energy"], learned_conv=q["converged"],
+                         learned_fock_ms=q["fock_ms"], guess_used=q["guess_used"],
                          purify_iterations=q["purify_iterations"], predict_s=t_pred))
     # held-out loss of the trained network against the plain densities
     both = [r for r in rows if r["plain_conv"] and r["learned_conv"]]
@@ -106,7 +108,10 @@ def run(n_geom: int = 2000, n_train: int = 1600, sigma: float = 0.05, seed: int 
             "both_converged": len(both),
             "fallbacks": sum(r["guess_used"] != "purified" for r in rows),
             "mean_predict_seconds": float(np.mean([r["predict_s"] for r in rows])),
+            "plain_mean_fock_ms_per_scf": float(np.mean([r["plain_fock_ms"] for r in rows])),
+            "learned_mean_fock_ms_per_scf": float(np.mean([r["learned_fock_ms"] for r in rows])),
         },
+        "one_electron_gpu_seconds_all_geometries": t_one,
         "scf": {"accel": "DIIS", "eps": eps, "diis_tol": diis_tol, "maxits": maxits},
         "loss_history": [float(x) for x in hist],
         "rows": rows,

@@ -1,0 +1,143 @@
+"""Measurements behind the committed summaries of the batching and precision forms.
+
+    python -m unomol_gb300.measure batch [--reps 5] [--out batch.json]
+        The batching workload (molecules.batch_workload(seed=0): 256 molecules, half all-trans alkanes
+        C_kH_2k+2 with k in 1..8, half water clusters of 1..6 monomers, STO-3G or 6-31G by a seeded coin
+        flip).  Densities: 0.9 x the projector onto nocc random orthonormal vectors (numpy default_rng(0)).
+        Device time per build of all 256 molecules (CUDA events on one stream, mean of `reps` after one
+        warm-up) for one molecule at a time, the batched persistent launches, the batched CUDA graph,
+        and both again after the autotuner; max |G(batch) - G(one at a time)|.  Then the RHF SCF of all
+        256 molecules (core-Hamiltonian guess, DIIS, 1e-10 Eh): batched with every iteration as one CUDA
+        graph, batched with plain launches, and one molecule at a time through the single-molecule
+        driver (wall times; contexts created outside the timing), with the energy differences.
+
+    python -m unomol_gb300.measure sweep [--out sweep.json]
+        FP32 cutoff sweep of the precision form on the 32-water 6-31G cluster (molecules.water_cluster(32, 0),
+        superposition-of-fragments guess, DIIS, 1e-10 Eh): the incremental mixed-precision SCF against the
+        plain FP64 SCF for every cutoff, with dE, max |dF| (G of the final FP64 density built by both
+        paths, full builds), iterations, device ms per build and SCF wall time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+from . import guess, molecules, native
+from .basis import Basis
+
+
+def _batch(reps: int, scf: bool = True) -> dict:
+    import torch
+    work = molecules.batch_workload(seed=0)
+    bases = [Basis(text=t) for _, t in work]
+    rng = np.random.default_rng(0)
+    Ps = []
+    for b in bases:
+        q, _ = np.linalg.qr(rng.normal(size=(b.norb, b.nelec // 2)))
+        Ps.append(np.ascontiguousarray((0.9 * q @ q.T)[np.tril_indices(b.norb)]))
+    bat = native.Batch(bases)
+    bat.set_densities(Ps)
+    s = torch.cuda.Stream()
+
+    def timeit(mode):
+        bat.fock(mode, s.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            bat.fock(mode, s.cuda_stream)
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {"molecules": len(bases), "basis_functions_total": int(sum(b.norb for b in bases)),
+           "nbf_min": int(min(b.norb for b in bases)), "nbf_max": int(max(b.norb for b in bases)), "modes": {}}
+    for name, mode in (("sequential", native.BATCH_SEQUENTIAL), ("batched_launches", native.BATCH_LAUNCHES),
+                       ("batched_graph", native.BATCH_GRAPH)):
+        out["modes"][name] = timeit(mode)
+    out["autotune_choice"] = [list(map(int, c)) for c in bat.autotune(2)]
+    for name, mode in (("tuned_launches", native.BATCH_LAUNCHES), ("tuned_graph", native.BATCH_GRAPH)):
+        out["modes"][name] = timeit(mode)
+    Gb = bat.get_focks()
+    bat.fock(native.BATCH_SEQUENTIAL)
+    Gq = bat.get_focks()
+    out["max_abs_dG_batch_vs_sequential"] = float(max(np.abs(a - c).max() for a, c in zip(Gb, Gq)))
+    out["builds_per_s"] = {k: len(bases) / v * 1e3 for k, v in out["modes"].items()}
+    out["speedup_vs_sequential"] = out["modes"]["sequential"] / min(
+        v for k, v in out["modes"].items() if k != "sequential")
+    if scf:
+        out["scf"] = _batch_scf(bat, bases)
+    return out
+
+
+def _batch_scf(bat, bases) -> dict:
+    """SCF of all molecules: batched (graph, plain launches) against one molecule at a time."""
+    import time
+    SH = [native.one_electron_gpu(b) for b in bases]
+    S, H = [x[0] for x in SH], [x[1] for x in SH]
+    kw = dict(eps=1e-10, diis_tol=1e-6, maxits=200)
+    rg = bat.scf(S=S, H=H, graph=True, **kw)
+    rl = bat.scf(S=S, H=H, graph=False, **kw)
+    ctxs = [native.TwoElectronInts(b) for b in bases]  # set-up outside the timing, as for the batch
+    native.scf(ctxs[0], bases[0], S=S[0], H=H[0], accel=native.SCF_DIIS, conv_type=0, **kw)  # warm-up
+    t0 = time.perf_counter()
+    seq = [native.scf(c, b, S=s, H=h, accel=native.SCF_DIIS, conv_type=0, **kw)
+           for c, b, s, h in zip(ctxs, bases, S, H)]
+    t_seq = time.perf_counter() - t0
+    for c in ctxs:
+        c.close()
+    e_seq = np.array([q["energy"] for q in seq])
+    return {"molecules": len(bases), "options": kw,
+            "batched_graph_s": rg["seconds"], "graph_used": rg["graph_used"], "capture_note": rg["capture_note"],
+            "batched_launches_s": rl["seconds"], "one_at_a_time_s": t_seq,
+            "speedup_graph_vs_one_at_a_time": t_seq / rg["seconds"],
+            "iterations_batched_max": int(rg["iterations"].max()),
+            "iterations_one_at_a_time_sum": int(sum(q["iterations"] for q in seq)),
+            "converged_batched": int(rg["converged"].sum()), "converged_one_at_a_time": int(sum(q["converged"] for q in seq)),
+            "max_abs_dE_batched_vs_one_at_a_time": float(np.max(np.abs(rg["energy"] - e_seq))),
+            "max_abs_dE_graph_vs_launches": float(np.max(np.abs(rg["energy"] - rl["energy"])))}
+
+
+def _sweep() -> dict:
+    b = Basis(text=molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10))
+    S, _, H = native.one_electron(b)
+    P0 = guess.fragment_density(b)
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, maxits=100, eps=1e-10, diis_tol=1e-7, guess_P=P0)
+    t64 = native.TwoElectronInts(b)
+    r64 = native.scf(t64, b, **kw)
+    G64 = t64.form_g(r64["P"])
+    ms64 = r64["fock_ms"] / r64["fock_builds"]
+    out = {"fp64": {"energy": r64["energy"], "iterations": r64["iterations"], "ms_per_build": ms64,
+                    "scf_wall_s": r64["seconds"]}, "rows": []}
+    for cut in (1e0, 1e-1, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7):
+        tm = native.TwoElectronInts(b)
+        tm.set_precision(native.PREC_MIXED, cut)
+        tm.set_density_screening(1e-12)
+        rm = native.scf(tm, b, incremental=True, **kw)
+        Gm = tm.form_g(r64["P"])
+        ms = rm["fock_ms"] / rm["fock_builds"]
+        out["rows"].append({"fp32_cutoff": cut, "dE": rm["energy"] - r64["energy"],
+                            "max_abs_dF": float(np.max(np.abs(Gm - G64))), "iterations": rm["iterations"],
+                            "converged": bool(rm["converged"]), "ms_per_build": ms, "speedup": ms64 / ms,
+                            "scf_wall_s": rm["seconds"]})
+        tm.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description="batching / precision-form measurements")
+    ap.add_argument("what", choices=["batch", "sweep"])
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    rep = _batch(a.reps) if a.what == "batch" else _sweep()
+    print(json.dumps(rep, indent=1))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(rep, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

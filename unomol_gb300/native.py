@@ -32,6 +32,8 @@ EXPORTS = [
     "unomol_mlp_last_error", "unomol_guess_create", "unomol_guess_info", "unomol_guess_add_molecule",
     "unomol_guess_num_molecules", "unomol_guess_train", "unomol_guess_loss", "unomol_guess_predict",
     "unomol_guess_get_params", "unomol_guess_set_params", "unomol_guess_destroy", "unomol_guess_last_error",
+    "unomol_gpu_one_electron", "unomol_gpu_one_electron_last_error", "unomol_gpu_l2_peak", "unomol_gpu_batch_scf",
+    "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -241,6 +243,11 @@ class ScfResult(C.Structure):
                 ("purify_iterations", C.c_int), ("purify_error", C.c_double), ("guess_trace", C.c_double)]
 
 
+class BatchScfResult(C.Structure):
+    _fields_ = [("energy", C.c_double), ("e_electronic", C.c_double), ("diis_error", C.c_double),
+                ("iterations", C.c_int), ("converged", C.c_int)]
+
+
 SCF_DAMPED = 0
 SCF_DIIS = 2
 GUESS_CORE, GUESS_GIVEN, GUESS_PURIFY = 0, 1, 2
@@ -255,6 +262,29 @@ def one_electron(b: Basis):
     S, T, H = np.zeros(b.no2), np.zeros(b.no2), np.zeros(b.no2)
     _check(L.unomol_one_electron(C.byref(d), np.ascontiguousarray(b.charges, np.float64), S, T, H))
     return S, T, H
+
+
+def one_electron_gpu(b: Basis, centers=None, with_t: bool = False):
+    """S, H (and T) packed on the GPU (unomol_gpu_one_electron); centers: None (the basis's geometry) or
+    an array [ngeom, ncen, 3] in bohr, giving arrays [ngeom, no2]."""
+    L = lib()
+    L.unomol_gpu_one_electron.argtypes = [C.POINTER(BasisDesc), _dp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]
+    L.unomol_gpu_one_electron_last_error.restype = C.c_char_p
+    d, keep = basis_desc(b)
+    many = centers is not None
+    cen = np.ascontiguousarray(b.centers if centers is None else centers, np.float64).reshape(-1, b.ncen, 3)
+    ng = cen.shape[0]
+    S, H = np.zeros((ng, b.no2)), np.zeros((ng, b.no2))
+    T = np.zeros((ng, b.no2)) if with_t else None
+    rc = L.unomol_gpu_one_electron(C.byref(d), np.ascontiguousarray(b.charges, np.float64), ng, cen.ctypes.data,
+                                   S.ctypes.data, T.ctypes.data if with_t else None, H.ctypes.data)
+    if rc != 0:
+        raise UnomolError(f"unomol_gpu_one_electron error {rc}: {L.unomol_gpu_one_electron_last_error().decode()}")
+    if not many:
+        S, H = S[0], H[0]
+        T = T[0] if with_t else None
+    return (S, T, H) if with_t else (S, H)
 
 
 def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPED, guess_P=None,
@@ -369,6 +399,39 @@ class Batch:
         n = self._chk(lib().unomol_gpu_batch_autotune(self._h, int(reps), chosen.ctypes.data))
         return [tuple(int(x) for x in chosen[3 * k:3 * k + 3]) for k in range(n)]
 
+    def scf(self, S=None, H=None, eps: float = 1e-10, diis_tol: float = 1e-6, maxits: int = 200,
+            diis_size: int = 8, graph: bool = True):
+        """RHF SCF of every molecule at once (unomol_gpu_batch_scf).  S, H: lists of packed matrices
+        (default: the GPU one-electron integrals of each basis).  Returns a dict with per-molecule
+        energies, iterations and convergence, the packed densities, the wall time and whether the
+        iteration ran as a CUDA graph."""
+        L = lib()
+        L.unomol_gpu_batch_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.c_int, C.POINTER(ScfOptions), C.c_int,
+                                           C.POINTER(BatchScfResult), _dp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        L.unomol_gpu_batch_scf_last_error.restype = C.c_char_p
+        n = len(self.bases)
+        if S is None or H is None:
+            SH = [one_electron_gpu(b) for b in self.bases]
+            S, H = [x[0] for x in SH], [x[1] for x in SH]
+        S = [np.ascontiguousarray(x, np.float64) for x in S]
+        H = [np.ascontiguousarray(x, np.float64) for x in H]
+        dp = C.POINTER(C.c_double)
+        inp = (ScfInput * n)(*[ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), s.ctypes.data_as(dp), h.ctypes.data_as(dp))
+                               for b, s, h in zip(self.bases, S, H)])
+        opt = ScfOptions(maxits, eps, 0, SCF_DIIS, GUESS_CORE, diis_size, diis_tol, 0.0, 0.0, 0.0, 0, 8)
+        res = (BatchScfResult * n)()
+        P = np.zeros(self.total)
+        sec, used = C.c_double(), C.c_int()
+        rc = L.unomol_gpu_batch_scf(self._h, inp, n, C.byref(opt), 1 if graph else 0, res, P, C.byref(sec), C.byref(used))
+        note = L.unomol_gpu_batch_scf_last_error().decode(errors="replace")
+        if rc != 0:
+            raise UnomolError(f"unomol_gpu_batch_scf error {rc}: {note}")
+        return {"energy": np.array([r.energy for r in res]), "iterations": np.array([r.iterations for r in res]),
+                "converged": np.array([bool(r.converged) for r in res]),
+                "diis_error": np.array([r.diis_error for r in res]),
+                "P": [P[o:o + b.no2].copy() for o, b in zip(self.offsets, self.bases)],
+                "seconds": sec.value, "graph_used": bool(used.value), "capture_note": note}
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             lib().unomol_gpu_batch_destroy(self._h)
@@ -379,6 +442,15 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def l2_peak():
+    """(L2 read GB/s, FP64 atomic adds 1e9/s) of the current device (unomol_gpu_l2_peak)."""
+    L = lib()
+    L.unomol_gpu_l2_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    r, a = C.c_double(), C.c_double()
+    _check(L.unomol_gpu_l2_peak(C.byref(r), C.byref(a)))
+    return r.value, a.value
 
 
 def fma_peak(fp64: bool = True) -> float:
