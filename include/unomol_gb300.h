@@ -256,6 +256,10 @@ typedef struct UnomolScfResult {
     int purify_iterations;
     double purify_error;  /* guess 2: ||Q^2 - Q||_F at the end of the purification (per spin: max) */
     double guess_trace;   /* guess 2: tr Q after the purification (alpha spin for UHF) */
+    double seconds_setup; /* wall time of the parts of the SCF: set-up (handles, X, guess), */
+    double seconds_fock;  /* Fock builds (host call to result on the host), */
+    double seconds_diis;  /* DIIS error and extrapolation (+ level shift), */
+    double seconds_diag;  /* diagonalisation and new density */
 } UnomolScfResult;
 
 #define UNOMOL_GUESS_CORE 0

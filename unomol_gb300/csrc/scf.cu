@@ -418,6 +418,10 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
             if (rc) return fail(rc);
         }
     }
+    using clk = std::chrono::steady_clock;
+    auto since = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    double t_fock = 0.0, t_diis = 0.0, t_diag = 0.0;
+    const double t_setup = since(t0);
     const int maxits = opt->maxits > 0 ? opt->maxits : 300;
     const double eps = opt->eps;
     const int cflag = opt->conv_type;
@@ -458,6 +462,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
         }
         PprevA = Pa;
         if (uhf) PprevB = Pb;
+        const auto tf = clk::now();
         cudaMemcpyAsync(d_P, srcA, no2 * sizeof(double), cudaMemcpyHostToDevice, s);
         int r;
         if (!uhf) {
@@ -481,6 +486,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
             d.err = "Fock build failed on the device";
             return UNOMOL_ECUDA;
         }
+        t_fock += since(tf);
         if (!uhf) {
             energy = 2.0 * trace_packed(Pa, H, n) + trace_packed(Pa, Ga, n);
         } else {
@@ -491,6 +497,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
         for (size_t k = 0; k < no2; ++k) Fa[k] = H[k] + Ga[k];
         if (uhf)
             for (size_t k = 0; k < no2; ++k) Fb[k] = H[k] + Gb[k];
+        const auto td = clk::now();
         if (opt->accel == 2) {
             // DIIS on F; for UHF one set of coefficients for both spins (errors and Fock matrices of
             // the two spins concatenated), extrapolation only once the error is below diis_start
@@ -523,6 +530,8 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
                 }
             }
         }
+        t_diis += since(td);
+        const auto tg = clk::now();
         PoldA2 = PoldA;
         PoldA = Pa;
         r = diag_density(d, Fa, d_pk, noccA, Pa, evA, nullptr);
@@ -535,6 +544,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
             if (r) return r;
             pdiff += diffnorm_packed(Pb, PoldB, n);
         }
+        t_diag += since(tg);
         if (res->energies && iteration < res->energies_cap) res->energies[iteration] = energy + in->nucrep;
         ++iteration;
         return UNOMOL_OK;
@@ -594,6 +604,10 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     res->purify_iterations = pur_it;
     res->purify_error = pur_err;
     res->guess_trace = pur_tr;
+    res->seconds_setup = t_setup;
+    res->seconds_fock = t_fock;
+    res->seconds_diis = t_diis;
+    res->seconds_diag = t_diag;
     res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return UNOMOL_OK;
 }

@@ -240,7 +240,9 @@ class ScfResult(C.Structure):
                 ("iterations", C.c_int), ("converged", C.c_int), ("fock_builds", C.c_int),
                 ("energies", C.POINTER(C.c_double)), ("energies_cap", C.c_int), ("fock_ms", C.c_double),
                 ("densities", C.POINTER(C.c_double)), ("densities_cap", C.c_int), ("guess_used", C.c_int),
-                ("purify_iterations", C.c_int), ("purify_error", C.c_double), ("guess_trace", C.c_double)]
+                ("purify_iterations", C.c_int), ("purify_error", C.c_double), ("guess_trace", C.c_double),
+                ("seconds_setup", C.c_double), ("seconds_fock", C.c_double), ("seconds_diis", C.c_double),
+                ("seconds_diag", C.c_double)]
 
 
 class BatchScfResult(C.Structure):
@@ -328,7 +330,8 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
         raise UnomolError(f"unomol_scf error {rc}: {res.message.decode(errors='replace')}")
     out = {k: getattr(res, k) for k in ("energy", "e_electronic", "init_energy", "ediff", "pdiff", "diis_error",
                                         "seconds", "iterations", "converged", "fock_builds", "fock_ms",
-                                        "purify_iterations", "purify_error", "guess_trace")}
+                                        "purify_iterations", "purify_error", "guess_trace", "seconds_setup",
+                                        "seconds_fock", "seconds_diis", "seconds_diag")}
     out["guess_used"] = GUESS_USED.get(res.guess_used, str(res.guess_used))
     out["P"] = P
     out["orbital_energies"] = eps_orb
