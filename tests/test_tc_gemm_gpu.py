@@ -5,7 +5,8 @@ import pytest
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 32, 16), (300, 100, 70), (1000, 256, 256), (257, 128, 200)])
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 32, 16), (300, 100, 70), (1000, 256, 256), (257, 128, 200),
+                                   (300, 200, 64), (257, 48, 24), (4000, 256, 520), (129, 256, 1000)])
 def test_tc_gemm_matches_torch(gpu, M, N, K):
     import torch
     from unomol_gb300 import native

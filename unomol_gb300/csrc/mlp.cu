@@ -21,7 +21,94 @@ namespace {
 
 unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
-bool vec_ok(const void* p, int ld) { return ld % 8 == 0 && (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+// ---- tensor maps and the GEMM launch ----
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                  const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// row-major BF16 [rows x K] (row stride ld elements) read in boxes of box_rows x 64, 128-byte swizzle
+cudaError_t make_map(CUtensorMap* m, const void* ptr, int rows, int K, int ld, int box_rows) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <int BN>
+cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, const TcGemmArgs& g, dim3 grid, cudaStream_t s) {
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(tc_gemm_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcSmem<BN>::DYN);
+    if (attr != cudaSuccess) return attr;
+    tc_gemm_tma<BN><<<grid, TC_THREADS, TcSmem<BN>::DYN, s>>>(ma, mb, g);
+    return cudaGetLastError();
+}
+
+// C = A . B^T; operands K-major, row strides multiples of 8 elements, 16-byte aligned.  Split-K (an
+// additive epilogue) when the output has fewer tiles than the GPU has SMs.
+cudaError_t tc_gemm_launch(TcGemmArgs g, cudaStream_t s, int num_sms) {
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
+    if ((g.lda & 7) || (g.ldb & 7) || (reinterpret_cast<uintptr_t>(g.A) & 15) || (reinterpret_cast<uintptr_t>(g.B) & 15))
+        return cudaErrorInvalidValue;
+    const int bn = g.N <= 64 ? 64 : g.N <= 128 ? 128 : 256;
+    const int tiles_m = (g.M + TC_BM - 1) / TC_BM, tiles_n = (g.N + bn - 1) / bn;
+    const int nk = (g.K + TC_BK - 1) / TC_BK;
+    int splits = 1;
+    if (g.epi == TC_EPI_F32_ADD) {
+        splits = std::min(num_sms / (tiles_m * tiles_n), nk / 4);
+        splits = std::max(1, std::min(splits, nk));
+    }
+    g.chunks_per_split = (nk + splits - 1) / splits;
+    splits = (nk + g.chunks_per_split - 1) / g.chunks_per_split;  // every split has >= 1 chunk
+    CUtensorMap ma, mb;
+    cudaError_t e = make_map(&ma, g.A, g.M, g.K, g.lda, TC_BM);
+    if (e == cudaSuccess) e = make_map(&mb, g.B, g.N, g.K, g.ldb, bn);
+    if (e != cudaSuccess) return e;
+    const dim3 grid(tiles_m, tiles_n, splits);
+    if (bn == 64) return launch_bn<64>(ma, mb, g, grid, s);
+    if (bn == 128) return launch_bn<128>(ma, mb, g, grid, s);
+    return launch_bn<256>(ma, mb, g, grid, s);
+}
+
+// dst[c][r] = src[r][c] (BF16), 32 x 32 tiles through shared memory
+__global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ src, int rows, int cols, int lds,
+                                 __nv_bfloat16* __restrict__ dst, int ldd) {
+    __shared__ __nv_bfloat16 t[32][34];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) t[i][threadIdx.x] = src[(long long)r * lds + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) dst[(long long)c * ldd + r] = t[threadIdx.x][i];
+    }
+}
+
+cudaError_t transpose(const __nv_bfloat16* src, int rows, int cols, int lds, __nv_bfloat16* dst, int ldd, cudaStream_t s) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    k_transpose_bf16<<<dim3((cols + 31) / 32, (rows + 31) / 32), dim3(32, 8), 0, s>>>(src, rows, cols, lds, dst, ldd);
+    return cudaGetLastError();
+}
 
 // fp32 [rows x ldx] (first n_in columns) -> bf16 [rows x n_pad], zero padding
 __global__ void k_to_bf16_pad(const float* __restrict__ x, int ldx, int rows, int n_in, int n_pad,
@@ -90,7 +177,7 @@ uint64_t mix64(uint64_t& s) {
     } while (0)
 
 Mlp::~Mlp() {
-    for (void* p : std::vector<void*>{P, G, Am, Av, Wb, Wt, X, Y, dYb, dZb[0], dZb[1], dZf, status})
+    for (void* p : std::vector<void*>{P, G, Am, Av, Wb, Wt, X, Y, dYb, dZb[0], dZb[1], dZf, Ta, Tb, status})
         if (p) cudaFree(p);
     for (float* p : Z)
         if (p) cudaFree(p);
@@ -163,7 +250,8 @@ int Mlp::reserve(int r) {
     auto rel = [](void* p) {
         if (p) cudaFree(p);
     };
-    rel(X), rel(Y), rel(dYb), rel(dZb[0]), rel(dZb[1]), rel(dZf);
+    rel(X), rel(Y), rel(dYb), rel(dZb[0]), rel(dZb[1]), rel(dZf), rel(Ta), rel(Tb);
+    Ta = Tb = nullptr;
     for (float* p : Z) rel(p);
     for (__nv_bfloat16* p : H) rel(p);
     X = nullptr, Y = nullptr, dYb = nullptr, dZb[0] = dZb[1] = nullptr, dZf = nullptr;
@@ -177,6 +265,9 @@ int Mlp::reserve(int r) {
     MLP_CK(cudaMalloc(&dZb[0], R * hidden * sizeof(__nv_bfloat16)));
     MLP_CK(cudaMalloc(&dZb[1], R * hidden * sizeof(__nv_bfloat16)));
     MLP_CK(cudaMalloc(&dZf, R * hidden * sizeof(float)));
+    const size_t Rp = (R + 7) / 8 * 8;  // transposed operands: row stride a multiple of 8 elements
+    MLP_CK(cudaMalloc(&Ta, Rp * std::max(hidden, n_out) * sizeof(__nv_bfloat16)));
+    MLP_CK(cudaMalloc(&Tb, Rp * std::max(hidden, n_in_pad) * sizeof(__nv_bfloat16)));
     for (int l = 0; l < layers; ++l) {
         MLP_CK(cudaMalloc(&Z[l], R * hidden * sizeof(float)));
         MLP_CK(cudaMalloc(&H[l], R * hidden * sizeof(__nv_bfloat16)));
@@ -213,8 +304,6 @@ int Mlp::forward_x(int r, cudaStream_t s) {
         g.M = r;
         g.N = dout[l];
         g.K = din_pad[l];
-        g.vec_a = vec_ok(g.A, g.lda);
-        g.vec_b = vec_ok(g.B, g.ldb);
         g.bias = P + b_off[l];
         g.status = status;
         if (l < layers) {
@@ -247,13 +336,15 @@ int Mlp::backward(const float* dy, bool accumulate, cudaStream_t s) {
         k_colsum<<<grid, 64, 0, s>>>(dy, r, n_out, n_out, G + b_off[L]);
     }
     MLP_CK(cudaGetLastError());
-    // dW_L = dY^T . h_L
+    const int rp = (r + 7) / 8 * 8;
+    // dW_L = dY^T . h_L  (operands transposed to K-major: K = rows)
     {
+        MLP_CK(transpose(dYb, r, n_out, n_out, Ta, rp, s));
+        MLP_CK(transpose(H[L - 1], r, hidden, hidden, Tb, rp, s));
         TcGemmArgs g{};
-        g.A = dYb, g.lda = n_out, g.a_trans = 1;
-        g.B = H[L - 1], g.ldb = hidden, g.b_trans = 1;
+        g.A = Ta, g.lda = rp;
+        g.B = Tb, g.ldb = rp;
         g.M = n_out, g.N = hidden, g.K = r;
-        g.vec_a = vec_ok(g.A, g.lda), g.vec_b = vec_ok(g.B, g.ldb);
         g.epi = TC_EPI_F32_ADD, g.Cf = G + w_off[L], g.ldc = din_pad[L];
         g.status = status;
         MLP_CK(tc_gemm_launch(g, s, num_sms));
@@ -268,7 +359,6 @@ int Mlp::backward(const float* dy, bool accumulate, cudaStream_t s) {
             g.A = dg, g.lda = dg_ld;
             g.B = Wt + wt_off[l + 1], g.ldb = dout[l + 1];
             g.M = r, g.N = hidden, g.K = dout[l + 1];
-            g.vec_a = vec_ok(g.A, g.lda), g.vec_b = vec_ok(g.B, g.ldb);
             g.epi = TC_EPI_DSILU, g.Z = Z[l], g.Cb = dZb[cur], g.Cf = dZf, g.ldc = hidden;
             g.status = status;
             MLP_CK(tc_gemm_launch(g, s, num_sms));
@@ -278,13 +368,14 @@ int Mlp::backward(const float* dy, bool accumulate, cudaStream_t s) {
             k_colsum<<<grid, 256, 0, s>>>(dZf, r, hidden, hidden, G + b_off[l]);
             MLP_CK(cudaGetLastError());
         }
-        // dW_l = dz_l^T . h_l  (h_0 = x)
+        // dW_l = dz_l^T . h_l  (h_0 = x; operands transposed to K-major)
         {
+            MLP_CK(transpose(dZb[cur], r, hidden, hidden, Ta, rp, s));
+            MLP_CK(transpose(l == 0 ? X : H[l - 1], r, din_pad[l], din_pad[l], Tb, rp, s));
             TcGemmArgs g{};
-            g.A = dZb[cur], g.lda = hidden, g.a_trans = 1;
-            g.B = l == 0 ? X : H[l - 1], g.ldb = din_pad[l], g.b_trans = 1;
+            g.A = Ta, g.lda = rp;
+            g.B = Tb, g.ldb = rp;
             g.M = hidden, g.N = din_pad[l], g.K = r;
-            g.vec_a = vec_ok(g.A, g.lda), g.vec_b = vec_ok(g.B, g.ldb);
             g.epi = TC_EPI_F32_ADD, g.Cf = G + w_off[l], g.ldc = din_pad[l];
             g.status = status;
             MLP_CK(tc_gemm_launch(g, s, num_sms));
@@ -367,16 +458,36 @@ int unomol_tc_gemm_bf16(const void* A, const void* B, int M, int N, int K, float
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    TcGemmArgs g{};
-    g.A = static_cast<const __nv_bfloat16*>(A);
-    g.B = static_cast<const __nv_bfloat16*>(B);
-    g.M = M, g.N = N, g.K = K, g.lda = K, g.ldb = K;
-    g.vec_a = vec_ok(A, K), g.vec_b = vec_ok(B, K);
-    g.epi = TC_EPI_F32;
-    g.Cf = C;
-    g.ldc = N;
-    g.status = status;
-    cudaError_t e = tc_gemm_launch(g, (cudaStream_t)stream, sms);
+    cudaStream_t s = (cudaStream_t)stream;
+    // the TMA unit wants 16-byte row strides and bases: copy ragged operands into padded rows
+    const int kp = (K + 7) / 8 * 8;
+    const bool pad = kp != K || (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15);
+    __nv_bfloat16 *pa = nullptr, *pb = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (pad && M > 0 && N > 0 && K > 0) {
+        e = cudaMalloc(&pa, (size_t)M * kp * 2);
+        if (e == cudaSuccess) e = cudaMalloc(&pb, (size_t)N * kp * 2);
+        if (e == cudaSuccess) e = cudaMemsetAsync(pa, 0, (size_t)M * kp * 2, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(pb, 0, (size_t)N * kp * 2, s);
+        if (e == cudaSuccess) e = cudaMemcpy2DAsync(pa, kp * 2, A, (size_t)K * 2, (size_t)K * 2, M, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpy2DAsync(pb, kp * 2, B, (size_t)K * 2, (size_t)K * 2, N, cudaMemcpyDeviceToDevice, s);
+    }
+    if (e == cudaSuccess) {
+        TcGemmArgs g{};
+        g.A = pad ? pa : static_cast<const __nv_bfloat16*>(A);
+        g.B = pad ? pb : static_cast<const __nv_bfloat16*>(B);
+        g.M = M, g.N = N, g.K = K, g.lda = pad ? kp : K, g.ldb = pad ? kp : K;
+        g.epi = TC_EPI_F32;
+        g.Cf = C;
+        g.ldc = N;
+        g.status = status;
+        e = tc_gemm_launch(g, s, sms);
+    }
+    if (pad) {
+        cudaStreamSynchronize(s);
+        if (pa) cudaFree(pa);
+        if (pb) cudaFree(pb);
+    }
     if (e != cudaSuccess) {
         g_mlp_err = cudaGetErrorString(e);
         return UNOMOL_ECUDA;

@@ -34,6 +34,7 @@ struct Mlp {
     __nv_bfloat16* dYb = nullptr;              // [cap x n_out]
     __nv_bfloat16* dZb[2] = {nullptr, nullptr};  // [cap x hidden]
     float* dZf = nullptr;                      // [cap x hidden]
+    __nv_bfloat16 *Ta = nullptr, *Tb = nullptr;  // transposed operands of the weight gradients
     int* status = nullptr;                     // device flag: a GEMM wait gave up
     std::string err;
 

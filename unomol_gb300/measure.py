@@ -11,6 +11,11 @@
         graph, batched with plain launches, and one molecule at a time through the single-molecule
         driver (wall times; contexts created outside the timing), with the energy differences.
 
+    python -m unomol_gb300.measure gemm [--reps 20] [--out gemm.json]
+        The tcgen05 GEMM of the learned guess at the network's shapes (13 856 rows = 16 decane molecules)
+        and one 8192^3 square, device time by CUDA events (mean of reps after a warm-up), TFLOP/s against
+        the measured BF16 peak of MEASURED_PEAKS.json, with cuBLAS (torch.matmul) beside it.
+
     python -m unomol_gb300.measure sweep [--out sweep.json]
         FP32 cutoff sweep of the precision form on the 32-water 6-31G cluster (molecules.water_cluster(32, 0),
         superposition-of-fragments guess, DIIS, 1e-10 Eh): the incremental mixed-precision SCF against the
@@ -126,13 +131,67 @@ def _sweep() -> dict:
     return out
 
 
+def _gemm(reps: int) -> dict:
+    """The tensor-core GEMM of the learned guess (unomol_tc_gemm_bf16, C = A B^T, BF16 in, FP32 out)
+    against cuBLAS (torch.matmul, BF16 in and out) at the network's shapes and one large square."""
+    import ctypes as C
+
+    import torch
+    from .learned import _lib
+    L = _lib()
+    dev = torch.device("cuda", 0)
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    s = torch.cuda.current_stream()
+    peak = None
+    try:
+        with open(__import__("os").path.join(__import__("os").path.dirname(__file__), "..", "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    shapes = [("hidden layer, 16 decane molecules", 13856, 256, 256), ("first layer", 13856, 256, 24),
+              ("output layer", 13856, 48, 256), ("dH backward", 13856, 256, 48), ("square 8192", 8192, 8192, 8192)]
+    out = {"bf16_peak_tflops": peak, "rows": []}
+    for name, M, N, K in shapes:
+        g = torch.Generator(device="cpu").manual_seed(M + N + K)
+        A = torch.randn(M, K, generator=g).to(torch.bfloat16).to(dev)
+        B = torch.randn(N, K, generator=g).to(torch.bfloat16).to(dev)
+        Cm = torch.empty(M, N, dtype=torch.float32, device=dev)
+
+        def ours():
+            rc = L.unomol_tc_gemm_bf16(A.data_ptr(), B.data_ptr(), M, N, K, Cm.data_ptr(), st.data_ptr(),
+                                       C.c_void_p(s.cuda_stream))
+            assert rc == 0
+
+        def timed(fn):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        ms = timed(ours)
+        ms_cublas = timed(lambda: A @ B.T)
+        err = float((Cm - (A.float() @ B.float().T)).abs().max())
+        fl = 2.0 * M * N * K
+        byt = 2.0 * (M * K + N * K) + 4.0 * M * N
+        out["rows"].append({"shape": name, "M": M, "N": N, "K": K, "ms": ms, "tflops": fl / ms / 1e9,
+                            "frac_of_bf16_peak": fl / ms / 1e9 / peak if peak else None,
+                            "gbs": byt / ms / 1e6, "ms_cublas_bf16_out": ms_cublas, "max_abs_err": err,
+                            "status_flag": int(st.item())})
+    return out
+
+
 def main():
-    ap = argparse.ArgumentParser(description="batching / precision-form measurements")
-    ap.add_argument("what", choices=["batch", "sweep"])
+    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM measurements")
+    ap.add_argument("what", choices=["batch", "sweep", "gemm"])
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
-    rep = _batch(a.reps) if a.what == "batch" else _sweep()
+    rep = _batch(a.reps) if a.what == "batch" else _sweep() if a.what == "sweep" else _gemm(max(a.reps, 10))
     print(json.dumps(rep, indent=1))
     if a.out:
         with open(a.out, "w") as f:
