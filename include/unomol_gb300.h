@@ -236,7 +236,13 @@ typedef struct UnomolScfOptions {
     double level_shift_until; /* ... applied while the DIIS error is above this */
     int incremental;     /* 1: G(P) = G(P_prev) + G(P - P_prev) between full builds (new) */
     int rebuild_every;   /* incremental: a full build every this many builds (<= 0: 8) */
+    int loop;            /* UNOMOL_SCF_LOOP_GROUND: the loop of findEnergy (two updates, then the
+                            convergence test; RHF.hpp:138-162); UNOMOL_SCF_LOOP_DPM: the loop of
+                            findPolarizationPotential (one update, then the test; RHF.hpp:323-329) */
 } UnomolScfOptions;
+
+#define UNOMOL_SCF_LOOP_GROUND 0
+#define UNOMOL_SCF_LOOP_DPM 1
 
 typedef struct UnomolScfResult {
     int status;
@@ -352,6 +358,12 @@ int unomol_guess_get_params(UnomolGuess* g, float* out);
 int unomol_guess_set_params(UnomolGuess* g, const float* in);
 void unomol_guess_destroy(UnomolGuess* g);
 const char* unomol_guess_last_error(const UnomolGuess* g);
+
+/* DPM polarisation-potential integrals (GDPMInts.cpp:86-143): H -= sum_k c_k (mu nu | g_k), with
+ * g_k = exp(-a_k |r - q|^2) the six-Gaussian positron charge at q (bohr), over the context's basis
+ * (packed H on the host, subtracted in place).  Shells up to d. */
+int unomol_gpu_gdpm(UnomolCtx* ctx, const double* q, double* H);
+const char* unomol_gpu_gdpm_last_error(void);
 
 /* Last error of this context (ctx may be NULL for errors raised before a context existed). */
 const char* unomol_gpu_last_error(const UnomolCtx* ctx);

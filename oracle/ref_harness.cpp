@@ -8,6 +8,7 @@
 //   * G(P) for RHF and UHF                           [TwoElectronInts.cpp:822-869]
 //   * one-electron S, T, H                          [OneElectronInts.cpp]
 //   * the stock RHF / UHF SCF                       [RHF.hpp:114-176, UHF.hpp:137-177]
+//   * the DPM one-electron matrices                 [OneElectronInts.cpp, GDPMInts.cpp:86-143]
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -169,6 +170,34 @@ int refh_scf(const char* patin, const char* workdir, double* out, double* P_out)
     }
     out[6] = std::chrono::duration<double>(t1 - t0).count();
     out[7] = std::chrono::duration<double>(t2 - t1).count();
+    if (chdir(cwd) != 0) return -3;
+    return 0;
+}
+
+// DPM one-electron matrices [OneElectronInts.cpp, GDPMInts.cpp:86-143]: in directory `dir` (patin.dat
+// with int_flag[0] = 1 and posin.bas), the basis augmented with the positron shells (Basis.hpp:341-345),
+// the positron centre at q (Basis.hpp:346-348); H_plain = T + V over all centres (the positron a +1
+// point charge), H_dpm = H_plain minus the DPM potential integrals.  Packed over the augmented basis.
+int refh_dpm_h(const char* dir, const double* q, double* S, double* H_plain, double* H_dpm, int* dims) {
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof(cwd))) return -1;
+    if (chdir(dir) != 0) return -2;
+    {
+        Basis b(std::string("patin.dat"));
+        const int pcen = b.skip_center();
+        b.dpm_augment();
+        b.SetCenterPosition(q[0], q[1], q[2], pcen);
+        const int no = b.number_of_orbitals(), no2 = no * (no + 1) / 2;
+        dims[0] = b.number_of_shells();
+        dims[1] = no;
+        dims[2] = b.number_of_centers();
+        if (S) {
+            std::vector<double> T(no2);
+            unomol::OneElectronInts(b, S, T.data(), H_plain);
+            std::memcpy(H_dpm, H_plain, sizeof(double) * no2);
+            unomol::GDPMInts(b, H_dpm);
+        }
+    }
     if (chdir(cwd) != 0) return -3;
     return 0;
 }

@@ -59,8 +59,27 @@ def lib(md=False) -> C.CDLL:
     L.refh_one_electron.argtypes = [C.c_void_p, _dp, _dp, _dp]
     L.refh_scf.restype = C.c_int
     L.refh_scf.argtypes = [C.c_char_p, C.c_char_p, _dp, C.c_void_p]
+    L.refh_dpm_h.restype = C.c_int
+    L.refh_dpm_h.argtypes = [C.c_char_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, _ip]
     _LIBS[name] = L
     return L
+
+
+def dpm_h(workdir: str, q):
+    """S, T + V, and T + V minus the DPM potential integrals of the reference (GDPMInts.cpp:86-143) over
+    the positron-augmented basis of workdir/patin.dat + workdir/posin.bas, positron at q (bohr)."""
+    L = lib()
+    dims = np.zeros(3, np.int32)
+    qq = np.ascontiguousarray(q, np.float64)
+    rc = L.refh_dpm_h(os.path.abspath(workdir).encode(), qq, None, None, None, dims)
+    if rc:
+        raise RuntimeError(f"refh_dpm_h: {rc}")
+    no2 = int(dims[1]) * (int(dims[1]) + 1) // 2
+    S, Hp, Hd = np.zeros(no2), np.zeros(no2), np.zeros(no2)
+    rc = L.refh_dpm_h(os.path.abspath(workdir).encode(), qq, S.ctypes.data, Hp.ctypes.data, Hd.ctypes.data, dims)
+    if rc:
+        raise RuntimeError(f"refh_dpm_h: {rc}")
+    return S, Hp, Hd
 
 
 class RefBasis:

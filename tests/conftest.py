@@ -20,6 +20,8 @@ def golden_cases(pattern="*.npz", exclude_md=True):
         name = os.path.basename(p)[:-4]
         if exclude_md and name.endswith("_md"):
             continue
+        if name.startswith("dpm_"):  # DPM grids: their own tests (test_dpm.py)
+            continue
         out.append(name)
     return out
 

@@ -2,8 +2,8 @@
 
 Only the input side of the reference is mirrored: the header and flags, centres, shells, AO
 offsets (Basis.hpp:226-232), the primitive normalisation folded into the coefficients
-(Shell::normalize, Basis.hpp:56-75) and the eps clamp (Basis.hpp:249-254).  The positron basis of
-the DPM path (posin.bas) is not read.
+(Shell::normalize, Basis.hpp:56-75) and the eps clamp (Basis.hpp:249-254).  The positron basis of the
+DPM path (posin.bas, Basis.hpp:207-245) is read by read_posin and appended by dpm_augment.
 """
 from __future__ import annotations
 
@@ -88,6 +88,56 @@ class Basis:
             for j in range(i + 1, self.ncen):
                 s += self.charges[i] * self.charges[j] / math.sqrt(float(((self.centers[i] - self.centers[j]) ** 2).sum()))
         return s
+
+
+def read_posin(text: str):
+    """posin.bas (Basis.hpp:207-245): "nshell norb maxl", then per shell "npr L" and npr lines
+    "alpha coef" (the shells sit on the positron centre).  Returns [(L, alphas, normalised coefs)]."""
+    tok = text.split()
+    nsh, norb, _maxl = int(tok[0]), int(tok[1]), int(tok[2])
+    pos, out, nf = 3, [], 0
+    for _ in range(nsh):
+        npr, l = int(tok[pos]), int(tok[pos + 1])
+        pos += 2
+        a = [float(tok[pos + 2 * k]) for k in range(npr)]
+        c = [float(tok[pos + 2 * k + 1]) for k in range(npr)]
+        pos += 2 * npr
+        out.append((l, a, _normalize(l, a, c)))
+        nf += (l + 1) * (l + 2) // 2
+    if nf != norb:
+        raise ValueError(f"posin.bas declares {norb} orbitals, shells give {nf}")
+    return out
+
+
+def dpm_augment(b: "Basis", posin: str, position) -> "Basis":
+    """The positron-augmented basis of the DPM path (Basis.hpp:229-245, 341-348): a centre of charge +1
+    at `position` (bohr) appended after the molecule's centres, carrying the posin.bas shells, whose
+    functions follow the molecule's.  The electron count does not change."""
+    import copy
+    a = copy.copy(b)
+    shells = read_posin(posin)
+    a.skip_center = b.ncen
+    a.ncen = b.ncen + 1
+    a.charges = np.append(np.asarray(b.charges, float), 1.0)
+    a.centers = np.vstack([np.asarray(b.centers, float), np.asarray(position, float).reshape(1, 3)])
+    a.shell_l, a.shell_nprim = list(b.shell_l), list(b.shell_nprim)
+    a.shell_center, a.shell_offset = list(b.shell_center), list(b.shell_offset)
+    alpha, coef = list(b.alpha), list(b.coef)
+    off = b.norb
+    for l, al, co in shells:
+        a.shell_l.append(l)
+        a.shell_nprim.append(len(al))
+        a.shell_center.append(b.ncen)
+        a.shell_offset.append(off)
+        off += (l + 1) * (l + 2) // 2
+        alpha += al
+        coef += co
+    a.alpha, a.coef = np.array(alpha), np.array(coef)
+    a.nshell = len(a.shell_l)
+    a.norb = off
+    a.no2 = off * (off + 1) // 2
+    a.maxl = max(b.maxl, max(l for l, _, _ in shells))
+    return a
 
 
 def _normalize(l: int, a, c):

@@ -569,10 +569,12 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     eold = 0.0;
     if ((rc = update())) return fail(rc);
     init_energy = energy + in->nucrep;
-    iteration = 1;
-    if (uhf) eold = 0.0;  // UHF.hpp:158-160 resets eold before the second update, RHF does not
-    if ((rc = update())) return fail(rc);
-    iteration = 2;
+    if (opt->loop != UNOMOL_SCF_LOOP_DPM) {
+        iteration = 1;
+        if (uhf) eold = 0.0;  // UHF.hpp:158-160 resets eold before the second update, RHF does not
+        if ((rc = update())) return fail(rc);
+        iteration = 2;
+    }
     bool conv = false;
     while (iteration < maxits) {
         converger();

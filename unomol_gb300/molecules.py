@@ -117,6 +117,25 @@ def batch_workload(seed: int = 0, n: int = 256):
     return out
 
 
+# A small positron basis for the DPM path (posin.bas: "nshell norb maxl", then per shell "npr L" and
+# npr lines "alpha coef"; the shells sit on the positron centre): two s and one p Gaussian.
+POSITRON_BASIS = [(0, [(2.0, 1.0)]), (0, [(0.4, 1.0)]), (1, [(0.5, 1.0)])]
+
+
+def posin_text(shells=POSITRON_BASIS) -> str:
+    norb = sum((l + 1) * (l + 2) // 2 for l, _ in shells)
+    out = [f"{len(shells)} {norb} {max(l for l, _ in shells)}"]
+    for l, prims in shells:
+        out.append(f"{len(prims)} {l}")
+        out += [f"{a:20.10f}{c:20.10f}" for a, c in prims]
+    return "\n".join(out) + "\n"
+
+
+def grid_text(points) -> str:
+    """pos.grid.dat: the number of points, then x y z (bohr) per point (RHF.hpp:308-313)."""
+    return "\n".join([str(len(points))] + [f"{x:.10f} {y:.10f} {z:.10f}" for x, y, z in points]) + "\n"
+
+
 def perturb(atoms, sigma: float, seed: int):
     """Isotropic Gaussian displacement of every atom (Angstrom)."""
     rng = np.random.default_rng(seed)
@@ -124,8 +143,9 @@ def perturb(atoms, sigma: float, seed: int):
 
 
 def patin_text(atoms, basis: str, charge: int = 0, maxits: int = 300, eps: float = 1e-10,
-               scf_flags=(2, 1, 0)) -> str:
-    """patin.dat text for `atoms` (Angstrom) in `basis`, shells atom after atom."""
+               scf_flags=(2, 1, 0), int_flags=(0, 0)) -> str:
+    """patin.dat text for `atoms` (Angstrom) in `basis`, shells atom after atom.  int_flags[0] = 1
+    asks for the DPM polarisation potential (positron basis in posin.bas, positions in pos.grid.dat)."""
     lib = basis_sets()
     shells = []
     for c, (e, _) in enumerate(atoms):
@@ -135,7 +155,7 @@ def patin_text(atoms, basis: str, charge: int = 0, maxits: int = 300, eps: float
     maxl = max(l for l, _, _ in shells)
     nelec = sum(Z[e.upper()] for e, _ in atoms) - charge
     out = [f"{len(shells):7d}{norb:7d}{len(atoms):7d}{maxl:3d}", f"{nelec:7d}{maxits:7d}", f"{eps:24.16e}",
-           " 0 0", " " + " ".join(str(v) for v in scf_flags), " 0 0 0"]
+           " " + " ".join(str(v) for v in int_flags), " " + " ".join(str(v) for v in scf_flags), " 0 0 0"]
     for e, x in atoms:
         out.append(f"{float(Z[e.upper()]):15.10f}" + "".join(f"{v / BOHR:20.12f}" for v in x))
     for l, prims, c in shells:

@@ -33,7 +33,7 @@ EXPORTS = [
     "unomol_guess_num_molecules", "unomol_guess_train", "unomol_guess_loss", "unomol_guess_predict",
     "unomol_guess_get_params", "unomol_guess_set_params", "unomol_guess_destroy", "unomol_guess_last_error",
     "unomol_gpu_one_electron", "unomol_gpu_one_electron_last_error", "unomol_gpu_l2_peak", "unomol_gpu_batch_scf",
-    "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size",
+    "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -176,6 +176,16 @@ class TwoElectronInts:
         _check(lib().unomol_gpu_fock_uhf_device(self._h, C.c_void_p(dPa), C.c_void_p(dPb), C.c_void_p(dGa),
                                                 C.c_void_p(dGb), C.c_void_p(stream)), self._h)
 
+    def gdpm(self, q, H):
+        """H -= the DPM potential integrals of a positron at q (unomol_gpu_gdpm, GDPMInts.cpp:86-143)."""
+        L = lib()
+        L.unomol_gpu_gdpm.argtypes = [C.c_void_p, _dp, _dp]
+        L.unomol_gpu_gdpm_last_error.restype = C.c_char_p
+        rc = L.unomol_gpu_gdpm(self._h, np.ascontiguousarray(q, np.float64), H)
+        if rc != 0:
+            raise UnomolError(f"unomol_gpu_gdpm error {rc}: {L.unomol_gpu_gdpm_last_error().decode()}")
+        return H
+
     def set_precision(self, mode: int, fp32_cutoff: float = 1e-10):
         _check(lib().unomol_gpu_set_precision(self._h, int(mode), float(fp32_cutoff)), self._h)
 
@@ -230,7 +240,7 @@ class ScfOptions(C.Structure):
     _fields_ = [("maxits", C.c_int), ("eps", C.c_double), ("conv_type", C.c_int), ("accel", C.c_int),
                 ("guess", C.c_int), ("diis_size", C.c_int), ("diis_tol", C.c_double),
                 ("diis_start", C.c_double), ("level_shift", C.c_double), ("level_shift_until", C.c_double),
-                ("incremental", C.c_int), ("rebuild_every", C.c_int)]
+                ("incremental", C.c_int), ("rebuild_every", C.c_int), ("loop", C.c_int)]
 
 
 class ScfResult(C.Structure):
@@ -252,17 +262,29 @@ class BatchScfResult(C.Structure):
 
 SCF_DAMPED = 0
 SCF_DIIS = 2
+SCF_LOOP_GROUND, SCF_LOOP_DPM = 0, 1
 GUESS_CORE, GUESS_GIVEN, GUESS_PURIFY = 0, 1, 2
 GUESS_USED = {0: "core", 1: "given", 2: "purified", 3: "fallback"}
 
 
-def one_electron(b: Basis):
+def attracting_charges(b: Basis):
+    """Charges of the nuclear attraction: every centre's, except the positron centre of a DPM basis,
+    which the reference skips there (OneElectronInts.cpp:43; its attraction is the DPM potential)."""
+    q = np.array(b.charges, np.float64)
+    skip = getattr(b, "skip_center", None)
+    if skip is not None and skip < len(q):
+        q[skip] = 0.0
+    return q
+
+
+def one_electron(b: Basis, charges=None):
     """S, T, H (packed) of the basis: unomol_one_electron (host code of the library)."""
     L = lib()
     L.unomol_one_electron.argtypes = [C.POINTER(BasisDesc), _dp, _dp, _dp, _dp]
     d, keep = basis_desc(b)
     S, T, H = np.zeros(b.no2), np.zeros(b.no2), np.zeros(b.no2)
-    _check(L.unomol_one_electron(C.byref(d), np.ascontiguousarray(b.charges, np.float64), S, T, H))
+    q = attracting_charges(b) if charges is None else charges
+    _check(L.unomol_one_electron(C.byref(d), np.ascontiguousarray(q, np.float64), S, T, H))
     return S, T, H
 
 
@@ -279,7 +301,7 @@ def one_electron_gpu(b: Basis, centers=None, with_t: bool = False):
     ng = cen.shape[0]
     S, H = np.zeros((ng, b.no2)), np.zeros((ng, b.no2))
     T = np.zeros((ng, b.no2)) if with_t else None
-    rc = L.unomol_gpu_one_electron(C.byref(d), np.ascontiguousarray(b.charges, np.float64), ng, cen.ctypes.data,
+    rc = L.unomol_gpu_one_electron(C.byref(d), np.ascontiguousarray(attracting_charges(b), np.float64), ng, cen.ctypes.data,
                                    S.ctypes.data, T.ctypes.data if with_t else None, H.ctypes.data)
     if rc != 0:
         raise UnomolError(f"unomol_gpu_one_electron error {rc}: {L.unomol_gpu_one_electron_last_error().decode()}")
@@ -293,7 +315,7 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
         maxits: int | None = None, eps: float | None = None, conv_type: int | None = None,
         diis_size: int = 8, diis_tol: float = 1e-6, record: int = 0, diis_start: float = 0.0,
         level_shift: float = 0.0, level_shift_until: float = 0.05, incremental: bool = False,
-        rebuild_every: int = 8, keep_densities: int = 0, purify: bool = False):
+        rebuild_every: int = 8, keep_densities: int = 0, purify: bool = False, loop: int = 0):
     """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ...
     purify: start from guess_P after McWeeny purification and a trace check, or from the core
     Hamiltonian when it fails them (out["guess_used"] says which)."""
@@ -310,7 +332,7 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
                      conv_type if conv_type is not None else b.scf_flag[0], accel,
                      GUESS_CORE if guess_P is None else (GUESS_PURIFY if purify else GUESS_GIVEN),
                      diis_size, diis_tol, diis_start, level_shift, level_shift_until, 1 if incremental else 0,
-                     rebuild_every)
+                     rebuild_every, loop)
     uhf = b.nelec % 2 == 1
     P = np.zeros(b.no2 * (2 if uhf else 1))
     if guess_P is not None:
@@ -421,7 +443,7 @@ class Batch:
         dp = C.POINTER(C.c_double)
         inp = (ScfInput * n)(*[ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), s.ctypes.data_as(dp), h.ctypes.data_as(dp))
                                for b, s, h in zip(self.bases, S, H)])
-        opt = ScfOptions(maxits, eps, 0, SCF_DIIS, GUESS_CORE, diis_size, diis_tol, 0.0, 0.0, 0.0, 0, 8)
+        opt = ScfOptions(maxits, eps, 0, SCF_DIIS, GUESS_CORE, diis_size, diis_tol, 0.0, 0.0, 0.0, 0, 8, 0)
         res = (BatchScfResult * n)()
         P = np.zeros(self.total)
         sec, used = C.c_double(), C.c_int()
