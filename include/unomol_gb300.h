@@ -288,14 +288,19 @@ int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* input, const UnomolScfOptio
  * X^T F X, batched eigen-solve, P = C_occ C_occ^T) for all molecules, with converged molecules frozen;
  * with graph != 0 the iteration is captured once as a CUDA graph and replayed (graph_used reports
  * whether the capture succeeded; unomol_gpu_batch_scf_last_error then names what stopped it).
- * inputs: [nmol] (S, H packed, nelec even), options: maxits, eps, diis_size, diis_tol (the DIIS
- * criterion of unomol_scf; core-Hamiltonian guess).  P_out: optional, the batch's packed densities. */
+ * inputs: [nmol] (S, H packed, nelec even); options: maxits, eps, conv_type, accel (UNOMOL_SCF_DIIS:
+ * the DIIS update and test of unomol_scf; otherwise the reference's damping and is_converged),
+ * guess (core Hamiltonian, or UNOMOL_GUESS_GIVEN: the densities in P_io), loop (ground-state or DPM
+ * loop order), diis_size, diis_tol.  P_io: the batch's packed densities (in: the guess when given;
+ * out: the final densities; may be NULL with the core-Hamiltonian guess). */
 typedef struct UnomolBatchScfResult {
     double energy, e_electronic, diis_error;
     int iterations, converged;
+    double init_energy;   /* energy after the first update (short.gs.out line 1; vpol's E_init) */
+    double ediff, pdiff;  /* of the last update */
 } UnomolBatchScfResult;
 int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* inputs, int nmol, const UnomolScfOptions* options,
-                         int graph, UnomolBatchScfResult* results, double* P_out, double* seconds, int* graph_used);
+                         int graph, UnomolBatchScfResult* results, double* P_io, double* seconds, int* graph_used);
 const char* unomol_gpu_batch_scf_last_error(void);
 
 /* ---- Learned initial density (no reference counterpart; the reference starts from the core

@@ -61,3 +61,19 @@ def test_gpu_polarization_potential_matches_reference(gpu, name):
         assert abs(r["alfa"] - v[4]) < 2.0 * r4 * 1e-10 + 1e-12  # alfa = -2 vpol r^4 carries vpol's error
         assert abs(r["vstat"] - v[5]) < 1e-10, (r["vstat"], v[5])
         assert abs(r["vsum"] - v[6]) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [True, False])
+def test_gpu_batched_polarization_potential_matches_reference(gpu, graph):
+    from unomol_gb300 import dpm
+    from unomol_gb300.basis import Basis
+    g = load_golden("dpm_h2o_sto3g")
+    b = Basis(text=str(g["patin"]))
+    rows, info = dpm.polarization_potential_batched(b, str(g["posin"]), g["points"], graph=graph)
+    assert info["graph_used"] == graph, info
+    for r, v, sp in zip(rows, g["vpol"], g["spol"]):
+        assert r["converged"]
+        assert abs(r["e_init"] - sp[2]) < 1e-9 and abs(r["e_final"] - sp[3]) < 1e-9
+        assert abs(r["vpol"] - v[3]) < 1e-10, (r["vpol"], v[3])
+        assert abs(r["vstat"] - v[5]) < 1e-10

@@ -4,7 +4,8 @@
 // driver (scf.cu): one batched Fock build (fock_batch.cu: persistent kernels over the merged work
 // lists), F = H + G and the energy 2 tr(PH) + tr(PG) per molecule, the DIIS error X^T (FPS - SPF) X,
 // Pulay extrapolation over the last diis_size Fock matrices, F' = X^T F X, the eigenvectors of F'
-// (cuSOLVER batched syev, FP64), C = X W and P = C_occ C_occ^T.  With `graph` set the whole iteration is
+// (cuSOLVER batched syev, FP64), C = X W and P = C_occ C_occ^T -- or, with the reference's
+// accelerator, its damping (RHF.hpp:536-569) and convergence tests.  With `graph` set the whole iteration is
 // captured once as a CUDA graph and replayed; the host reads only the per-molecule convergence flags
 // after each replay.  A molecule that has converged is frozen (its P and energy stop changing) while
 // the others go on.
@@ -45,7 +46,8 @@ struct BState {
            *Pf = nullptr, *Ecur = nullptr, *W = nullptr, *Hpk = nullptr;
     double *Fh = nullptr, *Eh = nullptr;  // [maxv][tot2]
     double *B = nullptr, *coef = nullptr;  // [nmol][maxv][maxv], [nmol][maxv]
-    double *Enew = nullptr, *Eold = nullptr, *err = nullptr;  // [nmol]
+    double *Enew = nullptr, *Eold = nullptr, *err = nullptr, *dE = nullptr, *pdiff = nullptr, *Einit = nullptr;  // [nmol]
+    double* Pold = nullptr;               // packed, batch order: the density before the last update's diagonalisation
     int *nupd = nullptr, *conv = nullptr, *its = nullptr, *info = nullptr, *bad = nullptr;
     // grouped-GEMM pointer arrays (device) per product
     const double** pa[8] = {};
@@ -63,7 +65,7 @@ struct BState {
     std::string err_msg, capture_error;
     ~BState() {
         for (void* p : std::vector<void*>{d_mols, S, X, H, F, Fo, T1, T2, Pf, Ecur, W, Hpk, Fh, Eh, B, coef, Enew, Eold,
-                                          err, nupd, conv, its, info, bad, dwork, cublas_ws})
+                                          err, dE, pdiff, Einit, Pold, nupd, conv, its, info, bad, dwork, cublas_ws})
             if (p) cudaFree(p);
         for (int k = 0; k < 8; ++k) {
             if (pa[k]) cudaFree(pa[k]);
@@ -285,18 +287,62 @@ __global__ void k_form_x(const MolDev* __restrict__ M, const double* __restrict_
     }
 }
 
-// per-update bookkeeping: energies, the update counter, the convergence test of the DIIS driver
-// (|dE| < eps and max |error| < tol, from the third update on)
-__global__ void k_converge(int nmol, const double* __restrict__ Enew, double* __restrict__ Eold, int* __restrict__ nupd,
-                           int* __restrict__ conv, int* __restrict__ its, const double* __restrict__ err, double eps,
-                           double tol) {
+// The reference's scf_converger (RHF.hpp:536-569): before an update from the damp_from-th on, a
+// molecule whose energy went up in the last update averages its density with the one before it.
+__global__ void k_damp(const MolDev* __restrict__ M, const int* __restrict__ conv, const int* __restrict__ nupd,
+                       const double* __restrict__ dE, int damp_from, const double* __restrict__ Pold, double* __restrict__ P) {
+    const MolDev m = M[blockIdx.x];
+    if (conv[m.bidx] || nupd[m.bidx] < damp_from || dE[m.bidx] < 0.0) return;
+    for (int t = threadIdx.x; t < m.n * (m.n + 1) / 2; t += blockDim.x) P[m.po + t] = 0.5 * (P[m.po + t] + Pold[m.po + t]);
+}
+
+// Pold = P (packed) of the active molecules, before the update replaces P (RHF.hpp:108)
+__global__ void k_save_old(const MolDev* __restrict__ M, const int* __restrict__ conv, const double* __restrict__ P,
+                           double* __restrict__ Pold) {
+    const MolDev m = M[blockIdx.x];
+    if (conv[m.bidx]) return;
+    for (int t = threadIdx.x; t < m.n * (m.n + 1) / 2; t += blockDim.x) Pold[m.po + t] = P[m.po + t];
+}
+
+// SymmPack::SymmPackDiffNorm (SymmPack.cpp:20-36): sqrt(2 (sum_{i>j} d^2 + sum_i d^2 / 2)) / N
+__global__ void k_pdiff(const MolDev* __restrict__ M, const int* __restrict__ conv, const double* __restrict__ P,
+                        const double* __restrict__ Pold, double* __restrict__ pdiff) {
+    const MolDev m = M[blockIdx.x];
+    if (conv[m.bidx]) return;
+    double sum = 0.0;
+    for (int t = threadIdx.x; t < m.n * (m.n + 1) / 2; t += blockDim.x) {
+        int i = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+        while ((long long)i * (i + 1) / 2 > t) --i;
+        while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+        const double d = P[m.po + t] - Pold[m.po + t];
+        sum += (t - (long long)i * (i + 1) / 2 == i ? 0.5 : 1.0) * d * d;
+    }
+    sum = block_sum(sum);
+    if (threadIdx.x == 0) pdiff[m.bidx] = sqrt(2.0 * sum) / m.n;
+}
+
+// per-update bookkeeping: energies, the update counter and the convergence test from the
+// first_check-th update on.  DIIS (accel 2): |dE| < eps and max |error| < tol (the single-molecule
+// driver's test); otherwise is_converged (RHF.hpp:390-402) on the signed dE and/or pdiff (cflag).
+__global__ void k_converge(int nmol, const double* __restrict__ Enew, double* __restrict__ Eold, double* __restrict__ dE,
+                           double* __restrict__ Einit, int* __restrict__ nupd, int* __restrict__ conv, int* __restrict__ its,
+                           const double* __restrict__ err, const double* __restrict__ pdiff, int accel, int cflag,
+                           int first_check, double eps, double tol) {
     const int mol = blockIdx.x * blockDim.x + threadIdx.x;
     if (mol >= nmol || conv[mol]) return;
     const double de = Enew[mol] - Eold[mol];
     Eold[mol] = Enew[mol];
+    dE[mol] = de;
     const int u = ++nupd[mol];
     its[mol] = u;
-    if (u >= 3 && fabs(de) < eps && err[mol] < tol) conv[mol] = 1;
+    if (u == 1) Einit[mol] = Enew[mol];
+    if (u < first_check) return;
+    bool ok;
+    if (accel == 2) ok = fabs(de) < eps && err[mol] < tol;
+    else if (cflag == 0) ok = de < eps;
+    else if (cflag == 1) ok = pdiff[mol] < eps;
+    else ok = pdiff[mol] < eps && de < eps;
+    if (ok) conv[mol] = 1;
 }
 
 unsigned blocks(long long n) { return (unsigned)((n + 255) / 256); }
@@ -383,14 +429,30 @@ int density_from_F(BState& st, double* dP, cudaStream_t s) {
     return UNOMOL_OK;
 }
 
+struct BOpts {
+    int accel, cflag, first_check;
+    double eps, tol;
+};
+
 // one SCF update of every active molecule (the part that is captured as a graph)
-int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, double eps, double tol, cudaStream_t s) {
+int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, const BOpts& o, cudaStream_t s) {
+    if (o.accel != 2) k_damp<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.nupd, st.dE, o.first_check - 1, st.Pold, dP);
     int rc = unomol_gpu_batch_fock(batch, UNOMOL_BATCH_LAUNCHES, s);
     if (rc) {
         st.err_msg = unomol_gpu_batch_last_error(batch);
         return rc;
     }
     k_fock<<<st.nmol, 256, 0, s>>>(st.d_mols, st.Hpk, dG, dP, st.F, st.Enew);
+    BK(cudaGetLastError(), UNOMOL_ECUDA);
+    if (o.accel != 2) {
+        k_save_old<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, dP, st.Pold);
+        if ((rc = density_from_F(st, dP, s))) return rc;
+        k_pdiff<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, dP, st.Pold, st.pdiff);
+        k_converge<<<blocks(st.nmol), 256, 0, s>>>(st.nmol, st.Enew, st.Eold, st.dE, st.Einit, st.nupd, st.conv, st.its, st.err,
+                                                   st.pdiff, o.accel, o.cflag, o.first_check, o.eps, o.tol);
+        BK(cudaGetLastError(), UNOMOL_ECUDA);
+        return UNOMOL_OK;
+    }
     k_unpack<<<st.nmol, 256, 0, s>>>(st.d_mols, dP, st.Pf);
     BK(cudaGetLastError(), UNOMOL_ECUDA);
     // DIIS error X^T (F P S - S P F) X
@@ -405,7 +467,8 @@ int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, double eps
     k_diis_extrap<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.nupd, st.maxv, st.tot2, st.coef, st.Fh, st.F);
     BK(cudaGetLastError(), UNOMOL_ECUDA);
     if ((rc = density_from_F(st, dP, s))) return rc;
-    k_converge<<<blocks(st.nmol), 256, 0, s>>>(st.nmol, st.Enew, st.Eold, st.nupd, st.conv, st.its, st.err, eps, tol);
+    k_converge<<<blocks(st.nmol), 256, 0, s>>>(st.nmol, st.Enew, st.Eold, st.dE, st.Einit, st.nupd, st.conv, st.its, st.err,
+                                               st.pdiff, o.accel, o.cflag, o.first_check, o.eps, o.tol);
     BK(cudaGetLastError(), UNOMOL_ECUDA);
     return UNOMOL_OK;
 }
@@ -421,6 +484,10 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     if (unomol_gpu_batch_buffers(batch, &dP, &dG, &poff, &ptot)) {
         st.err_msg = unomol_gpu_batch_last_error(batch);
         return fail(UNOMOL_EINVAL);
+    }
+    if (opt->guess != UNOMOL_GUESS_CORE && (opt->guess != UNOMOL_GUESS_GIVEN || !P_out)) {
+        st.err_msg = "batched SCF: the guess is the core Hamiltonian or the densities passed in P_io";
+        return UNOMOL_EINVAL;
     }
     if (unomol_gpu_batch_size(batch) != nmol) {
         st.err_msg = "batched SCF: " + std::to_string(nmol) + " inputs for a batch of " +
@@ -463,7 +530,10 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     BK(cudaMalloc(&st.Eh, b2 * st.maxv), UNOMOL_ENOMEM);
     BK(cudaMalloc(&st.B, sizeof(double) * nmol * st.maxv * st.maxv), UNOMOL_ENOMEM);
     BK(cudaMalloc(&st.coef, sizeof(double) * nmol * st.maxv), UNOMOL_ENOMEM);
-    for (double** p : {&st.Enew, &st.Eold, &st.err}) BK(cudaMalloc(p, sizeof(double) * nmol), UNOMOL_ENOMEM);
+    for (double** p : {&st.Enew, &st.Eold, &st.err, &st.dE, &st.pdiff, &st.Einit}) BK(cudaMalloc(p, sizeof(double) * nmol), UNOMOL_ENOMEM);
+    BK(cudaMalloc(&st.Pold, sizeof(double) * ptot), UNOMOL_ENOMEM);
+    BK(cudaMemset(st.dE, 0, sizeof(double) * nmol), UNOMOL_ECUDA);
+    BK(cudaMemset(st.pdiff, 0, sizeof(double) * nmol), UNOMOL_ECUDA);
     for (int** p : {&st.nupd, &st.conv, &st.its, &st.info, &st.bad}) BK(cudaMalloc(p, sizeof(int) * nmol), UNOMOL_ENOMEM);
     for (int** p : {&st.nupd, &st.conv, &st.its, &st.info, &st.bad}) BK(cudaMemset(*p, 0, sizeof(int) * nmol), UNOMOL_ECUDA);
     BK(cudaMemset(st.Eold, 0, sizeof(double) * nmol), UNOMOL_ECUDA);
@@ -527,9 +597,14 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     BK(cudaMemcpyAsync(st.X, st.S, b2, cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
     if ((rc = eig(st, st.X, s))) return fail(rc);
     k_form_x<<<nmol, 256, 0, s>>>(st.d_mols, st.W, st.X, st.bad);
-    // core-Hamiltonian guess (RHF.hpp:205-211): F = H
-    BK(cudaMemcpyAsync(st.F, st.H, b2, cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
-    if ((rc = density_from_F(st, dP, s))) return fail(rc);
+    if (opt->guess == UNOMOL_GUESS_GIVEN) {
+        // the caller's densities (PMATRIX.DAT form, batch order; RHF.hpp:120-123, 318)
+        BK(cudaMemcpyAsync(dP, P_out, sizeof(double) * ptot, cudaMemcpyHostToDevice, s), UNOMOL_ECUDA);
+    } else {
+        // core-Hamiltonian guess (RHF.hpp:205-211): F = H
+        BK(cudaMemcpyAsync(st.F, st.H, b2, cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
+        if ((rc = density_from_F(st, dP, s))) return fail(rc);
+    }
     BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
     {
         std::vector<int> bad(nmol), info(nmol);
@@ -547,14 +622,15 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         }
     }
     const int maxits = opt->maxits > 0 ? opt->maxits : 300;
-    const double eps = opt->eps, tol = opt->diis_tol;
+    const BOpts o{opt->accel == UNOMOL_SCF_DIIS ? 2 : 0, opt->conv_type, opt->loop == UNOMOL_SCF_LOOP_DPM ? 2 : 3, opt->eps,
+                  opt->diis_tol};
     cudaGraphExec_t exec = nullptr;
     int used_graph = 0;
     if (graph) {
         // capture one iteration; a library call that cannot be captured leaves plain launches
         cudaGraph_t gr = nullptr;
         BK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), UNOMOL_ECUDA);
-        rc = iteration(st, batch, dP, dG, eps, tol, s);
+        rc = iteration(st, batch, dP, dG, o, s);
         const cudaError_t e = cudaStreamEndCapture(s, &gr);
         if (!rc && e == cudaSuccess && gr && cudaGraphInstantiate(&exec, gr, 0) == cudaSuccess) used_graph = 1;
         if (gr) cudaGraphDestroy(gr);
@@ -571,7 +647,7 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     int it = 0;
     for (; it < maxits; ++it) {
         if (used_graph) BK(cudaGraphLaunch(exec, s), UNOMOL_ECUDA);
-        else if ((rc = iteration(st, batch, dP, dG, eps, tol, s))) return fail(rc);
+        else if ((rc = iteration(st, batch, dP, dG, o, s))) return fail(rc);
         BK(cudaMemcpyAsync(conv.data(), st.conv, sizeof(int) * nmol, cudaMemcpyDeviceToHost, s), UNOMOL_ECUDA);
         BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
         if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; })) {
@@ -580,7 +656,10 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         }
     }
     if (exec) cudaGraphExecDestroy(exec);
-    std::vector<double> E(nmol), err(nmol);
+    std::vector<double> E(nmol), err(nmol), E1(nmol), pd(nmol), de(nmol);
+    BK(cudaMemcpy(E1.data(), st.Einit, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
+    BK(cudaMemcpy(pd.data(), st.pdiff, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
+    BK(cudaMemcpy(de.data(), st.dE, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
     std::vector<int> its(nmol), info(nmol);
     BK(cudaMemcpy(E.data(), st.Eold, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
     BK(cudaMemcpy(err.data(), st.err, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
@@ -598,6 +677,9 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         res[m].iterations = its[m];
         res[m].converged = conv[m];
         res[m].diis_error = err[m];
+        res[m].init_energy = E1[m] + in[m].nucrep;
+        res[m].ediff = de[m];
+        res[m].pdiff = pd[m];
     }
     if (P_out) BK(cudaMemcpy(P_out, dP, sizeof(double) * ptot, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
     (void)it;

@@ -16,6 +16,11 @@
         and one 8192^3 square, device time by CUDA events (mean of reps after a warm-up), TFLOP/s against
         the measured BF16 peak of MEASURED_PEAKS.json, with cuBLAS (torch.matmul) beside it.
 
+    python -m unomol_gb300.measure dpm [--points 64] [--out dpm.json]
+        DPM polarisation potential of water/6-31G with a 2s1p positron basis on 64 positron positions:
+        the grid point after point (one context recalculated per point) against all points as one
+        batched SCF whose iterations replay as a CUDA graph.
+
     python -m unomol_gb300.measure sweep [--out sweep.json]
         FP32 cutoff sweep of the precision form on the 32-water 6-31G cluster (molecules.water_cluster(32, 0),
         superposition-of-fragments guess, DIIS, 1e-10 Eh): the incremental mixed-precision SCF against the
@@ -185,13 +190,46 @@ def _gemm(reps: int) -> dict:
     return out
 
 
+def _dpm(npts: int) -> dict:
+    """DPM polarisation potential of water/6-31G with the two-s-one-p positron basis on `npts` positron
+    positions (radii 3, 4, 5, 6 bohr, directions from a Fibonacci sphere): the points one after the
+    other against all points as one batched SCF (CUDA-graph iterations), with their differences."""
+    import time
+    from . import dpm
+    b = Basis(text=molecules.patin_text(molecules.water(), "6-31G", int_flags=(1, 0), scf_flags=(2, 1, 0)))
+    posin = molecules.posin_text()
+    ndir = max(1, npts // 4)
+    k = np.arange(ndir) + 0.5
+    th, ph = np.arccos(1 - 2 * k / ndir), np.pi * (1 + 5 ** 0.5) * k
+    dirs = np.stack([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)], 1)
+    pts = np.concatenate([r * dirs for r in (3.0, 4.0, 5.0, 6.0)])[:npts]
+    gs = dpm.ground_state(b)
+    dpm.polarization_potential(b, posin, pts[:1], gs=gs)  # warm-up
+    t0 = time.perf_counter()
+    seq = dpm.polarization_potential(b, posin, pts, gs=gs)
+    t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bat, info = dpm.polarization_potential_batched(b, posin, pts, gs=gs)
+    t_bat = time.perf_counter() - t0
+    dv = max(abs(x["vpol"] - y["vpol"]) for x, y in zip(seq, bat))
+    return {"workload": f"water/6-31G + positron basis (2s1p), {len(pts)} positions", "points": len(pts),
+            "one_at_a_time_s": t_seq, "batched_s": t_bat, "batched_parts": info, "speedup": t_seq / t_bat,
+            "max_abs_dvpol_batched_vs_sequential": dv,
+            "iterations_one_at_a_time": [int(x["iterations"]) for x in seq],
+            "iterations_batched_max": max(int(x["iterations"]) for x in bat),
+            "converged": [bool(x["converged"]) for x in bat],
+            "vpol_range": [float(min(x["vpol"] for x in seq)), float(max(x["vpol"] for x in seq))]}
+
+
 def main():
-    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM measurements")
-    ap.add_argument("what", choices=["batch", "sweep", "gemm"])
+    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM / DPM measurements")
+    ap.add_argument("what", choices=["batch", "sweep", "gemm", "dpm"])
+    ap.add_argument("--points", type=int, default=64)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
-    rep = _batch(a.reps) if a.what == "batch" else _sweep() if a.what == "sweep" else _gemm(max(a.reps, 10))
+    rep = (_batch(a.reps) if a.what == "batch" else _sweep() if a.what == "sweep" else
+           _gemm(max(a.reps, 10)) if a.what == "gemm" else _dpm(a.points))
     print(json.dumps(rep, indent=1))
     if a.out:
         with open(a.out, "w") as f:

@@ -257,7 +257,8 @@ class ScfResult(C.Structure):
 
 class BatchScfResult(C.Structure):
     _fields_ = [("energy", C.c_double), ("e_electronic", C.c_double), ("diis_error", C.c_double),
-                ("iterations", C.c_int), ("converged", C.c_int)]
+                ("iterations", C.c_int), ("converged", C.c_int), ("init_energy", C.c_double),
+                ("ediff", C.c_double), ("pdiff", C.c_double)]
 
 
 SCF_DAMPED = 0
@@ -425,11 +426,13 @@ class Batch:
         return [tuple(int(x) for x in chosen[3 * k:3 * k + 3]) for k in range(n)]
 
     def scf(self, S=None, H=None, eps: float = 1e-10, diis_tol: float = 1e-6, maxits: int = 200,
-            diis_size: int = 8, graph: bool = True):
+            diis_size: int = 8, graph: bool = True, accel: int = SCF_DIIS, conv_type: int = 0, guess_P=None,
+            loop: int = SCF_LOOP_GROUND):
         """RHF SCF of every molecule at once (unomol_gpu_batch_scf).  S, H: lists of packed matrices
-        (default: the GPU one-electron integrals of each basis).  Returns a dict with per-molecule
-        energies, iterations and convergence, the packed densities, the wall time and whether the
-        iteration ran as a CUDA graph."""
+        (default: the GPU one-electron integrals of each basis); guess_P: list of packed starting
+        densities (default: core Hamiltonian); accel / conv_type / loop as for scf().  Returns a dict
+        with per-molecule energies, iterations and convergence, the packed densities, the wall time
+        and whether the iteration ran as a CUDA graph."""
         L = lib()
         L.unomol_gpu_batch_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.c_int, C.POINTER(ScfOptions), C.c_int,
                                            C.POINTER(BatchScfResult), _dp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
@@ -443,15 +446,20 @@ class Batch:
         dp = C.POINTER(C.c_double)
         inp = (ScfInput * n)(*[ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), s.ctypes.data_as(dp), h.ctypes.data_as(dp))
                                for b, s, h in zip(self.bases, S, H)])
-        opt = ScfOptions(maxits, eps, 0, SCF_DIIS, GUESS_CORE, diis_size, diis_tol, 0.0, 0.0, 0.0, 0, 8, 0)
+        opt = ScfOptions(maxits, eps, conv_type, accel, GUESS_CORE if guess_P is None else GUESS_GIVEN, diis_size,
+                         diis_tol, 0.0, 0.0, 0.0, 0, 8, loop)
         res = (BatchScfResult * n)()
         P = np.zeros(self.total)
+        if guess_P is not None:
+            P[:] = np.concatenate([np.asarray(x, np.float64) for x in guess_P])
         sec, used = C.c_double(), C.c_int()
         rc = L.unomol_gpu_batch_scf(self._h, inp, n, C.byref(opt), 1 if graph else 0, res, P, C.byref(sec), C.byref(used))
         note = L.unomol_gpu_batch_scf_last_error().decode(errors="replace")
         if rc != 0:
             raise UnomolError(f"unomol_gpu_batch_scf error {rc}: {note}")
         return {"energy": np.array([r.energy for r in res]), "iterations": np.array([r.iterations for r in res]),
+                "init_energy": np.array([r.init_energy for r in res]), "ediff": np.array([r.ediff for r in res]),
+                "pdiff": np.array([r.pdiff for r in res]),
                 "converged": np.array([bool(r.converged) for r in res]),
                 "diis_error": np.array([r.diis_error for r in res]),
                 "P": [P[o:o + b.no2].copy() for o, b in zip(self.offsets, self.bases)],
