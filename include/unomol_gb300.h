@@ -210,6 +210,10 @@ int unomol_gpu_one_electron(const UnomolBasisDesc* basis, const double* charges,
                             double* S, double* T, double* H);
 const char* unomol_gpu_one_electron_last_error(void);
 
+/* Dipole and quadrupole integrals about the origin (the data MomentInts writes to RMOM.DAT,
+ * Moments.cpp:98-181): M[k][no2] packed, k = dx, dy, dz, qxx, qxy, qxz, qyy, qyz, qzz, unweighted. */
+int unomol_gpu_moment_ints(const UnomolBasisDesc* basis, double* M);
+
 typedef struct UnomolScfInput {
     int norb;            /* basis functions */
     int nelec;           /* electrons: even -> RHF, odd -> UHF (Unomol.cc:13-24) */

@@ -20,7 +20,7 @@ def golden_cases(pattern="*.npz", exclude_md=True):
         name = os.path.basename(p)[:-4]
         if exclude_md and name.endswith("_md"):
             continue
-        if name.startswith("dpm_"):  # DPM grids: their own tests (test_dpm.py)
+        if name.startswith(("dpm_", "prop_")):  # DPM grids, moments / finite field: their own tests
             continue
         out.append(name)
     return out

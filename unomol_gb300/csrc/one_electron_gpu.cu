@@ -230,6 +230,70 @@ __global__ void __launch_bounds__(128) k_one_electron(const OneArgs a) {
     a.H[o] = (tv + vv) * nrm;
 }
 
+// Dipole and quadrupole integrals about the origin (the data of MomentInts, Moments.cpp:5-181; the
+// reference expands them with McMurchie-Davidson D functions, here with the same Obara-Saika tables,
+// x = (x - A_x) + A_x):  <a|x|b> = S(a+1, b) + A_x S(a, b),  <a|x^2|b> = S(a+2, b) + 2 A_x S(a+1, b) + A_x^2 S(a, b).
+// Output M[k][packed] for k = dx, dy, dz, qxx, qxy, qxz, qyy, qyz, qzz (RMOM.DAT order, unweighted).
+template <int LM>
+__global__ void __launch_bounds__(128) k_moments(const OneArgs a, double* __restrict__ M) {
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= a.nitems) return;
+    const OneItem w = a.items[it];
+    const double* cen = a.centers;
+    const int la = a.sl[w.sa], lb = a.sl[w.sb];
+    int lx[2][3];
+    cart_of(la, w.ca, lx[0][0], lx[0][1], lx[0][2]);
+    cart_of(lb, w.cb, lx[1][0], lx[1][1], lx[1][2]);
+    const double* A = cen + 3 * a.sc[w.sa];
+    const double* B = cen + 3 * a.sc[w.sb];
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int ia = 0; ia < a.snp[w.sa]; ++ia)
+        for (int ib = 0; ib < a.snp[w.sb]; ++ib) {
+            const double al = a.alpha[a.sp0[w.sa] + ia], be = a.alpha[a.sp0[w.sb] + ib];
+            const double cab = a.coef[a.sp0[w.sa] + ia] * a.coef[a.sp0[w.sb] + ib];
+            const double p = al + be, mu = al * be / p, o2p = 0.5 / p;
+            const double rp = sqrt(3.14159265358979323846 / p);
+            double m0[3], m1[3], m2[3];  // per axis: <a|1|b>, <a|x|b>, <a|x^2|b>
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double Pk = (al * A[k] + be * B[k]) / p;
+                double t[LM + 3][LM + 2];
+                const int i0 = lx[0][k], j0 = lx[1][k];
+                t[0][0] = rp * exp(-mu * (A[k] - B[k]) * (A[k] - B[k]));
+                for (int i = 0; i <= i0 + 2; ++i)
+                    for (int j = 0; j <= j0; ++j) {
+                        if (i == 0 && j == 0) continue;
+                        double v;
+                        if (i > 0) {
+                            v = (Pk - A[k]) * t[i - 1][j];
+                            if (i > 1) v += (i - 1) * t[i - 2][j] * o2p;
+                            if (j > 0) v += j * t[i - 1][j - 1] * o2p;
+                        } else {
+                            v = (Pk - B[k]) * t[i][j - 1];
+                            if (j > 1) v += (j - 1) * t[i][j - 2] * o2p;
+                        }
+                        t[i][j] = v;
+                    }
+                m0[k] = t[i0][j0];
+                m1[k] = t[i0 + 1][j0] + A[k] * t[i0][j0];
+                m2[k] = t[i0 + 2][j0] + 2.0 * A[k] * t[i0 + 1][j0] + A[k] * A[k] * t[i0][j0];
+            }
+            acc[0] += cab * m1[0] * m0[1] * m0[2];
+            acc[1] += cab * m0[0] * m1[1] * m0[2];
+            acc[2] += cab * m0[0] * m0[1] * m1[2];
+            acc[3] += cab * m2[0] * m0[1] * m0[2];
+            acc[4] += cab * m1[0] * m1[1] * m0[2];
+            acc[5] += cab * m1[0] * m0[1] * m1[2];
+            acc[6] += cab * m0[0] * m2[1] * m0[2];
+            acc[7] += cab * m0[0] * m1[1] * m1[2];
+            acc[8] += cab * m0[0] * m0[1] * m2[2];
+        }
+    const double nrm = 1.0 / sqrt(dfact_ref(lx[0][0]) * dfact_ref(lx[0][1]) * dfact_ref(lx[0][2]) * dfact_ref(lx[1][0]) *
+                                  dfact_ref(lx[1][1]) * dfact_ref(lx[1][2]));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) M[k * a.no2 + a.kpk[it]] = acc[k] * nrm;
+}
+
 thread_local std::string g_one_err;
 
 template <class T>
@@ -241,11 +305,9 @@ struct Dv {
     cudaError_t alloc(size_t n) { return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)); }
 };
 
-}  // namespace
-
-extern "C" int unomol_gpu_one_electron(const UnomolBasisDesc* b, const double* charges, int ngeom, const double* centers,
-                                       double* S, double* T, double* H) {
-    if (!b || !charges || !S || !H || ngeom <= 0 || (!centers && ngeom != 1)) return UNOMOL_EINVAL;
+// host part of both entry points: M != NULL computes the moment integrals (one geometry) instead of S, T, H
+int one_electron_impl(const UnomolBasisDesc* b, const double* charges, int ngeom, const double* centers, double* S,
+                      double* T, double* H, double* M) {
     const int ns = b->nshell, nc = b->ncen, n = b->norb;
     int lmax = 0, np = 0;
     std::vector<int> p0(ns);
@@ -296,8 +358,9 @@ extern "C" int unomol_gpu_one_electron(const UnomolBasisDesc* b, const double* c
     ck(d_sl.alloc(ns)), ck(d_snp.alloc(ns)), ck(d_sc.alloc(ns)), ck(d_sp0.alloc(ns));
     ck(d_alpha.alloc(np)), ck(d_coef.alloc(np));
     ck(d_cen.alloc((size_t)ngeom * nc * 3)), ck(d_chg.alloc(nc));
-    ck(d_S.alloc(out)), ck(d_H.alloc(out));
-    if (T) ck(d_T.alloc(out));
+    if (M) ck(d_S.alloc((size_t)9 * no2));
+    else ck(d_S.alloc(out)), ck(d_H.alloc(out));
+    if (T && !M) ck(d_T.alloc(out));
     if (e != cudaSuccess) {
         g_one_err = std::string("one-electron: ") + cudaGetErrorString(e);
         return UNOMOL_ENOMEM;
@@ -311,26 +374,45 @@ extern "C" int unomol_gpu_one_electron(const UnomolBasisDesc* b, const double* c
     ck(cudaMemcpy(d_alpha.p, b->alpha, np * sizeof(double), cudaMemcpyHostToDevice));
     ck(cudaMemcpy(d_coef.p, b->coef, np * sizeof(double), cudaMemcpyHostToDevice));
     ck(cudaMemcpy(d_cen.p, centers ? centers : b->centers, (size_t)ngeom * nc * 3 * sizeof(double), cudaMemcpyHostToDevice));
-    ck(cudaMemcpy(d_chg.p, charges, nc * sizeof(double), cudaMemcpyHostToDevice));
+    if (charges) ck(cudaMemcpy(d_chg.p, charges, nc * sizeof(double), cudaMemcpyHostToDevice));
     OneArgs a{};
     a.items = d_items.p, a.nitems = (int)items.size(), a.sl = d_sl.p, a.snp = d_snp.p, a.sc = d_sc.p, a.sp0 = d_sp0.p;
     a.kpk = d_kpk.p, a.alpha = d_alpha.p, a.coef = d_coef.p, a.centers = d_cen.p, a.charges = d_chg.p, a.ncen = nc;
     a.no2 = no2, a.S = d_S.p, a.T = T ? d_T.p : nullptr, a.H = d_H.p;
     const dim3 grid((unsigned)((items.size() + 127) / 128), (unsigned)ngeom);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && M) {
+        if (lmax <= 1) k_moments<1><<<grid, 128>>>(a, d_S.p);
+        else if (lmax == 2) k_moments<2><<<grid, 128>>>(a, d_S.p);
+        else k_moments<4><<<grid, 128>>>(a, d_S.p);
+        ck(cudaGetLastError());
+        ck(cudaMemcpy(M, d_S.p, (size_t)9 * no2 * sizeof(double), cudaMemcpyDeviceToHost));
+    } else if (e == cudaSuccess) {
         if (lmax <= 1) k_one_electron<1><<<grid, 128>>>(a);
         else if (lmax == 2) k_one_electron<2><<<grid, 128>>>(a);
         else k_one_electron<4><<<grid, 128>>>(a);
         ck(cudaGetLastError());
+        ck(cudaMemcpy(S, d_S.p, out * sizeof(double), cudaMemcpyDeviceToHost));
+        ck(cudaMemcpy(H, d_H.p, out * sizeof(double), cudaMemcpyDeviceToHost));
+        if (T) ck(cudaMemcpy(T, d_T.p, out * sizeof(double), cudaMemcpyDeviceToHost));
     }
-    ck(cudaMemcpy(S, d_S.p, out * sizeof(double), cudaMemcpyDeviceToHost));
-    ck(cudaMemcpy(H, d_H.p, out * sizeof(double), cudaMemcpyDeviceToHost));
-    if (T) ck(cudaMemcpy(T, d_T.p, out * sizeof(double), cudaMemcpyDeviceToHost));
     if (e != cudaSuccess) {
         g_one_err = std::string("one-electron: ") + cudaGetErrorString(e);
         return UNOMOL_ECUDA;
     }
     return UNOMOL_OK;
+}
+
+}  // namespace
+
+extern "C" int unomol_gpu_one_electron(const UnomolBasisDesc* b, const double* charges, int ngeom, const double* centers,
+                                       double* S, double* T, double* H) {
+    if (!b || !charges || !S || !H || ngeom <= 0 || (!centers && ngeom != 1)) return UNOMOL_EINVAL;
+    return one_electron_impl(b, charges, ngeom, centers, S, T, H, nullptr);
+}
+
+extern "C" int unomol_gpu_moment_ints(const UnomolBasisDesc* b, double* M) {
+    if (!b || !M) return UNOMOL_EINVAL;
+    return one_electron_impl(b, nullptr, 1, nullptr, nullptr, nullptr, nullptr, M);
 }
 
 extern "C" const char* unomol_gpu_one_electron_last_error(void) { return g_one_err.c_str(); }

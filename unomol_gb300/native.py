@@ -34,6 +34,7 @@ EXPORTS = [
     "unomol_guess_get_params", "unomol_guess_set_params", "unomol_guess_destroy", "unomol_guess_last_error",
     "unomol_gpu_one_electron", "unomol_gpu_one_electron_last_error", "unomol_gpu_l2_peak", "unomol_gpu_batch_scf",
     "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
+    "unomol_gpu_moment_ints",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -310,6 +311,19 @@ def one_electron_gpu(b: Basis, centers=None, with_t: bool = False):
         S, H = S[0], H[0]
         T = T[0] if with_t else None
     return (S, T, H) if with_t else (S, H)
+
+
+def moment_ints(b: Basis) -> np.ndarray:
+    """[9, no2]: dx, dy, dz, qxx, qxy, qxz, qyy, qyz, qzz integrals (unomol_gpu_moment_ints)."""
+    L = lib()
+    L.unomol_gpu_moment_ints.argtypes = [C.POINTER(BasisDesc), C.c_void_p]
+    L.unomol_gpu_one_electron_last_error.restype = C.c_char_p
+    d, keep = basis_desc(b)
+    M = np.zeros((9, b.no2))
+    rc = L.unomol_gpu_moment_ints(C.byref(d), M.ctypes.data)
+    if rc != 0:
+        raise UnomolError(f"unomol_gpu_moment_ints error {rc}: {L.unomol_gpu_one_electron_last_error().decode()}")
+    return M
 
 
 def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPED, guess_P=None,
