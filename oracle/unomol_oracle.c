@@ -94,8 +94,9 @@ static void roots_weights(int n, double T, int compat, double* x, double* w) {
         return;
     }
     if (T < tmax_tab[n - 1]) {
-        int k = (int)T;
-        double y = 2.0 * (T - k) - 1.0;
+        const double Ts = T * (1.0 / RYS_H);
+        int k = (int)Ts;
+        double y = 2.0 * (Ts - k) - 1.0;
         const double* c = RYS_TABLE_H + RYS_OFF_H[n - 1] + k * (2 * n * (RYS_DEG + 1));
         for (int i = 0; i < n; ++i) {
             const double* cx = c + 2 * i * (RYS_DEG + 1);

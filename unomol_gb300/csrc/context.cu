@@ -169,11 +169,12 @@ void build_pair(UnomolCtx* ctx, int ish, int jsh, ShellPair& sp, std::vector<Pri
 
 // Algorithmic flops of the Rys kernels (FMA = 2, every +,-,*,/,sqrt = 1), counted from the steps of
 // fock_kernels.cuh.  Per primitive quartet past the prefactor cut: setup 20; Rys nodes and weights
-// NR * (2 polynomials * 13 Horner steps * 2) + 3; per root 10 for B00, B1, B1', then per axis 4 for
-// C, C', the 2D recurrence, the two horizontal transfers (2 per step), and 3 per function quartet for
-// the product and accumulation.  Per shell quartet: 17 per function quartet for normalisation and the
-// six density contractions.
-double flops_per_prim(int la, int lb, int lc, int ld) {
+// NR * (2 polynomials * deg Horner steps * 2) + 3, deg = the table degree of the precision (RYS_DEG
+// for FP64, RYS32_DEG for FP32); per root 10 for B00, B1, B1', then per axis 4 for C, C', the 2D
+// recurrence, the two horizontal transfers (2 per step), and 3 per function quartet for the product
+// and accumulation.  Per shell quartet: 17 per function quartet for normalisation and the six density
+// contractions.
+double flops_per_prim(int la, int lb, int lc, int ld, bool fp32 = false) {
     const int L12 = la + lb, L34 = lc + ld, NR = (L12 + L34) / 2 + 1;
     const int NF = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
     double vrr = 0;
@@ -184,7 +185,8 @@ double flops_per_prim(int la, int lb, int lc, int ld) {
     double hrr = 0;
     for (int b = 1; b <= lb; ++b) hrr += 2.0 * (L12 - b + 1) * (L34 + 1);
     for (int d = 1; d <= ld; ++d) hrr += 2.0 * (la + 1) * (lb + 1) * (L34 - d + 1);
-    return 20 + NR * 52.0 + 3 + NR * (10 + 3 * (4 + vrr + hrr) + 3.0 * NF);
+    const double roots = 2.0 * (fp32 ? RYS32_DEG : RYS_DEG) * 2.0;
+    return 20 + NR * roots + 3 + NR * (10 + 3 * (4 + vrr + hrr) + 3.0 * NF);
 }
 double flops_per_quartet(int la, int lb, int lc, int ld) {
     return 17.0 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
@@ -692,7 +694,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                 unsigned long long n = 0;
                 for (int k = 0; k < 32; ++k) n += c[(half * ncls + cls) * 32 + k];
                 prims += (int64_t)n;
-                const double f = (double)n * flops_per_prim(la, lb, lc, ld);
+                const double f = (double)n * flops_per_prim(la, lb, lc, ld, half != 0);
                 if (half) fl32 += f; else fl += f;
             }
             // quartet-level work: all quartets of the class (both halves together in mixed mode)

@@ -72,8 +72,9 @@ __device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, 
         }
     }
     if (T < TMAX) {
-        int k = (int)T;  // interval width RYS_H == 1
-        R y = R(2) * (T - R(k)) - R(1);
+        const R Ts = T * R(1.0 / RYS_H);  // intervals of width RYS_H (a power of two: exact)
+        const int k = (int)Ts;
+        const R y = R(2) * (Ts - R(k)) - R(1);
         const R* c = tab + rys_off(NR, DEG) + k * (2 * NR * (DEG + 1));
 #pragma unroll
         for (int i = 0; i < NR; ++i) {

@@ -28,7 +28,7 @@ Output arrays (C source included by the CUDA kernels):
   first), rys_hermite_x[n][i], rys_hermite_w[n][i].
 A float copy with lower degree (RYS32_DEG) serves the FP32 kernels.
 
-Run: python gen_rys_tables.py  (about two minutes; writes rys_tables.inc next to this file)
+Run: python gen_rys_tables.py  (a few minutes; writes rys_tables.inc next to this file)
 """
 from __future__ import annotations
 
@@ -40,9 +40,9 @@ import numpy as np
 
 mp.mp.dps = 60
 NMAX = 5
-H = 1.0          # interval width in T
-DEG = 13         # FP64 Horner degree (14 coefficients)
-DEG32 = 7        # FP32 Horner degree
+H = 0.5          # interval width in T
+DEG = 9          # FP64 Horner degree (10 coefficients; 3e-16 relative at H = 0.5, like 13 at H = 1)
+DEG32 = 5        # FP32 Horner degree (1.1e-7 relative at H = 0.5)
 NCHEB = 24       # interpolation nodes per interval for the fit
 
 
