@@ -803,19 +803,25 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
     for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
     // Rys tables (polynomial blocks, then the large-T limit)
     {
-        std::vector<double> t64(rys_table_len(RYS_DEG));
-        std::memcpy(t64.data(), RYS_TABLE_H, sizeof(double) * RYS_TABLE_SIZE);
-        std::vector<float> t32(rys_table_len(RYS32_DEG));
-        std::memcpy(t32.data(), RYS32_TABLE_H, sizeof(float) * RYS32_TABLE_SIZE);
+        // rows re-laid with the padded strides of the device (16-byte loads), zeros in the padding
+        constexpr int S64 = RysStride<double>::value, S32 = RysStride<float>::value;
+        static_assert(rys_table_len(RYS_DEG + 1) == RYS_TABLE_SIZE + 50, "layout of rys_tables.inc");
+        static_assert(rys_table_len(RYS32_DEG + 1) == RYS32_TABLE_SIZE + 50, "layout of rys_tables.inc");
+        std::vector<double> t64(rys_table_len(S64), 0.0);
+        std::vector<float> t32(rys_table_len(S32), 0.f);
+        const int rows = RYS_TABLE_SIZE / (RYS_DEG + 1);
+        for (int r = 0; r < rows; ++r) {
+            for (int d = 0; d <= RYS_DEG; ++d) t64[(size_t)r * S64 + d] = RYS_TABLE_H[(size_t)r * (RYS_DEG + 1) + d];
+            for (int d = 0; d <= RYS32_DEG; ++d) t32[(size_t)r * S32 + d] = RYS32_TABLE_H[(size_t)r * (RYS32_DEG + 1) + d];
+        }
+        const size_t h64 = t64.size() - 50, h32 = t32.size() - 50;
         for (int n = 0; n < 5; ++n)
             for (int i = 0; i < 5; ++i) {
-                t64[RYS_TABLE_SIZE + n * 5 + i] = RYS_HERMITE_X_H[n][i];
-                t64[RYS_TABLE_SIZE + 25 + n * 5 + i] = RYS_HERMITE_W_H[n][i];
-                t32[RYS32_TABLE_SIZE + n * 5 + i] = (float)RYS_HERMITE_X_H[n][i];
-                t32[RYS32_TABLE_SIZE + 25 + n * 5 + i] = (float)RYS_HERMITE_W_H[n][i];
+                t64[h64 + n * 5 + i] = RYS_HERMITE_X_H[n][i];
+                t64[h64 + 25 + n * 5 + i] = RYS_HERMITE_W_H[n][i];
+                t32[h32 + n * 5 + i] = (float)RYS_HERMITE_X_H[n][i];
+                t32[h32 + 25 + n * 5 + i] = (float)RYS_HERMITE_W_H[n][i];
             }
-        static_assert(rys_table_len(RYS_DEG) == RYS_TABLE_SIZE + 50, "table layout");
-        static_assert(rys_table_len(RYS32_DEG) == RYS32_TABLE_SIZE + 50, "table layout");
         CU(cudaMalloc(&ctx->d_rys, sizeof(double) * t64.size()));
         CU(cudaMalloc(&ctx->d_rys32, sizeof(float) * t32.size()));
         CU(cudaMemcpy(ctx->d_rys, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice));

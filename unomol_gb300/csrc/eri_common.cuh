@@ -30,7 +30,7 @@ __host__ __device__ constexpr int cart_lz(int l, int c) { return l - cart_lx(l, 
 
 // One primitive pair of a shell pair (a has the larger L after the swap of
 // TwoElectronInts.cpp:563-579).  72 bytes; the kernels read it through the read-only path.
-struct PrimPair {
+struct __align__(16) PrimPair {
     double p;          // alpha_a + alpha_b
     double rp;         // 1 / p
     double P[3];       // Gaussian product centre
@@ -38,10 +38,12 @@ struct PrimPair {
     double E;          // exp(-alpha_a alpha_b |AB|^2 / p) / p, coefficient free (prefactor screen)
     double cc;         // c_a c_b, times 2 for the i != j half of a same-shell pair
                        // (TwoElectronInts.cpp:444-449)
+    double pad_;       // 80 bytes: five 16-byte loads
 };
 
-struct PrimPair32 {
+struct __align__(16) PrimPair32 {
     float p, rp, P[3], PA[3], E, cc;
+    float pad_[2];  // 48 bytes: three 16-byte loads
 };
 
 // One shell pair, sorted into blocks of equal (class, primitive-pair count), within a block by

@@ -18,18 +18,44 @@ namespace ugb {
 template <typename R> struct RysDeg;
 template <> struct RysDeg<double> { static constexpr int value = RYS_DEG; };
 template <> struct RysDeg<float> { static constexpr int value = RYS32_DEG; };
+// Row length of one polynomial in the device tables: the coefficients padded to a multiple of 16
+// bytes, so that a row is read with 16-byte loads (FP64: 10 doubles; FP32: 6 floats padded to 8).
+template <typename R> struct RysStride;
+template <> struct RysStride<double> { static constexpr int value = (RYS_DEG + 2) / 2 * 2; };
+template <> struct RysStride<float> { static constexpr int value = (RYS32_DEG + 4) / 4 * 4; };
 
 __host__ __device__ constexpr double rys_tmax(int n) {
     return n == 1 ? RYS_TMAX_1 : n == 2 ? RYS_TMAX_2 : n == 3 ? RYS_TMAX_3 : n == 4 ? RYS_TMAX_4 : RYS_TMAX_5;
 }
-// Offset of the n-root block in a table of polynomials of degree deg (layout of rys_tables.inc).
-__host__ __device__ constexpr int rys_off(int n, int deg) {
+// Offset of the n-root block in a table whose polynomial rows hold `stride` coefficients (rys_tables.inc
+// with stride = degree + 1; the device tables with the padded strides of RysStride).
+__host__ __device__ constexpr int rys_off(int n, int stride) {
     int o = 0;
-    for (int m = 1; m < n; ++m) o += int(rys_tmax(m) / RYS_H) * 2 * m * (deg + 1);
+    for (int m = 1; m < n; ++m) o += int(rys_tmax(m) / RYS_H) * 2 * m * stride;
     return o;
 }
 // Size of a device table: polynomial blocks, then hermite x[5][5] and w[5][5].
-__host__ __device__ constexpr int rys_table_len(int deg) { return rys_off(RYS_NMAX + 1, deg) + 50; }
+__host__ __device__ constexpr int rys_table_len(int stride) { return rys_off(RYS_NMAX + 1, stride) + 50; }
+
+// one polynomial row (16-byte aligned) into registers with 16-byte loads
+__device__ __forceinline__ void load_row(const double* __restrict__ c, double (&v)[RysStride<double>::value]) {
+#pragma unroll
+    for (int q = 0; q < RysStride<double>::value / 2; ++q) {
+        const double2 t = __ldg(reinterpret_cast<const double2*>(c) + q);
+        v[2 * q] = t.x;
+        v[2 * q + 1] = t.y;
+    }
+}
+__device__ __forceinline__ void load_row(const float* __restrict__ c, float (&v)[RysStride<float>::value]) {
+#pragma unroll
+    for (int q = 0; q < RysStride<float>::value / 4; ++q) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(c) + q);
+        v[4 * q] = t.x;
+        v[4 * q + 1] = t.y;
+        v[4 * q + 2] = t.z;
+        v[4 * q + 3] = t.w;
+    }
+}
 
 // |v| > cut (cut >= 0) compared as IEEE bit patterns: integer pipe, no FP64 compare
 __device__ __forceinline__ bool above_cut(double v, double cut) {
@@ -75,22 +101,24 @@ __device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, 
         const R Ts = T * R(1.0 / RYS_H);  // intervals of width RYS_H (a power of two: exact)
         const int k = (int)Ts;
         const R y = R(2) * (Ts - R(k)) - R(1);
-        const R* c = tab + rys_off(NR, DEG) + k * (2 * NR * (DEG + 1));
+        constexpr int ST = RysStride<R>::value;
+        const R* c = tab + rys_off(NR, ST) + k * (2 * NR * ST);
 #pragma unroll
         for (int i = 0; i < NR; ++i) {
-            const R* cx = c + (2 * i) * (DEG + 1);
-            const R* cw = cx + (DEG + 1);
-            R vx = __ldg(cx), vw = __ldg(cw);
+            R cx[ST], cw[ST];
+            load_row(c + (2 * i) * ST, cx);
+            load_row(c + (2 * i + 1) * ST, cw);
+            R vx = cx[0], vw = cw[0];
 #pragma unroll
             for (int d = 1; d <= DEG; ++d) {
-                vx = fma(vx, y, __ldg(cx + d));
-                vw = fma(vw, y, __ldg(cw + d));
+                vx = fma(vx, y, cx[d]);
+                vw = fma(vw, y, cw[d]);
             }
             x[i] = vx;
             w[i] = vw;
         }
     } else {  // large-T limit (also taken by a NaN T, which keeps the table index in range)
-        const R* herm = tab + rys_table_len(DEG) - 50;
+        const R* herm = tab + rys_table_len(RysStride<R>::value) - 50;
         R rT = R(1) / T;
         R s = sqrt(rT);
 #pragma unroll
@@ -184,11 +212,13 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     const PP* pk = prims + ket.prim_begin;
     const int nb = bra.nprim, nk = ket.nprim;
     for (int ib = 0; ib < nb; ++ib) {
-        const R p = pb[ib].p, rp = pb[ib].rp, Eab = pb[ib].E, cab = pb[ib].cc;
-        const R Px = pb[ib].P[0], Py = pb[ib].P[1], Pz = pb[ib].P[2];
-        const R PAx = pb[ib].PA[0], PAy = pb[ib].PA[1], PAz = pb[ib].PA[2];
+        const PP bp = pb[ib];  // whole 16-byte-aligned record: vector loads
+        const R p = bp.p, rp = bp.rp, Eab = bp.E, cab = bp.cc;
+        const R Px = bp.P[0], Py = bp.P[1], Pz = bp.P[2];
+        const R PAx = bp.PA[0], PAy = bp.PA[1], PAz = bp.PA[2];
         for (int ik = 0; ik < nk; ++ik) {
-            const R q = pk[ik].p, rq = pk[ik].rp, Ecd = pk[ik].E, ccd = pk[ik].cc;
+            const PP kp = pk[ik];
+            const R q = kp.p, rq = kp.rp, Ecd = kp.E, ccd = kp.cc;
             // one reciprocal square root gives both 1/sqrt(p+q) and 1/(p+q) (the FP64 pipe of this
             // GPU is 1/64 of the FP32 one: a division and a square root cost twice as much)
             const R rs = rsqrt(p + q);
@@ -197,8 +227,8 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
             const R rpq = rs * rs;
             sr *= cab * ccd;
             if (npass) ++*npass;
-            const R QCx = pk[ik].PA[0], QCy = pk[ik].PA[1], QCz = pk[ik].PA[2];
-            const R PQx = Px - R(pk[ik].P[0]), PQy = Py - R(pk[ik].P[1]), PQz = Pz - R(pk[ik].P[2]);
+            const R QCx = kp.PA[0], QCy = kp.PA[1], QCz = kp.PA[2];
+            const R PQx = Px - R(kp.P[0]), PQy = Py - R(kp.P[1]), PQz = Pz - R(kp.P[2]);
             const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
             R x[NR], w[NR];
             rys_roots<NR, R>(T, rys, x, w, compat);
