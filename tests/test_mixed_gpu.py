@@ -4,7 +4,7 @@
   equal the plain FP64 build within the G tolerance (1e-10) when the skip cutoff is tiny;
 * with every quartet in FP32 the result must stay within FP32 accuracy of the FP64 build (relative
   1e-5 of max|G|) and differ from it (the FP32 kernels really ran);
-* an incremental mixed-precision SCF reaches the FP64 SCF energy within 1e-6 Eh (the spec bar of
+* an incremental mixed-precision SCF reaches the FP64 SCF energy within 1e-6 Eh (the accuracy bar of
   the precision form), for RHF and UHF.
 """
 import numpy as np

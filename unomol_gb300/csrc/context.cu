@@ -988,9 +988,10 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
 //
 // The regular build keeps its per-build scratch (the dense copy of P and the N x N accumulator T) in
 // device buffers that it allocates on first use.  Some callers cannot let a library call cudaMalloc
-// once they are running: a host framework that owns every device allocation after start-up (fixed
-// budget, its own pool), or an iteration loop that must not take cudaMalloc's implicit device
-// synchronisation.  For them this build keeps that scratch in one file-scope device array instead.
+// once they are running: a host framework that owns every device allocation after start-up (a fixed
+// memory allowance, its own pool), or an iteration loop that must not take cudaMalloc's implicit device
+// synchronisation.  For them the allocation-free build keeps that scratch in one file-scope device
+// array instead.
 // The array is part of the library's device image, so every GPU on which the library's kernels are
 // loaded holds it (NOALLOC_SCRATCH_BYTES) until the process exits.
 // ---------------------------------------------------------------------------------------------
