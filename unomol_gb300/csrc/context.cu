@@ -160,6 +160,8 @@ void build_pair(UnomolCtx* ctx, int ish, int jsh, ShellPair& sp, std::vector<Pri
             }
             pp.E = std::exp(-ai * bj * ab2 * pp.rp) * pp.rp;
             pp.cc = ci * cj * f;
+            pp.pf = (float)pp.p;
+            pp.Ef = (float)pp.E;
             prims.push_back(pp);
         }
     }

@@ -77,6 +77,8 @@ extern "C" int unomol_gpu_gdpm(UnomolCtx* ctx, const double* q, double* H) {
         for (int x = 0; x < 3; ++x) g.P[x] = q[x], g.PA[x] = 0.0;
         g.E = 1.0 / GDPM_ALF[k];  // exp(0) / a_k: the Gaussian is its own product, K_cd = 1
         g.cc = GDPM_COF[k];
+        g.pf = (float)g.p;
+        g.Ef = (float)g.E;
         prims.push_back(g);
     }
     for (const ShellPair& sp : pairs)

@@ -38,7 +38,7 @@ struct __align__(16) PrimPair {
     double E;          // exp(-alpha_a alpha_b |AB|^2 / p) / p, coefficient free (prefactor screen)
     double cc;         // c_a c_b, times 2 for the i != j half of a same-shell pair
                        // (TwoElectronInts.cpp:444-449)
-    double pad_;       // 80 bytes: five 16-byte loads
+    float pf, Ef;      // p and E in FP32, for a cheap pre-screen (80 bytes: five 16-byte loads)
 };
 
 struct __align__(16) PrimPair32 {

@@ -211,52 +211,94 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     const PP* pb = prims + bra.prim_begin;
     const PP* pk = prims + ket.prim_begin;
     const int nb = bra.nprim, nk = ket.nprim;
-    for (int ib = 0; ib < nb; ++ib) {
-        const PP bp = pb[ib];  // whole 16-byte-aligned record: vector loads
-        const R p = bp.p, rp = bp.rp, Eab = bp.E, cab = bp.cc;
+    // one surviving primitive quartet: bra record bp, ket record kp, rs = 1/sqrt(p+q), sr its prefactor
+    auto primitive = [&](const PP& bp, const PP& kp, R rs, R sr) {
+        const R p = bp.p, rp = bp.rp, cab = bp.cc;
         const R Px = bp.P[0], Py = bp.P[1], Pz = bp.P[2];
         const R PAx = bp.PA[0], PAy = bp.PA[1], PAz = bp.PA[2];
-        for (int ik = 0; ik < nk; ++ik) {
-            const PP kp = pk[ik];
-            const R q = kp.p, rq = kp.rp, Ecd = kp.E, ccd = kp.cc;
-            // one reciprocal square root gives both 1/sqrt(p+q) and 1/(p+q) (the FP64 pipe of this
-            // GPU is 1/64 of the FP32 one: a division and a square root cost twice as much)
-            const R rs = rsqrt(p + q);
-            R sr = R(SRTERM) * Eab * Ecd * rs;
-            if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
-            const R rpq = rs * rs;
-            sr *= cab * ccd;
-            if (npass) ++*npass;
-            const R QCx = kp.PA[0], QCy = kp.PA[1], QCz = kp.PA[2];
-            const R PQx = Px - R(kp.P[0]), PQy = Py - R(kp.P[1]), PQz = Pz - R(kp.P[2]);
-            const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
-            R x[NR], w[NR];
-            rys_roots<NR, R>(T, rys, x, w, compat);
+        const R q = kp.p, rq = kp.rp, ccd = kp.cc;
+        const R rpq = rs * rs;
+        sr *= cab * ccd;
+        if (npass) ++*npass;
+        const R QCx = kp.PA[0], QCy = kp.PA[1], QCz = kp.PA[2];
+        const R PQx = Px - R(kp.P[0]), PQy = Py - R(kp.P[1]), PQz = Pz - R(kp.P[2]);
+        const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
+        R x[NR], w[NR];
+        rys_roots<NR, R>(T, rys, x, w, compat);
 #pragma unroll
-            for (int r = 0; r < NR; ++r) {
-                const R fff = x[r] * rpq;  // t^2 / (p + q)   (Rys.hpp:126-129)
-                const R B00 = R(0.5) * fff;
-                const R B1 = (R(0.5) - B00 * q) * rp;
-                const R B1p = (R(0.5) - B00 * p) * rq;
-                const R qf = q * fff, pf = p * fff;
-                R Ix[Q::NI], Iy[Q::NI], Iz[Q::NI];
-                rys_axis<LA, LB, LC, LD, R>(R(1), PAx - qf * PQx, QCx + pf * PQx, B00, B1, B1p, ABx, CDx, Ix);
-                rys_axis<LA, LB, LC, LD, R>(R(1), PAy - qf * PQy, QCy + pf * PQy, B00, B1, B1p, ABy, CDy, Iy);
-                rys_axis<LA, LB, LC, LD, R>(w[r] * sr, PAz - qf * PQz, QCz + pf * PQz, B00, B1, B1p, ABz, CDz, Iz);
+        for (int r = 0; r < NR; ++r) {
+            const R fff = x[r] * rpq;  // t^2 / (p + q)   (Rys.hpp:126-129)
+            const R B00 = R(0.5) * fff;
+            const R B1 = (R(0.5) - B00 * q) * rp;
+            const R B1p = (R(0.5) - B00 * p) * rq;
+            const R qf = q * fff, pf = p * fff;
+            R Ix[Q::NI], Iy[Q::NI], Iz[Q::NI];
+            rys_axis<LA, LB, LC, LD, R>(R(1), PAx - qf * PQx, QCx + pf * PQx, B00, B1, B1p, ABx, CDx, Ix);
+            rys_axis<LA, LB, LC, LD, R>(R(1), PAy - qf * PQy, QCy + pf * PQy, B00, B1, B1p, ABy, CDy, Iy);
+            rys_axis<LA, LB, LC, LD, R>(w[r] * sr, PAz - qf * PQz, QCz + pf * PQz, B00, B1, B1p, ABz, CDz, Iz);
 #pragma unroll
-                for (int ia = 0; ia < Q::NA; ++ia)
+            for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
-                    for (int ibb = 0; ibb < Q::NB; ++ibb)
+                for (int ibb = 0; ibb < Q::NB; ++ibb)
 #pragma unroll
-                        for (int ic = 0; ic < Q::NC; ++ic)
+                    for (int ic = 0; ic < Q::NC; ++ic)
 #pragma unroll
-                            for (int id = 0; id < Q::ND; ++id) {
-                                const int f = ((ia * Q::NB + ibb) * Q::NC + ic) * Q::ND + id;
-                                const int jx = Q::iidx(cart_lx(LA, ia), cart_lx(LB, ibb), cart_lx(LC, ic), cart_lx(LD, id));
-                                const int jy = Q::iidx(cart_ly(LA, ia), cart_ly(LB, ibb), cart_ly(LC, ic), cart_ly(LD, id));
-                                const int jz = Q::iidx(cart_lz(LA, ia), cart_lz(LB, ibb), cart_lz(LC, ic), cart_lz(LD, id));
-                                acc[f] = fma(Ix[jx] * Iy[jy], Iz[jz], acc[f]);
-                            }
+                        for (int id = 0; id < Q::ND; ++id) {
+                            const int f = ((ia * Q::NB + ibb) * Q::NC + ic) * Q::ND + id;
+                            const int jx = Q::iidx(cart_lx(LA, ia), cart_lx(LB, ibb), cart_lx(LC, ic), cart_lx(LD, id));
+                            const int jy = Q::iidx(cart_ly(LA, ia), cart_ly(LB, ibb), cart_ly(LC, ic), cart_ly(LD, id));
+                            const int jz = Q::iidx(cart_lz(LA, ia), cart_lz(LB, ibb), cart_lz(LC, ic), cart_lz(LD, id));
+                            acc[f] = fma(Ix[jx] * Iy[jy], Iz[jz], acc[f]);
+                        }
+        }
+    };
+    if constexpr (sizeof(R) == 8) {
+        // FP64: each lane walks its primitive quartets (bra-major, as the reference) and first looks
+        // ahead for the next one past the prefactor screen (TwoElectronInts.cpp:478-479), with an FP32
+        // pre-screen on float copies of p and E (quartets clearly below the cut cost no FP64 work; the
+        // others take the exact FP64 test, so the surviving set and the order of the sums are
+        // unchanged).  The warp then evaluates one surviving quartet per lane and round, so lanes whose
+        // quartets were screened out do not sit idle through another lane's FP64 work.
+        const float prescreen = (float)prim_cut * 0.999f;
+        int ib = 0, ik = 0, cb = -1;
+        PP bp = pb[0];
+        for (;;) {
+            PP kp;
+            R rs = R(0), sr = R(0);
+            bool found = false;
+            while (ib < nb) {
+                if (ib != cb) {
+                    bp = pb[ib];  // whole 16-byte-aligned records: vector loads
+                    cb = ib;
+                }
+                kp = pk[ik];
+                if (++ik == nk) {
+                    ik = 0;
+                    ++ib;
+                }
+                if (float(SRTERM) * bp.Ef * kp.Ef * rsqrtf(bp.pf + kp.pf) < prescreen) continue;
+                // one reciprocal square root gives both 1/sqrt(p+q) and 1/(p+q) (the FP64 pipe of this
+                // GPU is 1/64 of the FP32 one: a division and a square root cost twice as much)
+                rs = rsqrt(bp.p + kp.p);
+                sr = R(SRTERM) * bp.E * kp.E * rs;
+                if (above_cut(sr, (double)prim_cut)) {
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) break;
+            primitive(bp, kp, rs, sr);
+        }
+    } else {
+        // FP32 (bound by its loads, not by divergence): the plain nested loops
+        for (int ib = 0; ib < nb; ++ib) {
+            const PP bp = pb[ib];
+            for (int ik = 0; ik < nk; ++ik) {
+                const PP kp = pk[ik];
+                const R rs = rsqrt(bp.p + kp.p);
+                const R sr = R(SRTERM) * bp.E * kp.E * rs;
+                if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
+                primitive(bp, kp, rs, sr);
             }
         }
     }
