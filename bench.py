@@ -57,7 +57,8 @@ def basis():
 
 
 def dist_env():
-    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+    from unomol_gb300.replicas import env
+    return env()
 
 
 class Clocks:
@@ -237,7 +238,7 @@ def counted_flops(ctx, inputs, dev, stream):
 def run_ours(args):
     import torch
 
-    from unomol_gb300 import guess, native
+    from unomol_gb300 import guess, native, replicas
     ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist
@@ -288,20 +289,14 @@ def run_ours(args):
     timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
     f64, f32, launches, nq, nq32, nfq = counted_flops(mixed, inputs, dev, stream)
     # timed region
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier(ws)
     torch.cuda.synchronize(dev)
     clocks = Clocks(local)
     step_ms, eri_ms = timed_builds(mixed, inputs, args.steps, dev, stream, flush)
     torch.cuda.synchronize(dev)
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier(ws)
     clk = clocks.stop()
-    total_s = sum(step_ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = replicas.max_over_ranks(sum(step_ms) / 1e3, ws, dev)
     value = ws * args.steps / total_s
     # the plain FP64 path on the same densities (full builds)
     plain_inputs = [(True, D) for D in rm["densities"]]
@@ -325,12 +320,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     e2e_steps(args.steps)
     torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = ws * args.steps / e2e_s
+    e2e = replicas.job_rate(args.steps, time.perf_counter() - t0, ws, dev)
     # roofline of the ERI + J/K kernels over the timed steps
     peak64 = native.fma_peak(True)
     peak32 = native.fma_peak(False)
