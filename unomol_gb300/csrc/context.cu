@@ -211,7 +211,7 @@ int build_worklists(UnomolCtx* ctx) {
     ctx->launches.clear();
     const int nb = (int)ctx->block_begin.size();
     const double cut = ctx->schwarz_cut;
-    int64_t total_quartets = 0, screened = 0, fq = 0, pq = 0;
+    int64_t total_quartets = 0, screened = 0, fq = 0;
     // group block pairs by quartet class
     std::vector<std::vector<BlockPair>> per_class(NPAIRCLASS * NPAIRCLASS);
     for (int X = 0; X < nb; ++X) {
@@ -245,12 +245,10 @@ int build_worklists(UnomolCtx* ctx) {
                 total_quartets += full;
                 run += n;
                 ctx->prefix.push_back(run);
-                pq += (long long)n * ctx->pairs[bp.bra_begin + i].nprim * 0;  // filled below
             }
             bp.work_count = run;
             screened += run;
             fq += run * nfq;
-            (void)pq;
             const int cls = ctx->block_class[X] * NPAIRCLASS + ctx->block_class[Y];
             if (run > 0) per_class[cls].push_back(bp);
             else ctx->prefix.resize(bp.prefix_off);  // drop the unused prefix
@@ -721,8 +719,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     return UNOMOL_OK;
 }
 
-int finish_timing(UnomolCtx* ctx, cudaStream_t s) {
-    (void)s;
+int finish_timing(UnomolCtx* ctx) {
     CU(cudaEventSynchronize(ctx->ev[3]));
     float ms_eri = 0.f, ms_tot = 0.f;
     CU(cudaEventElapsedTime(&ms_eri, ctx->ev[1], ctx->ev[2]));
@@ -889,7 +886,7 @@ int unomol_gpu_set_rys_mode(UnomolCtx* ctx, int mode) {
 
 int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total) {
     if (!ctx || !ms_eri || !ms_total) return fail(ctx, UNOMOL_EINVAL, "null argument");
-    int rc = finish_timing(ctx, ctx->stream);
+    int rc = finish_timing(ctx);
     if (rc) return rc;
     *ms_eri = ctx->stats.ms_eri;
     *ms_total = ctx->stats.ms_total;
@@ -932,7 +929,7 @@ int unomol_gpu_fock_rhf(UnomolCtx* ctx, const double* P, double* G) {
     if (rc) return rc;
     CU(cudaMemcpyAsync(G, ctx->d_Ga, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));  // G is the caller's host array: wait for the copy back
-    return finish_timing(ctx, ctx->stream);
+    return finish_timing(ctx);
 }
 
 int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, double* Ga, double* Gb) {
@@ -949,7 +946,7 @@ int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, doub
     CU(cudaMemcpyAsync(Ga, ctx->d_Ga, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaMemcpyAsync(Gb, ctx->d_Gb, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));  // G is the caller's host array: wait for the copy back
-    return finish_timing(ctx, ctx->stream);
+    return finish_timing(ctx);
 }
 
 void unomol_gpu_destroy(UnomolCtx* ctx) {

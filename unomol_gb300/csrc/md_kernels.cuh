@@ -81,9 +81,7 @@ __device__ double md_function_quartet(const ShellPair& bra, const ShellPair& ket
         Tb[k] = T12[k] + T34[k];
     }
     const int L = la + lb + lc + ld;
-    const int nbox = (Tb[0] + 1) * (Tb[1] + 1) * (Tb[2] + 1);
     double Rn[2][(MD_LT / 3 + 2) * (MD_LT / 3 + 2) * (MD_LT / 3 + 2) + 64];  // two levels of the box
-    (void)nbox;
     auto bidx = [&](int t, int u, int v) { return (t * (Tb[1] + 1) + u) * (Tb[2] + 1) + v; };
     double sum = 0.0;
     const PrimPair* pb = prims + bra.prim_begin;

@@ -383,7 +383,7 @@ int set_ptrs(BState& st, int id, const double* A, const double* B, double* C) {
 
 // eigenvectors (in place) and eigenvalues of every group's matrices in A (W: eigenvalues): one batched
 // cuSOLVER call per group, or one syevd per matrix for a group the batched solver does not take
-int eig(BState& st, double* A, cudaStream_t s) {
+int eig(BState& st, double* A) {
     for (size_t g = 0; g < st.gn.size(); ++g) {
         const int n = st.gn[g];
         const int first = st.gstart[g], cnt = (g + 1 < st.gn.size() ? st.gstart[g + 1] : st.nmol) - first;
@@ -412,7 +412,6 @@ int eig(BState& st, double* A, cudaStream_t s) {
                                   hsz ? st.hwork.data() : nullptr, hsz, st.info + first, cnt),
            UNOMOL_ECUDA);
     }
-    (void)s;
     return UNOMOL_OK;
 }
 
@@ -421,7 +420,7 @@ int density_from_F(BState& st, double* dP, cudaStream_t s) {
     int rc;
     if ((rc = gemm(st, 4, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T1 = F X
     if ((rc = gemm(st, 5, CUBLAS_OP_T, CUBLAS_OP_N, false))) return rc;  // Fo = X^T T1
-    if ((rc = eig(st, st.Fo, s))) return rc;
+    if ((rc = eig(st, st.Fo))) return rc;
     if ((rc = gemm(st, 6, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T2 = C = X Fo
     if ((rc = gemm(st, 7, CUBLAS_OP_N, CUBLAS_OP_T, true))) return rc;   // Pf = C_occ C_occ^T
     k_pack<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.Pf, dP);
@@ -595,7 +594,7 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         return fail(rc);
     // X from S (canonical, RHF.hpp:214-233)
     BK(cudaMemcpyAsync(st.X, st.S, b2, cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
-    if ((rc = eig(st, st.X, s))) return fail(rc);
+    if ((rc = eig(st, st.X))) return fail(rc);
     k_form_x<<<nmol, 256, 0, s>>>(st.d_mols, st.W, st.X, st.bad);
     if (opt->guess == UNOMOL_GUESS_GIVEN) {
         // the caller's densities (PMATRIX.DAT form, batch order; RHF.hpp:120-123, 318)
@@ -644,16 +643,12 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     }
     if (graph_used) *graph_used = used_graph;
     std::vector<int> conv(nmol);
-    int it = 0;
-    for (; it < maxits; ++it) {
+    for (int it = 0; it < maxits; ++it) {
         if (used_graph) BK(cudaGraphLaunch(exec, s), UNOMOL_ECUDA);
         else if ((rc = iteration(st, batch, dP, dG, o, s))) return fail(rc);
         BK(cudaMemcpyAsync(conv.data(), st.conv, sizeof(int) * nmol, cudaMemcpyDeviceToHost, s), UNOMOL_ECUDA);
         BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
-        if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; })) {
-            ++it;
-            break;
-        }
+        if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; })) break;
     }
     if (exec) cudaGraphExecDestroy(exec);
     std::vector<double> E(nmol), err(nmol), E1(nmol), pd(nmol), de(nmol);
@@ -682,7 +677,6 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         res[m].pdiff = pd[m];
     }
     if (P_out) BK(cudaMemcpy(P_out, dP, sizeof(double) * ptot, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
-    (void)it;
     return UNOMOL_OK;
 }
 
