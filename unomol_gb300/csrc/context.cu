@@ -1,13 +1,15 @@
 // C ABI of the direct Fock build (include/unomol_gb300.h): the GPU counterpart of unomol's
 // TwoElectronInts (TwoElectronInts.hpp:79-110).
 //
-// Setup (create / recalculate): shell pairs with their primitive-pair data are built and sorted into
-// blocks of equal (pair class, primitive-pair count); the Schwarz diagonal (ab|ab) is computed on the
-// GPU; pairs are re-sorted by descending bound within their block; then for every pair of blocks the
-// Schwarz "staircase" (bra i keeps the first n_i ket pairs) gives a compact work list per quartet class.
+// Setup (create / recalculate), on the device (setup.cu): shell pairs with their primitive-pair data are
+// built and sorted into blocks of equal (pair class, primitive-pair count); the Schwarz diagonal
+// (ab|ab) is computed; pairs are re-sorted by descending bound within their block; then for every pair
+// of blocks the Schwarz "staircase" (bra i keeps the first n_i ket pairs) gives a compact work list per
+// quartet class.  The host keeps the block boundaries and the block-pair list.
 // Fock build (fock_rhf / fock_uhf): expand packed P to a dense N x N copy, zero the accumulators,
 // launch one kernel per quartet class, fold G += T + T^T into packed storage.
 #include <algorithm>
+#include <climits>
 #include <memory>
 #include <mutex>
 #include <cmath>
@@ -20,6 +22,7 @@
 #include "ctx_view.h"
 #include "fock_dispatch.cuh"
 #include "fock_kernels.cuh"
+#include "setup.h"
 
 using namespace ugb;
 
@@ -43,15 +46,18 @@ struct UnomolCtx {
     std::vector<int> sl, snp, scen, soff, sprim;
     std::vector<double> alpha, coef, centers;
     NormTable nt{};
-    // host copies of the setup
-    std::vector<ShellPair> pairs;
-    std::vector<PrimPair> prims;
-    std::vector<int> block_begin, block_count, block_class;
+    // host side of the setup: block boundaries and keys, block pairs, class launches
+    int npairs = 0;
+    long long nprims = 0, nrows = 0;
+    std::vector<int> block_begin, block_count, block_class, block_nprim;
     std::vector<char> block_new;
     std::vector<BlockPair> bps;
-    std::vector<long long> prefix;
-    std::vector<int> row_bp;
     std::vector<ClassLaunch> launches;
+    // the basis on the device (centres refreshed by recalculate) and the setup's scratch
+    int *d_snp = nullptr, *d_scen = nullptr, *d_sprim = nullptr;
+    double *d_alpha = nullptr, *d_coef = nullptr, *d_centers = nullptr;
+    char* d_ws = nullptr;
+    size_t ws_bytes = 0;
     // per-build work lists of the density-screened / mixed-precision build
     int *d_rowbp = nullptr, *d_mseg = nullptr;
     long long *d_c64 = nullptr, *d_c32 = nullptr, *d_pre64 = nullptr, *d_pre32 = nullptr;
@@ -66,7 +72,6 @@ struct UnomolCtx {
     long long* d_prefix = nullptr;
     double* d_rys = nullptr;
     float* d_rys32 = nullptr;
-    double* d_q = nullptr;
     double *d_Pa = nullptr, *d_Pb = nullptr, *d_Ta = nullptr, *d_Tb = nullptr;
     double *d_Ga = nullptr, *d_Gb = nullptr, *d_pk_a = nullptr, *d_pk_b = nullptr;
     float* d_pmax = nullptr;
@@ -80,7 +85,6 @@ struct UnomolCtx {
     int prec_mode = UNOMOL_PREC_FP64;
     int rys_mode = UNOMOL_RYS_REFERENCE;
     int eri_method = UNOMOL_ERI_REFERENCE;
-    unsigned long long* d_qbits = nullptr;
     int counting = 0;
     double fp32_cut = 1e-10;
     UnomolStats stats{};
@@ -125,50 +129,6 @@ void build_norms(NormTable& nt) {
             nt.v[l][c] = 1.0 / std::sqrt(dfact[cart_lx(l, c)] * dfact[cart_ly(l, c)] * dfact[cart_lz(l, c)]);
 }
 
-// Primitive pairs of shell pair (ish, jsh) after the L swap (a = larger L), following the loops of
-// TwoElectronInts.cpp:439-460: a same-shell pair keeps j <= i with the factor 2 for j < i.
-void build_pair(UnomolCtx* ctx, int ish, int jsh, ShellPair& sp, std::vector<PrimPair>& prims) {
-    int a = ish, b = jsh;
-    if (ctx->sl[a] < ctx->sl[b]) std::swap(a, b);
-    sp.ish = ish;
-    sp.jsh = jsh;
-    sp.maxsh = ish;
-    sp.canon = ish * (ish + 1) / 2 + jsh;
-    sp.same = (ish == jsh);
-    sp.la = ctx->sl[a];
-    sp.lb = ctx->sl[b];
-    sp.a_off = ctx->soff[a];
-    sp.b_off = ctx->soff[b];
-    const double* A = &ctx->centers[3 * ctx->scen[a]];
-    const double* B = &ctx->centers[3 * ctx->scen[b]];
-    for (int k = 0; k < 3; ++k) sp.AB[k] = A[k] - B[k];
-    const double ab2 = sp.AB[0] * sp.AB[0] + sp.AB[1] * sp.AB[1] + sp.AB[2] * sp.AB[2];
-    sp.prim_begin = (int)prims.size();
-    const int na = ctx->snp[a], nb = ctx->snp[b];
-    for (int i = 0; i < na; ++i) {
-        const double ai = ctx->alpha[ctx->sprim[a] + i], ci = ctx->coef[ctx->sprim[a] + i];
-        const int jend = sp.same ? i + 1 : nb;
-        for (int j = 0; j < jend; ++j) {
-            const double bj = ctx->alpha[ctx->sprim[b] + j], cj = ctx->coef[ctx->sprim[b] + j];
-            const double f = (sp.same && i != j) ? 2.0 : 1.0;
-            PrimPair pp;
-            pp.p = ai + bj;
-            pp.rp = 1.0 / pp.p;
-            for (int k = 0; k < 3; ++k) {
-                pp.P[k] = (ai * A[k] + bj * B[k]) * pp.rp;
-                pp.PA[k] = pp.P[k] - A[k];
-            }
-            pp.E = std::exp(-ai * bj * ab2 * pp.rp) * pp.rp;
-            pp.cc = ci * cj * f;
-            pp.pf = (float)pp.p;
-            pp.Ef = (float)pp.E;
-            prims.push_back(pp);
-        }
-    }
-    sp.nprim = (int)prims.size() - sp.prim_begin;
-    sp.q = 0.0;
-}
-
 // Algorithmic flops of the Rys kernels (FMA = 2, every +,-,*,/,sqrt = 1), counted from the steps of
 // fock_kernels.cuh.  Per primitive quartet past the prefactor cut: setup 20; Rys nodes and weights
 // NR * (2 polynomials * deg Horner steps * 2) + 3, deg = the table degree of the precision (RYS_DEG
@@ -200,21 +160,63 @@ void free_setup(UnomolCtx* c) {
     dfree(c->d_prims32);
     dfree(c->d_bps);
     dfree(c->d_prefix);
-    dfree(c->d_q);
-    dfree(c->d_qbits);
 }
 
-// Work lists for the current Schwarz cutoff (host side; O(npairs * nblocks log npairs)).
+// Bump allocation of the setup's scratch arrays in one device buffer (256-byte aligned pieces); a pass
+// with no buffer only adds up the sizes.
+struct Carve {
+    char* base = nullptr;
+    size_t used = 0;
+    template <typename T>
+    T* take(size_t n) {
+        const size_t off = (used + 255) & ~size_t(255);
+        used = off + sizeof(T) * std::max<size_t>(n, 1);
+        return base ? reinterpret_cast<T*>(base + off) : nullptr;
+    }
+};
+
+int ensure_ws(UnomolCtx* ctx, size_t bytes) {
+    if (bytes <= ctx->ws_bytes) return UNOMOL_OK;
+    CU(cudaStreamSynchronize(ctx->stream));  // nothing may still use the old buffer
+    dfree(ctx->d_ws);
+    ctx->ws_bytes = 0;
+    CU(cudaMalloc(&ctx->d_ws, bytes));
+    ctx->ws_bytes = bytes;
+    return UNOMOL_OK;
+}
+
+ShellsDev shells_dev(const UnomolCtx* ctx) {
+    ShellsDev sh;
+    sh.nshell = ctx->nshell;
+    sh.start_shell = ctx->start_shell;
+    sh.sl = ctx->d_sl;
+    sh.snp = ctx->d_snp;
+    sh.scen = ctx->d_scen;
+    sh.soff = ctx->d_soff;
+    sh.sprim = ctx->d_sprim;
+    sh.alpha = ctx->d_alpha;
+    sh.coef = ctx->d_coef;
+    sh.centers = ctx->d_centers;
+    return sh;
+}
+
+// Work lists for the current Schwarz cutoff: the block-pair list on the host (a size set by the number
+// of blocks), the staircase of every bra row on the device, one read-back of the per-block-pair totals.
 int build_worklists(UnomolCtx* ctx) {
+    cudaStream_t s = ctx->stream;
     ctx->bps.clear();
-    ctx->prefix.clear();
     ctx->launches.clear();
+    dfree(ctx->d_bps);
+    dfree(ctx->d_prefix);
+    for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
+    dfree(ctx->d_rowbp);
+    dfree(ctx->d_mseg);
     const int nb = (int)ctx->block_begin.size();
-    const double cut = ctx->schwarz_cut;
-    int64_t total_quartets = 0, screened = 0, fq = 0;
-    // group block pairs by quartet class
-    std::vector<std::vector<BlockPair>> per_class(NPAIRCLASS * NPAIRCLASS);
-    for (int X = 0; X < nb; ++X) {
+    std::vector<BlockPair> all;
+    std::vector<int> all_x, all_y;
+    long long nrows = 0;
+    int64_t total_quartets = 0;
+    for (int X = 0; X < nb; ++X)
         for (int Y = 0; Y <= X; ++Y) {
             if (ctx->start_shell > 0 && !ctx->block_new[X] && !ctx->block_new[Y]) continue;
             BlockPair bp{};
@@ -223,39 +225,61 @@ int build_worklists(UnomolCtx* ctx) {
             bp.ket_begin = ctx->block_begin[Y];
             bp.ket_count = ctx->block_count[Y];
             bp.triangle = (X == Y);
-            bp.prefix_off = (int)ctx->prefix.size();
-            long long run = 0;
-            ctx->prefix.push_back(0);
-            const ShellPair* kp = &ctx->pairs[bp.ket_begin];
-            const int nbra = bp.bra_count, nket = bp.ket_count;
-            const int la = ctx->pairs[bp.bra_begin].la, lb = ctx->pairs[bp.bra_begin].lb;
-            const int lc = kp[0].la, ld = kp[0].lb;
-            const int nfq = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
-            for (int i = 0; i < nbra; ++i) {
-                const double qi = ctx->pairs[bp.bra_begin + i].q;
-                // ket pairs sorted by descending q: count those with qi*qj >= cut
-                int lo = 0, hi = nket;
-                while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (qi * kp[mid].q >= cut) lo = mid + 1; else hi = mid;
-                }
-                int n = lo;
-                const int full = bp.triangle ? i + 1 : nket;
-                if (n > full) n = full;
-                total_quartets += full;
-                run += n;
-                ctx->prefix.push_back(run);
-            }
-            bp.work_count = run;
-            screened += run;
-            fq += run * nfq;
-            const int cls = ctx->block_class[X] * NPAIRCLASS + ctx->block_class[Y];
-            if (run > 0) per_class[cls].push_back(bp);
-            else ctx->prefix.resize(bp.prefix_off);  // drop the unused prefix
+            bp.prefix_off = (int)std::min<long long>(nrows, INT_MAX);
+            nrows += bp.bra_count + 1;
+            total_quartets += bp.triangle ? (int64_t)bp.bra_count * (bp.bra_count + 1) / 2
+                                          : (int64_t)bp.bra_count * bp.ket_count;
+            all.push_back(bp);
+            all_x.push_back(X);
+            all_y.push_back(Y);
         }
+    if (nrows >= INT_MAX) return fail(ctx, UNOMOL_EINVAL, "too many staircase rows for one context");
+    ctx->nrows = nrows;
+    const int nall = (int)all.size();
+    size_t t_scan = 0;
+    CU(setup_inclusive_sum(nullptr, t_scan, nullptr, nullptr, (int)std::max<long long>(1, nrows), s));
+    auto carve = [&](Carve& w, BlockPair*& d_all, long long*& S, long long*& totals, char*& tmp) {
+        d_all = w.take<BlockPair>(nall);
+        S = w.take<long long>(nrows);
+        totals = w.take<long long>(nall);
+        tmp = w.take<char>(t_scan);
+    };
+    BlockPair* d_all;
+    long long *S, *totals;
+    char* tmp;
+    Carve sizing;
+    carve(sizing, d_all, S, totals, tmp);
+    int rc = ensure_ws(ctx, sizing.used);
+    if (rc) return rc;
+    Carve w;
+    w.base = ctx->d_ws;
+    carve(w, d_all, S, totals, tmp);
+    CU(cudaMalloc(&ctx->d_prefix, sizeof(long long) * std::max<long long>(1, nrows)));
+    std::vector<long long> tot(nall);
+    if (nall > 0) {
+        CU(cudaMemcpyAsync(d_all, all.data(), sizeof(BlockPair) * nall, cudaMemcpyHostToDevice, s));
+        CU(setup_staircase(d_all, nall, ctx->d_pairs, ctx->schwarz_cut, ctx->d_prefix, s));
+        size_t tb = t_scan;
+        CU(setup_inclusive_sum(tmp, tb, ctx->d_prefix, S, (int)nrows, s));
+        CU(setup_prefix_fix(d_all, nall, S, ctx->d_prefix, totals, s));
+        CU(cudaMemcpyAsync(tot.data(), totals, sizeof(long long) * nall, cudaMemcpyDeviceToHost, s));
     }
-    // primitive-quartet count: nprim is uniform within a block
-    int64_t prim_q = 0;
+    CU(cudaStreamSynchronize(s));
+    // non-empty block pairs grouped by quartet class, work ranges 32-aligned (warps never straddle)
+    int64_t screened = 0, fq = 0, prim_q = 0;
+    std::vector<std::vector<BlockPair>> per_class(NPAIRCLASS * NPAIRCLASS);
+    for (int k = 0; k < nall; ++k) {
+        if (tot[k] == 0) continue;
+        BlockPair bp = all[k];
+        bp.work_count = tot[k];
+        const int X = all_x[k], Y = all_y[k];
+        const int bc = ctx->block_class[X], kc = ctx->block_class[Y];
+        const int nfq = ncart(pc_la(bc)) * ncart(pc_lb(bc)) * ncart(pc_la(kc)) * ncart(pc_lb(kc));
+        screened += tot[k];
+        fq += tot[k] * nfq;
+        prim_q += tot[k] * (int64_t)ctx->block_nprim[X] * ctx->block_nprim[Y];
+        per_class[bc * NPAIRCLASS + kc].push_back(bp);
+    }
     for (int cls = 0; cls < NPAIRCLASS * NPAIRCLASS; ++cls) {
         auto& v = per_class[cls];
         if (v.empty()) continue;
@@ -264,134 +288,170 @@ int build_worklists(UnomolCtx* ctx) {
         L.kc = cls % NPAIRCLASS;
         L.bp_begin = (int)ctx->bps.size();
         L.nbp = (int)v.size();
-        long long w = 0;
+        long long wk = 0;
         for (auto& bp : v) {
-            bp.work_begin = w;
-            w += (bp.work_count + 31) / 32 * 32;
+            bp.work_begin = wk;
+            wk += (bp.work_count + 31) / 32 * 32;
             L.quartets += bp.work_count;
-            prim_q += bp.work_count * (int64_t)ctx->pairs[bp.bra_begin].nprim * ctx->pairs[bp.ket_begin].nprim;
             ctx->bps.push_back(bp);
         }
-        L.nwork = w;
+        L.nwork = wk;
         ctx->launches.push_back(L);
     }
     ctx->stats.shell_quartets = screened;
     ctx->stats.shell_quartets_total = total_quartets;
     ctx->stats.primitive_quartets = prim_q;
     ctx->stats.function_quartets = fq;
-    dfree(ctx->d_bps);
-    dfree(ctx->d_prefix);
-    for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
-    dfree(ctx->d_rowbp);
-    dfree(ctx->d_mseg);
     if (!ctx->bps.empty()) {
-        CU(cudaMalloc(&ctx->d_bps, sizeof(BlockPair) * ctx->bps.size()));
-        CU(cudaMemcpyAsync(ctx->d_bps, ctx->bps.data(), sizeof(BlockPair) * ctx->bps.size(), cudaMemcpyHostToDevice, ctx->stream));
-        CU(cudaMalloc(&ctx->d_prefix, sizeof(long long) * ctx->prefix.size()));
-        CU(cudaMemcpyAsync(ctx->d_prefix, ctx->prefix.data(), sizeof(long long) * ctx->prefix.size(), cudaMemcpyHostToDevice, ctx->stream));
-        // row -> block pair map and the per-build work-list buffers of the density-screened build
-        ctx->row_bp.assign(ctx->prefix.size(), -1);
-        for (size_t k = 0; k < ctx->bps.size(); ++k)
-            for (int i = 0; i < ctx->bps[k].bra_count; ++i) ctx->row_bp[ctx->bps[k].prefix_off + i] = (int)k;
-        const size_t nr = ctx->prefix.size(), nbp = ctx->bps.size();
+        const size_t nbp = ctx->bps.size();
+        CU(cudaMalloc(&ctx->d_bps, sizeof(BlockPair) * nbp));
+        CU(cudaMemcpyAsync(ctx->d_bps, ctx->bps.data(), sizeof(BlockPair) * nbp, cudaMemcpyHostToDevice, s));
+        // row -> block pair map (-1 on the end-of-block-pair entries and on the rows of empty block pairs)
+        // and the per-build work-list buffers of the density-screened build
+        const size_t nr = (size_t)nrows;
         CU(cudaMalloc(&ctx->d_rowbp, sizeof(int) * nr));
-        CU(cudaMemcpyAsync(ctx->d_rowbp, ctx->row_bp.data(), sizeof(int) * nr, cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemsetAsync(ctx->d_rowbp, 0xff, sizeof(int) * nr, s));
+        CU(setup_row_bp(ctx->d_bps, (int)nbp, ctx->d_rowbp, s));
         CU(cudaMalloc(&ctx->d_mseg, sizeof(int) * nr));
         for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32}) CU(cudaMalloc(p, sizeof(long long) * nr));
         CU(cudaMalloc(&ctx->d_cnt64, sizeof(long long) * nbp));
         CU(cudaMalloc(&ctx->d_cnt32, sizeof(long long) * nbp));
-        CU(cudaMemsetAsync(ctx->d_c64, 0, sizeof(long long) * nr, ctx->stream));
-        CU(cudaMemsetAsync(ctx->d_c32, 0, sizeof(long long) * nr, ctx->stream));
-        CU(cudaMemsetAsync(ctx->d_mseg, 0, sizeof(int) * nr, ctx->stream));
+        CU(cudaMemsetAsync(ctx->d_c64, 0, sizeof(long long) * nr, s));
+        CU(cudaMemsetAsync(ctx->d_c32, 0, sizeof(long long) * nr, s));
+        CU(cudaMemsetAsync(ctx->d_mseg, 0, sizeof(int) * nr, s));
     }
-    CU(cudaStreamSynchronize(ctx->stream));
+    CU(cudaStreamSynchronize(s));
     return UNOMOL_OK;
 }
 
-// Pairs, Schwarz bounds, block structure and work lists for the current geometry.
+// Pairs, Schwarz bounds, block structure and work lists for the current geometry, built on the device.
 int build_setup(UnomolCtx* ctx) {
     free_setup(ctx);
-    ctx->pairs.clear();
-    ctx->prims.clear();
+    cudaStream_t s = ctx->stream;
     const int ns = ctx->nshell;
-    std::vector<ShellPair> raw;
-    raw.reserve((size_t)ns * (ns + 1) / 2);
+    const long long np64 = (long long)ns * (ns + 1) / 2;
+    if (np64 > (1ll << 28)) return fail(ctx, UNOMOL_EINVAL, "too many shell pairs for one context");
+    const int P = (int)np64;
+    long long nprims = 0;
     for (int i = 0; i < ns; ++i)
-        for (int j = 0; j <= i; ++j) {
-            ShellPair sp{};
-            build_pair(ctx, i, j, sp, ctx->prims);
-            raw.push_back(sp);
-        }
-    // blocks: (class, nprim, new-ness) ascending by class
-    auto key = [&](const ShellPair& s) {
-        const int cls = pair_class(s.la, s.lb);
-        const int isnew = (s.maxsh >= ctx->start_shell) ? 1 : 0;
-        return ((long long)cls << 40) | ((long long)isnew << 32) | (long long)s.nprim;
+        for (int j = 0; j <= i; ++j)
+            nprims += i == j ? (long long)ctx->snp[i] * (ctx->snp[i] + 1) / 2 : (long long)ctx->snp[i] * ctx->snp[j];
+    if (nprims >= INT_MAX) return fail(ctx, UNOMOL_EINVAL, "too many primitive pairs for one context");
+    ctx->npairs = P;
+    ctx->nprims = nprims;
+    ctx->stats.npairs = P;
+    CU(cudaMemcpyAsync(ctx->d_centers, ctx->centers.data(), sizeof(double) * 3 * ctx->ncen, cudaMemcpyHostToDevice, s));
+    CU(cudaMalloc(&ctx->d_pairs, sizeof(ShellPair) * P));
+    CU(cudaMalloc(&ctx->d_prims, sizeof(PrimPair) * nprims));
+    CU(cudaMalloc(&ctx->d_prims32, sizeof(PrimPair32) * nprims));
+    // library scratch sizes (the segmented sort's for the largest possible number of blocks)
+    size_t t_scan = 0, t_sort = 0, t_rle = 0, t_seg = 0;
+    CU(setup_exclusive_sum(nullptr, t_scan, nullptr, nullptr, P, s));
+    CU(setup_sort_keys(nullptr, t_sort, nullptr, nullptr, nullptr, nullptr, P, s));
+    CU(setup_run_length(nullptr, t_rle, nullptr, nullptr, nullptr, nullptr, P, s));
+    CU(setup_sort_desc_segments(nullptr, t_seg, nullptr, nullptr, nullptr, nullptr, P, P, nullptr, nullptr, s));
+    const size_t t_max = std::max(std::max(t_scan, t_sort), std::max(t_rle, t_seg));
+    struct Arrays {
+        unsigned *key0, *key1, *uniq;
+        int *np, *poff, *iota, *perm1, *perm2, *counts, *nruns, *seg;
+        ShellPair *raw, *sorted1;
+        double *q, *q2;
+        unsigned long long* qbits;
+        char* tmp;
+    } a{};
+    auto carve = [&](Carve& w) {
+        a.key0 = w.take<unsigned>(P);
+        a.key1 = w.take<unsigned>(P);
+        a.uniq = w.take<unsigned>(P);
+        a.np = w.take<int>(P);
+        a.poff = w.take<int>(P);
+        a.iota = w.take<int>(P);
+        a.perm1 = w.take<int>(P);
+        a.perm2 = w.take<int>(P);
+        a.counts = w.take<int>(P);
+        a.nruns = w.take<int>(1);
+        a.seg = w.take<int>((size_t)P + 1);
+        a.raw = w.take<ShellPair>(P);
+        a.sorted1 = w.take<ShellPair>(P);
+        a.q = w.take<double>(P);
+        a.q2 = w.take<double>(P);
+        a.qbits = w.take<unsigned long long>(P);
+        a.tmp = w.take<char>(t_max);
     };
-    std::stable_sort(raw.begin(), raw.end(), [&](const ShellPair& x, const ShellPair& y) { return key(x) < key(y); });
-    // Schwarz diagonal on the device
-    CU(cudaMalloc(&ctx->d_pairs, sizeof(ShellPair) * raw.size()));
-    CU(cudaMalloc(&ctx->d_prims, sizeof(PrimPair) * ctx->prims.size()));
-    CU(cudaMalloc(&ctx->d_q, sizeof(double) * raw.size()));
-    CU(cudaMemcpyAsync(ctx->d_pairs, raw.data(), sizeof(ShellPair) * raw.size(), cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(ctx->d_prims, ctx->prims.data(), sizeof(PrimPair) * ctx->prims.size(), cudaMemcpyHostToDevice, ctx->stream));
-    {
-        size_t i = 0;
-        while (i < raw.size()) {
-            const int cls = pair_class(raw[i].la, raw[i].lb);
-            size_t j = i;
-            while (j < raw.size() && pair_class(raw[j].la, raw[j].lb) == cls) ++j;
-            if (cls < NTMPLCLASS) {
-                CU(launch_schwarz(cls, ctx->d_pairs, ctx->d_prims, (int)i, (int)(j - i), ctx->nt, ctx->d_rys, ctx->d_q,
-                                  ctx->stream));
-            } else {
-                if (!ctx->d_qbits) CU(cudaMalloc(&ctx->d_qbits, sizeof(unsigned long long) * raw.size()));
-                CU(launch_schwarz_high(pc_la(cls), pc_lb(cls), ctx->d_pairs, ctx->d_prims, (int)i, (int)(j - i), ctx->nt,
-                                       ctx->d_rys, ctx->d_q, ctx->d_qbits, ctx->stream));
-            }
-            i = j;
-        }
+    Carve sizing;
+    carve(sizing);
+    int rc = ensure_ws(ctx, sizing.used);
+    if (rc) return rc;
+    Carve w;
+    w.base = ctx->d_ws;
+    carve(w);
+    // pairs in canonical order, their primitive pairs, and the sort by (class, new/old, primitive pairs)
+    const ShellsDev sh = shells_dev(ctx);
+    size_t tb = t_max;
+    CU(setup_pair_keys(sh, P, a.key0, a.np, a.iota, s));
+    CU(setup_exclusive_sum(a.tmp, tb, a.np, a.poff, P, s));
+    CU(setup_build_pairs(sh, P, a.poff, a.raw, ctx->d_prims, ctx->d_prims32, s));
+    tb = t_max;
+    CU(setup_sort_keys(a.tmp, tb, a.key0, a.key1, a.iota, a.perm1, P, s));
+    tb = t_max;
+    CU(setup_run_length(a.tmp, tb, a.key1, a.uniq, a.counts, a.nruns, P, s));
+    CU(setup_gather_pairs(a.raw, a.perm1, nullptr, P, a.sorted1, s));
+    // block boundaries and keys to the host
+    int nb = 0;
+    const int head = std::min(P, 4096);
+    std::vector<unsigned> ukeys(head);
+    std::vector<int> ucnt(head);
+    CU(cudaMemcpyAsync(&nb, a.nruns, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(ukeys.data(), a.uniq, sizeof(unsigned) * head, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(ucnt.data(), a.counts, sizeof(int) * head, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    if (nb < 1 || nb > P) return fail(ctx, UNOMOL_ECUDA, "shell-pair sort returned no blocks");
+    if (nb > head) {
+        ukeys.resize(nb);
+        ucnt.resize(nb);
+        CU(cudaMemcpyAsync(ukeys.data(), a.uniq, sizeof(unsigned) * nb, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(ucnt.data(), a.counts, sizeof(int) * nb, cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
     }
-    std::vector<double> q(raw.size());
-    CU(cudaMemcpyAsync(q.data(), ctx->d_q, sizeof(double) * raw.size(), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
-    for (size_t i = 0; i < raw.size(); ++i) raw[i].q = q[i];
-    // within each block, descending q
     ctx->block_begin.clear();
     ctx->block_count.clear();
     ctx->block_class.clear();
+    ctx->block_nprim.clear();
     ctx->block_new.clear();
-    size_t i = 0;
-    while (i < raw.size()) {
-        size_t j = i;
-        while (j < raw.size() && key(raw[j]) == key(raw[i])) ++j;
-        std::stable_sort(raw.begin() + i, raw.begin() + j, [](const ShellPair& x, const ShellPair& y) { return x.q > y.q; });
-        ctx->block_begin.push_back((int)i);
-        ctx->block_count.push_back((int)(j - i));
-        ctx->block_class.push_back(pair_class(raw[i].la, raw[i].lb));
-        ctx->block_new.push_back(raw[i].maxsh >= ctx->start_shell);
-        i = j;
+    std::vector<int> seg(nb + 1);
+    int off = 0;
+    for (int k = 0; k < nb; ++k) {
+        seg[k] = off;
+        ctx->block_begin.push_back(off);
+        ctx->block_count.push_back(ucnt[k]);
+        ctx->block_class.push_back((int)pair_key_class(ukeys[k]));
+        ctx->block_new.push_back((char)pair_key_new(ukeys[k]));
+        ctx->block_nprim.push_back((int)pair_key_nprim(ukeys[k]));
+        off += ucnt[k];
     }
-    ctx->pairs = raw;
-    ctx->stats.npairs = (int)raw.size();
-    CU(cudaMemcpyAsync(ctx->d_pairs, raw.data(), sizeof(ShellPair) * raw.size(), cudaMemcpyHostToDevice, ctx->stream));
-    // FP32 copy of the primitive pairs
-    std::vector<PrimPair32> p32(ctx->prims.size());
-    for (size_t k = 0; k < ctx->prims.size(); ++k) {
-        const PrimPair& s = ctx->prims[k];
-        PrimPair32& d = p32[k];
-        d.p = (float)s.p;
-        d.rp = (float)s.rp;
-        for (int m = 0; m < 3; ++m) {
-            d.P[m] = (float)s.P[m];
-            d.PA[m] = (float)s.PA[m];
-        }
-        d.E = (float)s.E;
-        d.cc = (float)s.cc;
+    seg[nb] = off;
+    if (off != P) return fail(ctx, UNOMOL_ECUDA, "shell-pair blocks do not cover the pairs");
+    // Schwarz diagonal, one launch per class run of the class-sorted pairs
+    for (int k = 0; k < nb;) {
+        int k2 = k;
+        while (k2 < nb && ctx->block_class[k2] == ctx->block_class[k]) ++k2;
+        const int cls = ctx->block_class[k], begin = ctx->block_begin[k];
+        const int count = ctx->block_begin[k2 - 1] + ctx->block_count[k2 - 1] - begin;
+        if (cls < NTMPLCLASS)
+            CU(launch_schwarz(cls, a.sorted1, ctx->d_prims, begin, count, ctx->nt, ctx->d_rys, a.q, s));
+        else
+            CU(launch_schwarz_high(pc_la(cls), pc_lb(cls), a.sorted1, ctx->d_prims, begin, count, ctx->nt, ctx->d_rys, a.q,
+                                   a.qbits, s));
+        k = k2;
     }
-    CU(cudaMalloc(&ctx->d_prims32, sizeof(PrimPair32) * p32.size()));
-    CU(cudaMemcpyAsync(ctx->d_prims32, p32.data(), sizeof(PrimPair32) * p32.size(), cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
+    // descending bound inside every block (stable: equal bounds keep the canonical order)
+    size_t t_need = 0;
+    CU(setup_sort_desc_segments(nullptr, t_need, nullptr, nullptr, nullptr, nullptr, P, nb, nullptr, nullptr, s));
+    if (t_need > t_max) return fail(ctx, UNOMOL_ECUDA, "segmented sort needs more scratch than reserved");
+    CU(cudaMemcpyAsync(a.seg, seg.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
+    tb = t_max;
+    CU(setup_sort_desc_segments(a.tmp, tb, a.q, a.q2, a.iota, a.perm2, P, nb, a.seg, a.seg + 1, s));
+    CU(setup_gather_pairs(a.sorted1, a.perm2, a.q2, P, ctx->d_pairs, s));
     return build_worklists(ctx);
 }
 
@@ -609,7 +669,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         CU(cudaMemsetAsync(ctx->d_dmax, 0, sizeof(float), s));
         shell_pmax<<<(ns2 + 255) / 256, 256, 0, s>>>(ctx->d_Pa, A.Pb, ctx->d_soff, ctx->d_sl, ctx->nshell, n, ctx->d_pmax,
                                                      ctx->d_dmax);
-        const long long nr = (long long)ctx->prefix.size();
+        const long long nr = ctx->nrows;
         split_rows<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(ctx->d_pairs, ctx->d_bps, ctx->d_rowbp, ctx->d_prefix, nr,
                                                                 ctx->d_dmax, std::max(ctx->fp32_cut, ctx->skip_cut),
                                                                 ctx->skip_cut, ctx->d_c64, ctx->d_c32, ctx->d_mseg);
@@ -739,10 +799,17 @@ CtxView ctx_view(const UnomolCtx* c) {
     v.nshell = c->nshell;
     v.rys_compat = c->rys_mode == UNOMOL_RYS_REFERENCE;
     v.eri_method = c->eri_method;
-    v.pairs = &c->pairs;
-    v.prims = &c->prims;
+    v.d_pairs = c->d_pairs;
+    v.npairs = c->npairs;
+    v.d_prims = c->d_prims;
+    v.nprims = c->nprims;
+    v.d_prefix = c->d_prefix;
+    v.nrows = c->nrows;
     v.bps = &c->bps;
-    v.prefix = &c->prefix;
+    v.block_begin = &c->block_begin;
+    v.block_count = &c->block_count;
+    v.block_class = &c->block_class;
+    v.stream = c->stream;
     for (const ClassLaunch& L : c->launches) v.launches.push_back({L.bc, L.kc, L.bp_begin, L.nbp, L.nwork, L.quartets});
     v.nt = c->nt;
     v.d_rys = c->d_rys;
@@ -781,6 +848,7 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
         const int l = b->shell_l[i];
         if (l < 0 || l > LMAX) return fail(nullptr, UNOMOL_EINVAL, "shell angular momentum above 4 (g) is not supported (Basis.hpp:222)");
         if (b->shell_nprim[i] <= 0) return fail(nullptr, UNOMOL_EINVAL, "shell with no primitives");
+        if (b->shell_nprim[i] > 255) return fail(nullptr, UNOMOL_EINVAL, "shell with more than 255 primitives");
         if (b->shell_center[i] < 0 || b->shell_center[i] >= b->ncen) return fail(nullptr, UNOMOL_EINVAL, "shell centre out of range");
         if (b->shell_offset[i] != off) return fail(nullptr, UNOMOL_EINVAL, "shell offsets must follow shell order");
         ctx->sl.push_back(l);
@@ -832,6 +900,18 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
     CU(cudaMalloc(&ctx->d_sl, sizeof(int) * ctx->nshell));
     CU(cudaMemcpy(ctx->d_soff, ctx->soff.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(ctx->d_sl, ctx->sl.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
+    // the rest of the basis for the device setup (centres are uploaded by every setup)
+    CU(cudaMalloc(&ctx->d_snp, sizeof(int) * ctx->nshell));
+    CU(cudaMalloc(&ctx->d_scen, sizeof(int) * ctx->nshell));
+    CU(cudaMalloc(&ctx->d_sprim, sizeof(int) * ctx->nshell));
+    CU(cudaMalloc(&ctx->d_alpha, sizeof(double) * np));
+    CU(cudaMalloc(&ctx->d_coef, sizeof(double) * np));
+    CU(cudaMalloc(&ctx->d_centers, sizeof(double) * 3 * ctx->ncen));
+    CU(cudaMemcpy(ctx->d_snp, ctx->snp.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(ctx->d_scen, ctx->scen.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(ctx->d_sprim, ctx->sprim.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(ctx->d_alpha, ctx->alpha.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(ctx->d_coef, ctx->coef.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
     ctx->stats.nbf = ctx->nbf;
     int rc = build_setup(ctx);
     if (rc) {
@@ -968,6 +1048,13 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
     dfree(ctx->d_counters);
     dfree(ctx->d_soff);
     dfree(ctx->d_sl);
+    dfree(ctx->d_snp);
+    dfree(ctx->d_scen);
+    dfree(ctx->d_sprim);
+    dfree(ctx->d_alpha);
+    dfree(ctx->d_coef);
+    dfree(ctx->d_centers);
+    dfree(ctx->d_ws);
     for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
     dfree(ctx->d_rowbp);
     dfree(ctx->d_mseg);

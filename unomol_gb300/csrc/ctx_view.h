@@ -1,5 +1,6 @@
-// Internal: read-only view of a context's set-up (shell pairs, primitive pairs, block pairs, staircase
-// prefix sums, class launches), used to merge the work of many molecules into one batch.
+// Internal: read-only view of a context's set-up (device shell pairs, primitive pairs and staircase prefix
+// sums; host block pairs, blocks and class launches), used to merge the work of many molecules into one
+// batch and by the DPM integrals.
 #pragma once
 #include <vector>
 
@@ -18,10 +19,17 @@ struct ClassLaunchInfo {
 
 struct CtxView {
     int nbf = 0, nshell = 0, rys_compat = 1, eri_method = 0;
-    const std::vector<ShellPair>* pairs = nullptr;
-    const std::vector<PrimPair>* prims = nullptr;
-    const std::vector<BlockPair>* bps = nullptr;
-    const std::vector<long long>* prefix = nullptr;
+    const ShellPair* d_pairs = nullptr;  // device arrays of the setup
+    int npairs = 0;
+    const PrimPair* d_prims = nullptr;
+    long long nprims = 0;
+    const long long* d_prefix = nullptr;
+    long long nrows = 0;
+    const std::vector<BlockPair>* bps = nullptr;  // host: block pairs, blocks of equal (class, primitive pairs)
+    const std::vector<int>* block_begin = nullptr;
+    const std::vector<int>* block_count = nullptr;
+    const std::vector<int>* block_class = nullptr;
+    cudaStream_t stream = nullptr;  // the context's stream (its setup ran there)
     std::vector<ClassLaunchInfo> launches;
     NormTable nt{};
     const double* d_rys = nullptr;

@@ -17,6 +17,7 @@
 
 #include "../../include/unomol_gb300.h"
 #include "ctx_view.h"
+#include "fock_dispatch.cuh"
 
 namespace ugb {
 namespace {
@@ -67,9 +68,13 @@ using namespace ugb;
 extern "C" int unomol_gpu_gdpm(UnomolCtx* ctx, const double* q, double* H) {
     if (!ctx || !q || !H) return UNOMOL_EINVAL;
     const CtxView v = ctx_view(ctx);
-    const std::vector<ShellPair>& pairs = *v.pairs;
-    std::vector<PrimPair> prims = *v.prims;
-    const int gbegin = (int)prims.size();
+    for (int cls : *v.block_class)
+        if (pc_la(cls) > 2) {
+            g_dpm_err = "DPM integrals: shells above d are not supported";
+            return UNOMOL_EINVAL;
+        }
+    // the context's primitive pairs (on the device) followed by the six of the positron charge
+    std::vector<PrimPair> gp(GDPM_N);
     for (int k = 0; k < GDPM_N; ++k) {
         PrimPair g{};
         g.p = GDPM_ALF[k];
@@ -79,40 +84,40 @@ extern "C" int unomol_gpu_gdpm(UnomolCtx* ctx, const double* q, double* H) {
         g.cc = GDPM_COF[k];
         g.pf = (float)g.p;
         g.Ef = (float)g.E;
-        prims.push_back(g);
+        gp[k] = g;
     }
-    for (const ShellPair& sp : pairs)
-        if (sp.la > 2 || sp.lb > 2) {
-            g_dpm_err = "DPM integrals: shells above d are not supported";
-            return UNOMOL_EINVAL;
-        }
+    const int gbegin = (int)v.nprims;
     const long long no2 = (long long)v.nbf * (v.nbf + 1) / 2;
-    ShellPair* d_pairs = nullptr;
     PrimPair* d_prims = nullptr;
     double* d_out = nullptr;
-    cudaError_t e = cudaMalloc(&d_pairs, sizeof(ShellPair) * std::max<size_t>(1, pairs.size()));
-    if (e == cudaSuccess) e = cudaMalloc(&d_prims, sizeof(PrimPair) * prims.size());
+    cudaStream_t s = v.stream;
+    cudaError_t e = cudaMalloc(&d_prims, sizeof(PrimPair) * (v.nprims + GDPM_N));
     if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * std::max<long long>(1, no2));
-    if (e == cudaSuccess && !pairs.empty())
-        e = cudaMemcpy(d_pairs, pairs.data(), sizeof(ShellPair) * pairs.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_prims, prims.data(), sizeof(PrimPair) * prims.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(d_out, 0, sizeof(double) * std::max<long long>(1, no2));
-    // one launch per run of pairs of one class
-    for (size_t b = 0; e == cudaSuccess && b < pairs.size();) {
-        size_t en = b;
-        while (en < pairs.size() && pairs[en].la == pairs[b].la && pairs[en].lb == pairs[b].lb) ++en;
-        const int la = pairs[b].la, lb = pairs[b].lb, cnt = (int)(en - b);
-        if (la == 0) e = launch<0, 0>(d_pairs, (int)b, cnt, d_prims, gbegin, v, d_out, nullptr);
-        else if (la == 1 && lb == 0) e = launch<1, 0>(d_pairs, (int)b, cnt, d_prims, gbegin, v, d_out, nullptr);
-        else if (la == 1) e = launch<1, 1>(d_pairs, (int)b, cnt, d_prims, gbegin, v, d_out, nullptr);
-        else if (lb == 0) e = launch<2, 0>(d_pairs, (int)b, cnt, d_prims, gbegin, v, d_out, nullptr);
-        else if (lb == 1) e = launch<2, 1>(d_pairs, (int)b, cnt, d_prims, gbegin, v, d_out, nullptr);
-        else e = launch<2, 2>(d_pairs, (int)b, cnt, d_prims, gbegin, v, d_out, nullptr);
-        b = en;
+    if (e == cudaSuccess && v.nprims > 0)
+        e = cudaMemcpyAsync(d_prims, v.d_prims, sizeof(PrimPair) * v.nprims, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_prims + gbegin, gp.data(), sizeof(PrimPair) * GDPM_N, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(double) * std::max<long long>(1, no2), s);
+    // one launch per run of blocks of one class (pairs are sorted by class)
+    const std::vector<int>& bb = *v.block_begin;
+    const std::vector<int>& bn = *v.block_count;
+    const std::vector<int>& bc = *v.block_class;
+    for (size_t k = 0; e == cudaSuccess && k < bc.size();) {
+        size_t k2 = k;
+        while (k2 < bc.size() && bc[k2] == bc[k]) ++k2;
+        const int begin = bb[k], cnt = bb[k2 - 1] + bn[k2 - 1] - begin;
+        const int la = pc_la(bc[k]), lb = pc_lb(bc[k]);
+        if (la == 0) e = launch<0, 0>(v.d_pairs, begin, cnt, d_prims, gbegin, v, d_out, s);
+        else if (la == 1 && lb == 0) e = launch<1, 0>(v.d_pairs, begin, cnt, d_prims, gbegin, v, d_out, s);
+        else if (la == 1) e = launch<1, 1>(v.d_pairs, begin, cnt, d_prims, gbegin, v, d_out, s);
+        else if (lb == 0) e = launch<2, 0>(v.d_pairs, begin, cnt, d_prims, gbegin, v, d_out, s);
+        else if (lb == 1) e = launch<2, 1>(v.d_pairs, begin, cnt, d_prims, gbegin, v, d_out, s);
+        else e = launch<2, 2>(v.d_pairs, begin, cnt, d_prims, gbegin, v, d_out, s);
+        k = k2;
     }
     std::vector<double> out((size_t)std::max<long long>(1, no2));
-    if (e == cudaSuccess) e = cudaMemcpy(out.data(), d_out, sizeof(double) * no2, cudaMemcpyDeviceToHost);
-    cudaFree(d_pairs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), d_out, sizeof(double) * no2, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(d_prims);
     cudaFree(d_out);
     if (e != cudaSuccess) {

@@ -3,6 +3,7 @@
 // and an autotuner choosing the CTA size (quartets per tile) and the CTAs per SM of every class.
 // FP64, RHF, shells up to d (the batch workload is s/p).
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -10,6 +11,7 @@
 #include "../../include/unomol_gb300.h"
 #include "ctx_view.h"
 #include "fock_dispatch.cuh"
+#include "setup.h"
 
 using namespace ugb;
 
@@ -186,10 +188,10 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
         unomol_gpu_batch_destroy(b);
         return rc;
     };
-    std::vector<ShellPair> pairs;
-    std::vector<PrimPair> prims;
-    std::vector<long long> prefix;
     std::vector<std::vector<BlockPair>> per_class(NTMPLCLASS * NTMPLCLASS);
+    std::vector<int> pair0s, prim0s;
+    std::vector<long long> row0s;
+    long long npair_tot = 0, nprim_tot = 0, nrow_tot = 0;
     long long dense = 0, packed = 0;
     for (int m = 0; m < nmol; ++m) {
         UnomolCtx* c = nullptr;
@@ -205,14 +207,13 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
             b->rys = v.d_rys;
             b->rys_compat = v.rys_compat;
         }
-        const int pair0 = (int)pairs.size(), prim0 = (int)prims.size(), pre0 = (int)prefix.size();
-        for (ShellPair sp : *v.pairs) {
-            sp.prim_begin += prim0;
-            sp.pad = m;
-            pairs.push_back(sp);
+        if (npair_tot + v.npairs >= INT_MAX || nprim_tot + v.nprims >= INT_MAX || nrow_tot + v.nrows >= INT_MAX) {
+            bfail(b, UNOMOL_EINVAL, "batched build: too many shell pairs for one batch");
+            return cleanup(UNOMOL_EINVAL);
         }
-        prims.insert(prims.end(), v.prims->begin(), v.prims->end());
-        prefix.insert(prefix.end(), v.prefix->begin(), v.prefix->end());
+        pair0s.push_back((int)npair_tot);
+        prim0s.push_back((int)nprim_tot);
+        row0s.push_back(nrow_tot);
         for (const ClassLaunchInfo& L : v.launches) {
             if (L.bc >= NTMPLCLASS || L.kc >= NTMPLCLASS) {
                 bfail(b, UNOMOL_EINVAL, "batched build: shells above d are not supported");
@@ -220,12 +221,15 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
             }
             for (int k = 0; k < L.nbp; ++k) {
                 BlockPair bp = (*v.bps)[L.bp_begin + k];
-                bp.bra_begin += pair0;
-                bp.ket_begin += pair0;
-                bp.prefix_off += pre0;
+                bp.bra_begin += (int)npair_tot;
+                bp.ket_begin += (int)npair_tot;
+                bp.prefix_off += (int)nrow_tot;
                 per_class[L.bc * NTMPLCLASS + L.kc].push_back(bp);
             }
         }
+        npair_tot += v.npairs;
+        nprim_tot += v.nprims;
+        nrow_tot += v.nrows;
         b->nbf.push_back(v.nbf);
         b->doff.push_back(dense);
         b->poff.push_back(packed);
@@ -257,10 +261,24 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
     BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-    BCU(cudaMalloc(&b->d_pairs, sizeof(ShellPair) * std::max<size_t>(1, pairs.size())));
-    BCU(cudaMalloc(&b->d_prims, sizeof(PrimPair) * std::max<size_t>(1, prims.size())));
+    BCU(cudaMalloc(&b->d_pairs, sizeof(ShellPair) * std::max<long long>(1, npair_tot)));
+    BCU(cudaMalloc(&b->d_prims, sizeof(PrimPair) * std::max<long long>(1, nprim_tot)));
     BCU(cudaMalloc(&b->d_bps, sizeof(BlockPair) * std::max<size_t>(1, bps.size())));
-    BCU(cudaMalloc(&b->d_prefix, sizeof(long long) * std::max<size_t>(1, prefix.size())));
+    BCU(cudaMalloc(&b->d_prefix, sizeof(long long) * std::max<long long>(1, nrow_tot)));
+    // the molecules' device set-ups side by side: pairs point into the merged primitive array and carry
+    // their molecule; prefix sums are relative to their block pair and copy unchanged
+    for (int m = 0; m < nmol; ++m) {
+        const CtxView v = ctx_view(b->mols[m]);
+        if (v.npairs > 0) {
+            BCU(cudaMemcpyAsync(b->d_pairs + pair0s[m], v.d_pairs, sizeof(ShellPair) * v.npairs, cudaMemcpyDeviceToDevice, b->stream));
+            BCU(setup_offset_pairs(b->d_pairs + pair0s[m], v.npairs, prim0s[m], m, b->stream));
+        }
+        if (v.nprims > 0)
+            BCU(cudaMemcpyAsync(b->d_prims + prim0s[m], v.d_prims, sizeof(PrimPair) * v.nprims, cudaMemcpyDeviceToDevice, b->stream));
+        if (v.nrows > 0)
+            BCU(cudaMemcpyAsync(b->d_prefix + row0s[m], v.d_prefix, sizeof(long long) * v.nrows, cudaMemcpyDeviceToDevice, b->stream));
+    }
+    BCU(cudaStreamSynchronize(b->stream));
     BCU(cudaMalloc(&b->d_nbf, sizeof(int) * nmol));
     BCU(cudaMalloc(&b->d_doff, sizeof(long long) * nmol));
     BCU(cudaMalloc(&b->d_poff, sizeof(long long) * nmol));
@@ -269,10 +287,7 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
     BCU(cudaMalloc(&b->d_Pfull, sizeof(double) * dense));
     BCU(cudaMalloc(&b->d_T, sizeof(double) * dense));
     BCU(cudaMalloc(&b->d_tiles, sizeof(unsigned long long) * std::max<size_t>(1, b->launches.size())));
-    BCU(cudaMemcpy(b->d_pairs, pairs.data(), sizeof(ShellPair) * pairs.size(), cudaMemcpyHostToDevice));
-    BCU(cudaMemcpy(b->d_prims, prims.data(), sizeof(PrimPair) * prims.size(), cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->d_bps, bps.data(), sizeof(BlockPair) * bps.size(), cudaMemcpyHostToDevice));
-    BCU(cudaMemcpy(b->d_prefix, prefix.data(), sizeof(long long) * prefix.size(), cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->d_nbf, b->nbf.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->d_doff, b->doff.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->d_poff, b->poff.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice));
