@@ -58,6 +58,15 @@ struct UnomolCtx {
     double *d_alpha = nullptr, *d_coef = nullptr, *d_centers = nullptr;
     char* d_ws = nullptr;
     size_t ws_bytes = 0;
+    // device memory in four allocations: the basis (status flag, shell arrays, exponents, coefficients,
+    // centres); the pair records (ShellPair, PrimPair, PrimPair32); the work lists (block pairs,
+    // staircase prefix sums, per-build row lists); the setup's scratch (d_ws).  The arrays below point
+    // into them; the pair and list allocations are kept while the next setup fits.
+    char* d_basis = nullptr;
+    char* d_setup = nullptr;
+    size_t setup_bytes = 0;
+    char* d_lists = nullptr;
+    size_t lists_bytes = 0;
     // per-build work lists of the density-screened / mixed-precision build
     int *d_rowbp = nullptr, *d_mseg = nullptr;
     long long *d_c64 = nullptr, *d_c32 = nullptr, *d_pre64 = nullptr, *d_pre32 = nullptr;
@@ -154,35 +163,37 @@ double flops_per_quartet(int la, int lb, int lc, int ld) {
     return 17.0 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
 }
 
-void free_setup(UnomolCtx* c) {
-    dfree(c->d_pairs);
-    dfree(c->d_prims);
-    dfree(c->d_prims32);
-    dfree(c->d_bps);
-    dfree(c->d_prefix);
-}
-
-// Bump allocation of the setup's scratch arrays in one device buffer (256-byte aligned pieces); a pass
-// with no buffer only adds up the sizes.
+// Bump allocation of several arrays in one device buffer (256-byte aligned pieces); a pass with no
+// buffer only adds up the sizes (and gives the offsets).
 struct Carve {
     char* base = nullptr;
     size_t used = 0;
+    size_t next(size_t bytes) {
+        const size_t off = (used + 255) & ~size_t(255);
+        used = off + std::max<size_t>(bytes, 1);
+        return off;
+    }
     template <typename T>
     T* take(size_t n) {
-        const size_t off = (used + 255) & ~size_t(255);
-        used = off + sizeof(T) * std::max<size_t>(n, 1);
+        const size_t off = next(sizeof(T) * n);
         return base ? reinterpret_cast<T*>(base + off) : nullptr;
     }
 };
 
-int ensure_ws(UnomolCtx* ctx, size_t bytes) {
-    if (bytes <= ctx->ws_bytes) return UNOMOL_OK;
-    CU(cudaStreamSynchronize(ctx->stream));  // nothing may still use the old buffer
-    dfree(ctx->d_ws);
-    ctx->ws_bytes = 0;
-    CU(cudaMalloc(&ctx->d_ws, bytes));
-    ctx->ws_bytes = bytes;
+// One allocation of at least `bytes`, kept while it is large enough.  Callers make sure that no work
+// still reads the old buffer (cudaFree would wait for the whole device anyway).
+int ensure_arena(UnomolCtx* ctx, char*& buf, size_t& cap, size_t bytes) {
+    if (buf && bytes <= cap) return UNOMOL_OK;
+    dfree(buf);
+    cap = 0;
+    CU(cudaMalloc(&buf, bytes));
+    cap = bytes;
     return UNOMOL_OK;
+}
+
+int ensure_ws(UnomolCtx* ctx, size_t bytes) {
+    if (bytes > ctx->ws_bytes) CU(cudaStreamSynchronize(ctx->stream));  // nothing may still use the old scratch
+    return ensure_arena(ctx, ctx->d_ws, ctx->ws_bytes, bytes);
 }
 
 ShellsDev shells_dev(const UnomolCtx* ctx) {
@@ -204,13 +215,9 @@ ShellsDev shells_dev(const UnomolCtx* ctx) {
 // of blocks), the staircase of every bra row on the device, one read-back of the per-block-pair totals.
 int build_worklists(UnomolCtx* ctx) {
     cudaStream_t s = ctx->stream;
+    CU(cudaDeviceSynchronize());  // builds still in flight (on any stream) read the lists rewritten here
     ctx->bps.clear();
     ctx->launches.clear();
-    dfree(ctx->d_bps);
-    dfree(ctx->d_prefix);
-    for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
-    dfree(ctx->d_rowbp);
-    dfree(ctx->d_mseg);
     const int nb = (int)ctx->block_begin.size();
     std::vector<BlockPair> all;
     std::vector<int> all_x, all_y;
@@ -254,7 +261,28 @@ int build_worklists(UnomolCtx* ctx) {
     Carve w;
     w.base = ctx->d_ws;
     carve(w, d_all, S, totals, tmp);
-    CU(cudaMalloc(&ctx->d_prefix, sizeof(long long) * std::max<long long>(1, nrows)));
+    // the lists allocation, sized for every block pair being non-empty
+    {
+        auto lists = [&](Carve& c) {
+            ctx->d_bps = c.take<BlockPair>(nall);
+            ctx->d_cnt64 = c.take<long long>(nall);
+            ctx->d_cnt32 = c.take<long long>(nall);
+            ctx->d_prefix = c.take<long long>(nrows);
+            ctx->d_c64 = c.take<long long>(nrows);
+            ctx->d_c32 = c.take<long long>(nrows);
+            ctx->d_pre64 = c.take<long long>(nrows);
+            ctx->d_pre32 = c.take<long long>(nrows);
+            ctx->d_rowbp = c.take<int>(nrows);
+            ctx->d_mseg = c.take<int>(nrows);
+        };
+        Carve lay;
+        lists(lay);
+        rc = ensure_arena(ctx, ctx->d_lists, ctx->lists_bytes, lay.used);
+        if (rc) return rc;
+        Carve c;
+        c.base = ctx->d_lists;
+        lists(c);
+    }
     std::vector<long long> tot(nall);
     if (nall > 0) {
         CU(cudaMemcpyAsync(d_all, all.data(), sizeof(BlockPair) * nall, cudaMemcpyHostToDevice, s));
@@ -304,18 +332,12 @@ int build_worklists(UnomolCtx* ctx) {
     ctx->stats.function_quartets = fq;
     if (!ctx->bps.empty()) {
         const size_t nbp = ctx->bps.size();
-        CU(cudaMalloc(&ctx->d_bps, sizeof(BlockPair) * nbp));
         CU(cudaMemcpyAsync(ctx->d_bps, ctx->bps.data(), sizeof(BlockPair) * nbp, cudaMemcpyHostToDevice, s));
         // row -> block pair map (-1 on the end-of-block-pair entries and on the rows of empty block pairs)
         // and the per-build work-list buffers of the density-screened build
         const size_t nr = (size_t)nrows;
-        CU(cudaMalloc(&ctx->d_rowbp, sizeof(int) * nr));
         CU(cudaMemsetAsync(ctx->d_rowbp, 0xff, sizeof(int) * nr, s));
         CU(setup_row_bp(ctx->d_bps, (int)nbp, ctx->d_rowbp, s));
-        CU(cudaMalloc(&ctx->d_mseg, sizeof(int) * nr));
-        for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32}) CU(cudaMalloc(p, sizeof(long long) * nr));
-        CU(cudaMalloc(&ctx->d_cnt64, sizeof(long long) * nbp));
-        CU(cudaMalloc(&ctx->d_cnt32, sizeof(long long) * nbp));
         CU(cudaMemsetAsync(ctx->d_c64, 0, sizeof(long long) * nr, s));
         CU(cudaMemsetAsync(ctx->d_c32, 0, sizeof(long long) * nr, s));
         CU(cudaMemsetAsync(ctx->d_mseg, 0, sizeof(int) * nr, s));
@@ -326,8 +348,8 @@ int build_worklists(UnomolCtx* ctx) {
 
 // Pairs, Schwarz bounds, block structure and work lists for the current geometry, built on the device.
 int build_setup(UnomolCtx* ctx) {
-    free_setup(ctx);
     cudaStream_t s = ctx->stream;
+    CU(cudaDeviceSynchronize());  // builds still in flight (on any stream) read the pairs rewritten here
     const int ns = ctx->nshell;
     const long long np64 = (long long)ns * (ns + 1) / 2;
     if (np64 > (1ll << 28)) return fail(ctx, UNOMOL_EINVAL, "too many shell pairs for one context");
@@ -341,9 +363,20 @@ int build_setup(UnomolCtx* ctx) {
     ctx->nprims = nprims;
     ctx->stats.npairs = P;
     CU(cudaMemcpyAsync(ctx->d_centers, ctx->centers.data(), sizeof(double) * 3 * ctx->ncen, cudaMemcpyHostToDevice, s));
-    CU(cudaMalloc(&ctx->d_pairs, sizeof(ShellPair) * P));
-    CU(cudaMalloc(&ctx->d_prims, sizeof(PrimPair) * nprims));
-    CU(cudaMalloc(&ctx->d_prims32, sizeof(PrimPair32) * nprims));
+    {
+        auto recs = [&](Carve& c) {
+            ctx->d_pairs = c.take<ShellPair>(P);
+            ctx->d_prims = c.take<PrimPair>(nprims);
+            ctx->d_prims32 = c.take<PrimPair32>(nprims);
+        };
+        Carve lay;
+        recs(lay);
+        const int rc = ensure_arena(ctx, ctx->d_setup, ctx->setup_bytes, lay.used);
+        if (rc) return rc;
+        Carve c;
+        c.base = ctx->d_setup;
+        recs(c);
+    }
     // library scratch sizes (the segmented sort's for the largest possible number of blocks)
     size_t t_scan = 0, t_sort = 0, t_rle = 0, t_seg = 0;
     CU(setup_exclusive_sum(nullptr, t_scan, nullptr, nullptr, P, s));
@@ -818,6 +851,64 @@ CtxView ctx_view(const UnomolCtx* c) {
 
 }  // namespace ugb
 
+namespace {
+
+// The Rys tables of every context on one device: file-scope device arrays of the library's image,
+// filled once per device (rows re-laid with the padded strides of the kernels, zeros in the padding:
+// 16-byte loads), then the large-T limits.
+constexpr int RYS64_LEN = rys_table_len(RysStride<double>::value);
+constexpr int RYS32_LEN = rys_table_len(RysStride<float>::value);
+static __device__ __align__(16) double g_rys64[RYS64_LEN];
+static __device__ __align__(16) float g_rys32[RYS32_LEN];
+constexpr int RYS_MAX_DEVICES = 64;
+double* g_rys64_ptr[RYS_MAX_DEVICES] = {nullptr};
+float* g_rys32_ptr[RYS_MAX_DEVICES] = {nullptr};
+std::mutex g_rys_mu;
+
+int rys_tables(int dev, double*& d64, float*& d32, std::string& err) {
+    static_assert(rys_table_len(RYS_DEG + 1) == RYS_TABLE_SIZE + 50, "layout of rys_tables.inc");
+    static_assert(rys_table_len(RYS32_DEG + 1) == RYS32_TABLE_SIZE + 50, "layout of rys_tables.inc");
+    if (dev < 0 || dev >= RYS_MAX_DEVICES) {
+        err = "device index out of range";
+        return UNOMOL_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(g_rys_mu);
+    if (!g_rys64_ptr[dev]) {
+        constexpr int S64 = RysStride<double>::value, S32 = RysStride<float>::value;
+        std::vector<double> t64(RYS64_LEN, 0.0);
+        std::vector<float> t32(RYS32_LEN, 0.f);
+        const int rows = RYS_TABLE_SIZE / (RYS_DEG + 1);
+        for (int r = 0; r < rows; ++r) {
+            for (int d = 0; d <= RYS_DEG; ++d) t64[(size_t)r * S64 + d] = RYS_TABLE_H[(size_t)r * (RYS_DEG + 1) + d];
+            for (int d = 0; d <= RYS32_DEG; ++d) t32[(size_t)r * S32 + d] = RYS32_TABLE_H[(size_t)r * (RYS32_DEG + 1) + d];
+        }
+        const size_t h64 = t64.size() - 50, h32 = t32.size() - 50;
+        for (int n = 0; n < 5; ++n)
+            for (int i = 0; i < 5; ++i) {
+                t64[h64 + n * 5 + i] = RYS_HERMITE_X_H[n][i];
+                t64[h64 + 25 + n * 5 + i] = RYS_HERMITE_W_H[n][i];
+                t32[h32 + n * 5 + i] = (float)RYS_HERMITE_X_H[n][i];
+                t32[h32 + 25 + n * 5 + i] = (float)RYS_HERMITE_W_H[n][i];
+            }
+        void *p64 = nullptr, *p32 = nullptr;
+        cudaError_t e = cudaMemcpyToSymbol(g_rys64, t64.data(), sizeof(double) * t64.size());
+        if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_rys32, t32.data(), sizeof(float) * t32.size());
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&p64, g_rys64);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&p32, g_rys32);
+        if (e != cudaSuccess) {
+            err = std::string("Rys tables: ") + cudaGetErrorString(e);
+            return UNOMOL_ECUDA;
+        }
+        g_rys64_ptr[dev] = static_cast<double*>(p64);
+        g_rys32_ptr[dev] = static_cast<float*>(p32);
+    }
+    d64 = g_rys64_ptr[dev];
+    d32 = g_rys32_ptr[dev];
+    return UNOMOL_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* unomol_gpu_version(void) { return "unomol_gb300 0.1 (sm_103a)"; }
@@ -868,50 +959,42 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
     CU(cudaGetDevice(&ctx->dev));
     CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
-    // Rys tables (polynomial blocks, then the large-T limit)
     {
-        // rows re-laid with the padded strides of the device (16-byte loads), zeros in the padding
-        constexpr int S64 = RysStride<double>::value, S32 = RysStride<float>::value;
-        static_assert(rys_table_len(RYS_DEG + 1) == RYS_TABLE_SIZE + 50, "layout of rys_tables.inc");
-        static_assert(rys_table_len(RYS32_DEG + 1) == RYS32_TABLE_SIZE + 50, "layout of rys_tables.inc");
-        std::vector<double> t64(rys_table_len(S64), 0.0);
-        std::vector<float> t32(rys_table_len(S32), 0.f);
-        const int rows = RYS_TABLE_SIZE / (RYS_DEG + 1);
-        for (int r = 0; r < rows; ++r) {
-            for (int d = 0; d <= RYS_DEG; ++d) t64[(size_t)r * S64 + d] = RYS_TABLE_H[(size_t)r * (RYS_DEG + 1) + d];
-            for (int d = 0; d <= RYS32_DEG; ++d) t32[(size_t)r * S32 + d] = RYS32_TABLE_H[(size_t)r * (RYS32_DEG + 1) + d];
-        }
-        const size_t h64 = t64.size() - 50, h32 = t32.size() - 50;
-        for (int n = 0; n < 5; ++n)
-            for (int i = 0; i < 5; ++i) {
-                t64[h64 + n * 5 + i] = RYS_HERMITE_X_H[n][i];
-                t64[h64 + 25 + n * 5 + i] = RYS_HERMITE_W_H[n][i];
-                t32[h32 + n * 5 + i] = (float)RYS_HERMITE_X_H[n][i];
-                t32[h32 + 25 + n * 5 + i] = (float)RYS_HERMITE_W_H[n][i];
-            }
-        CU(cudaMalloc(&ctx->d_rys, sizeof(double) * t64.size()));
-        CU(cudaMalloc(&ctx->d_rys32, sizeof(float) * t32.size()));
-        CU(cudaMemcpy(ctx->d_rys, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(ctx->d_rys32, t32.data(), sizeof(float) * t32.size(), cudaMemcpyHostToDevice));
+        const int rc = rys_tables(ctx->dev, ctx->d_rys, ctx->d_rys32, ctx->err);
+        if (rc) return fail(nullptr, rc, ctx->err);
     }
-    CU(cudaMalloc(&ctx->d_status, sizeof(int)));
-    CU(cudaMemset(ctx->d_status, 0, sizeof(int)));
-    CU(cudaMalloc(&ctx->d_soff, sizeof(int) * ctx->nshell));
-    CU(cudaMalloc(&ctx->d_sl, sizeof(int) * ctx->nshell));
-    CU(cudaMemcpy(ctx->d_soff, ctx->soff.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(ctx->d_sl, ctx->sl.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
-    // the rest of the basis for the device setup (centres are uploaded by every setup)
-    CU(cudaMalloc(&ctx->d_snp, sizeof(int) * ctx->nshell));
-    CU(cudaMalloc(&ctx->d_scen, sizeof(int) * ctx->nshell));
-    CU(cudaMalloc(&ctx->d_sprim, sizeof(int) * ctx->nshell));
-    CU(cudaMalloc(&ctx->d_alpha, sizeof(double) * np));
-    CU(cudaMalloc(&ctx->d_coef, sizeof(double) * np));
-    CU(cudaMalloc(&ctx->d_centers, sizeof(double) * 3 * ctx->ncen));
-    CU(cudaMemcpy(ctx->d_snp, ctx->snp.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(ctx->d_scen, ctx->scen.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(ctx->d_sprim, ctx->sprim.data(), sizeof(int) * ctx->nshell, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(ctx->d_alpha, ctx->alpha.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(ctx->d_coef, ctx->coef.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    // the basis in one allocation (status flag, shell arrays, exponents, coefficients, centres), from a
+    // host image of the same layout
+    {
+        const int ns = ctx->nshell;
+        Carve lay;
+        const size_t o_status = lay.next(sizeof(int)), o_soff = lay.next(sizeof(int) * ns), o_sl = lay.next(sizeof(int) * ns),
+                     o_snp = lay.next(sizeof(int) * ns), o_scen = lay.next(sizeof(int) * ns),
+                     o_sprim = lay.next(sizeof(int) * ns), o_alpha = lay.next(sizeof(double) * np),
+                     o_coef = lay.next(sizeof(double) * np), o_cen = lay.next(sizeof(double) * 3 * ctx->ncen);
+        std::vector<char> img(lay.used, 0);
+        auto put = [&](size_t off, const void* src, size_t bytes) { std::memcpy(img.data() + off, src, bytes); };
+        put(o_soff, ctx->soff.data(), sizeof(int) * ns);
+        put(o_sl, ctx->sl.data(), sizeof(int) * ns);
+        put(o_snp, ctx->snp.data(), sizeof(int) * ns);
+        put(o_scen, ctx->scen.data(), sizeof(int) * ns);
+        put(o_sprim, ctx->sprim.data(), sizeof(int) * ns);
+        put(o_alpha, ctx->alpha.data(), sizeof(double) * np);
+        put(o_coef, ctx->coef.data(), sizeof(double) * np);
+        put(o_cen, ctx->centers.data(), sizeof(double) * 3 * ctx->ncen);
+        CU(cudaMalloc(&ctx->d_basis, img.size()));
+        CU(cudaMemcpy(ctx->d_basis, img.data(), img.size(), cudaMemcpyHostToDevice));
+        char* base = ctx->d_basis;
+        ctx->d_status = reinterpret_cast<int*>(base + o_status);
+        ctx->d_soff = reinterpret_cast<int*>(base + o_soff);
+        ctx->d_sl = reinterpret_cast<int*>(base + o_sl);
+        ctx->d_snp = reinterpret_cast<int*>(base + o_snp);
+        ctx->d_scen = reinterpret_cast<int*>(base + o_scen);
+        ctx->d_sprim = reinterpret_cast<int*>(base + o_sprim);
+        ctx->d_alpha = reinterpret_cast<double*>(base + o_alpha);
+        ctx->d_coef = reinterpret_cast<double*>(base + o_coef);
+        ctx->d_centers = reinterpret_cast<double*>(base + o_cen);
+    }
     ctx->stats.nbf = ctx->nbf;
     int rc = build_setup(ctx);
     if (rc) {
@@ -1032,9 +1115,10 @@ int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, doub
 void unomol_gpu_destroy(UnomolCtx* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    free_setup(ctx);
-    dfree(ctx->d_rys);
-    dfree(ctx->d_rys32);
+    dfree(ctx->d_basis);
+    dfree(ctx->d_setup);
+    dfree(ctx->d_lists);
+    dfree(ctx->d_ws);
     dfree(ctx->d_Pa);
     dfree(ctx->d_Pb);
     dfree(ctx->d_Ta);
@@ -1044,20 +1128,7 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
     dfree(ctx->d_pk_a);
     dfree(ctx->d_pk_b);
     dfree(ctx->d_pmax);
-    dfree(ctx->d_status);
     dfree(ctx->d_counters);
-    dfree(ctx->d_soff);
-    dfree(ctx->d_sl);
-    dfree(ctx->d_snp);
-    dfree(ctx->d_scen);
-    dfree(ctx->d_sprim);
-    dfree(ctx->d_alpha);
-    dfree(ctx->d_coef);
-    dfree(ctx->d_centers);
-    dfree(ctx->d_ws);
-    for (long long** p : {&ctx->d_c64, &ctx->d_c32, &ctx->d_pre64, &ctx->d_pre32, &ctx->d_cnt64, &ctx->d_cnt32}) dfree(*p);
-    dfree(ctx->d_rowbp);
-    dfree(ctx->d_mseg);
     dfree(ctx->d_dmax);
     dfree(ctx->d_Pa32);
     dfree(ctx->d_Pb32);

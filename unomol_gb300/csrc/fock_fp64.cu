@@ -38,7 +38,7 @@ static cudaError_t schwarz_one(const ShellPair* pairs, const PrimPair* prims, in
     if (count <= 0) return cudaSuccess;
     constexpr int NAB = ncart(pc_la(PC)) * ncart(pc_lb(PC));
     if constexpr (NAB * NAB <= 81)
-        schwarz_kernel<pc_la(PC), pc_lb(PC)><<<(count + 127) / 128, 128, 0, s>>>(pairs, prims, begin, count, nt, rys, q);
+        schwarz_kernel<pc_la(PC), pc_lb(PC)><<<(unsigned)(((long long)count * 32 + 127) / 128), 128, 0, s>>>(pairs, prims, begin, count, nt, rys, q);
     else
         schwarz_generic<<<(count + 63) / 64, 64, 0, s>>>(pairs, prims, begin, count, nt, rys, q);
     return cudaGetLastError();

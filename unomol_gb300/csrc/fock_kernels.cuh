@@ -196,12 +196,15 @@ struct QClass {
 };
 
 // Contracted integrals (ab|cd) of one shell quartet, without the component normalisation factors,
-// accumulated into acc[NF] (function quartet f = ((ia*NB + ib)*NC + ic)*ND + id).
+// accumulated into acc[NF] (function quartet f = ((ia*NB + ib)*NC + ic)*ND + id).  With nparts > 1 only
+// the primitive quartets t = part, part + nparts, ... (bra-major) are summed: the caller's threads
+// split one shell quartet and add their partial sums afterwards.
 template <int LA, int LB, int LC, int LD, typename R, typename PP>
 __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const ShellPair& ket,
                                                   const PP* __restrict__ prims,
                                                   const R* __restrict__ rys, R prim_cut, bool compat,
-                                                  R (&acc)[QClass<LA, LB, LC, LD>::NF], unsigned* npass = nullptr) {
+                                                  R (&acc)[QClass<LA, LB, LC, LD>::NF], unsigned* npass = nullptr,
+                                                  int part = 0, int nparts = 1) {
     using Q = QClass<LA, LB, LC, LD>;
     constexpr int NR = Q::NR;
 #pragma unroll
@@ -252,6 +255,18 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
                         }
         }
     };
+    if (nparts > 1) {
+        for (int t = part; t < nb * nk; t += nparts) {
+            const int ib = t / nk, ik = t - ib * nk;
+            const PP bp = pb[ib];
+            const PP kp = pk[ik];
+            const R rs = rsqrt(bp.p + kp.p);
+            const R sr = R(SRTERM) * bp.E * kp.E * rs;
+            if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
+            primitive(bp, kp, rs, sr);
+        }
+        return;
+    }
     if constexpr (sizeof(R) == 8) {
         // FP64: each lane walks its primitive quartets (bra-major, as the reference) and first looks
         // ahead for the next one past the prefactor screen (TwoElectronInts.cpp:478-479), with an FP32
@@ -588,27 +603,32 @@ __global__ void __launch_bounds__(256) fock_jk_persistent(const FockArgs A, cons
 }
 
 // Schwarz diagonal: q[pair] = sqrt(max_{a,b} |(ab|ab)|) for every pair of one class (no primitive
-// cut, so the bound is that of the exact integrals).
+// cut, so the bound is that of the exact integrals).  One warp per shell pair: the lanes split its
+// primitive quartets and add their partial integrals with warp shuffles (one thread per pair would
+// leave most SMs idle at these counts and serialise each warp on the FP64 pipe).
 template <int LA, int LB>
 __global__ void __launch_bounds__(128) schwarz_kernel(const ShellPair* __restrict__ pairs, const PrimPair* __restrict__ prims,
                                                       int begin, int count, const NormTable nt,
                                                       const double* __restrict__ rys, double* __restrict__ q_out) {
     using Q = QClass<LA, LB, LA, LB>;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count) return;
-    const ShellPair sp = pairs[begin + t];
+    const int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= count) return;  // whole warps: count is per warp
+    const ShellPair sp = pairs[begin + w];
     double acc[Q::NF];
-    shell_quartet_eri<LA, LB, LA, LB, double, PrimPair>(sp, sp, prims, rys, 0.0, false, acc);
+    shell_quartet_eri<LA, LB, LA, LB, double, PrimPair>(sp, sp, prims, rys, 0.0, false, acc, nullptr, lane, 32);
     double m = 0.0;
 #pragma unroll
     for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
         for (int ib = 0; ib < Q::NB; ++ib) {
             const int f = ((ia * Q::NB + ib) * Q::NC + ia) * Q::ND + ib;
+            double v = acc[f];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             const double n = nt.v[LA][ia] * nt.v[LB][ib];
-            m = fmax(m, fabs(acc[f]) * n * n);
+            m = fmax(m, fabs(v) * n * n);
         }
-    q_out[begin + t] = sqrt(m);
+    if (lane == 0) q_out[begin + w] = sqrt(m);
 }
 
 }  // namespace ugb

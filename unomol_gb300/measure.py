@@ -21,6 +21,11 @@
         the grid point after point (one context recalculated per point) against all points as one
         batched SCF whose iterations replay as a CUDA graph.
 
+    python -m unomol_gb300.measure setup [--reps 5] [--out setup.json]
+        Wall time of the device set-up (shell pairs, primitive pairs, sorts, Schwarz diagonal, staircase
+        work lists): create and the best of `reps` recalculates of one context for n-decane, 32 and 64
+        waters (6-31G), and the creation of the 256-molecule batch.
+
     python -m unomol_gb300.measure sweep [--out sweep.json]
         FP32 cutoff sweep of the precision form on the 32-water 6-31G cluster (molecules.water_cluster(32, 0),
         superposition-of-fragments guess, DIIS, 1e-10 Eh): the incremental mixed-precision SCF against the
@@ -236,15 +241,46 @@ def _dpm(npts: int) -> dict:
             "vpol_range": [float(min(x["vpol"] for x in seq)), float(max(x["vpol"] for x in seq))]}
 
 
+def _setup(reps: int) -> dict:
+    """Wall time of the device set-up (create, recalculate) on three clusters and of the batch create."""
+    import time
+    cases = [("n-decane/6-31G", molecules.patin_text(molecules.alkane(10), "6-31G")),
+             ("32 waters/6-31G", molecules.patin_text(molecules.water_cluster(32, 0), "6-31G")),
+             ("64 waters/6-31G (13 A box)", molecules.patin_text(molecules.water_cluster(64, 0, box=13.0), "6-31G"))]
+    native.TwoElectronInts(Basis(text=cases[0][1])).close()  # first use: module loading stays out
+    out = {"contexts": []}
+    for name, text in cases:
+        b = Basis(text=text)
+        t0 = time.perf_counter()
+        t = native.TwoElectronInts(b)
+        create = time.perf_counter() - t0
+        rec = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            t.recalculate(b)
+            rec.append(time.perf_counter() - t0)
+        st = t.stats()
+        t.close()
+        out["contexts"].append({"system": name, "nbf": b.norb, "shell_pairs": st["npairs"],
+                                "create_ms": 1e3 * create, "recalculate_ms": 1e3 * min(rec)})
+    bases = [Basis(text=x) for _, x in molecules.batch_workload(seed=0)]
+    t0 = time.perf_counter()
+    bat = native.Batch(bases)
+    out["batch_create_ms"] = 1e3 * (time.perf_counter() - t0)
+    out["batch_molecules"] = len(bases)
+    bat.close()
+    return out
+
+
 def main():
-    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM / DPM measurements")
-    ap.add_argument("what", choices=["batch", "sweep", "gemm", "dpm"])
+    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM / DPM / set-up measurements")
+    ap.add_argument("what", choices=["batch", "sweep", "gemm", "dpm", "setup"])
     ap.add_argument("--points", type=int, default=64)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
     rep = (_batch(a.reps) if a.what == "batch" else _sweep() if a.what == "sweep" else
-           _gemm(max(a.reps, 10)) if a.what == "gemm" else _dpm(a.points))
+           _gemm(max(a.reps, 10)) if a.what == "gemm" else _setup(a.reps) if a.what == "setup" else _dpm(a.points))
     print(json.dumps(rep, indent=1))
     if a.out:
         with open(a.out, "w") as f:
