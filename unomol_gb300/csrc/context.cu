@@ -907,6 +907,50 @@ int rys_tables(int dev, double*& d64, float*& d32, std::string& err) {
     return UNOMOL_OK;
 }
 
+// Stream, events, Rys tables, the basis on the device and the first set-up of a new context.
+int init_device(UnomolCtx* ctx, int np) {
+    CU(cudaGetDevice(&ctx->dev));
+    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
+    {
+        const int rc = rys_tables(ctx->dev, ctx->d_rys, ctx->d_rys32, ctx->err);
+        if (rc) return fail(ctx, rc, ctx->err);
+    }
+    // the basis in one allocation (status flag, shell arrays, exponents, coefficients, centres), from a
+    // host image of the same layout
+    {
+        const int ns = ctx->nshell;
+        Carve lay;
+        const size_t o_status = lay.next(sizeof(int)), o_soff = lay.next(sizeof(int) * ns), o_sl = lay.next(sizeof(int) * ns),
+                     o_snp = lay.next(sizeof(int) * ns), o_scen = lay.next(sizeof(int) * ns),
+                     o_sprim = lay.next(sizeof(int) * ns), o_alpha = lay.next(sizeof(double) * np),
+                     o_coef = lay.next(sizeof(double) * np), o_cen = lay.next(sizeof(double) * 3 * ctx->ncen);
+        std::vector<char> img(lay.used, 0);
+        auto put = [&](size_t off, const void* src, size_t bytes) { std::memcpy(img.data() + off, src, bytes); };
+        put(o_soff, ctx->soff.data(), sizeof(int) * ns);
+        put(o_sl, ctx->sl.data(), sizeof(int) * ns);
+        put(o_snp, ctx->snp.data(), sizeof(int) * ns);
+        put(o_scen, ctx->scen.data(), sizeof(int) * ns);
+        put(o_sprim, ctx->sprim.data(), sizeof(int) * ns);
+        put(o_alpha, ctx->alpha.data(), sizeof(double) * np);
+        put(o_coef, ctx->coef.data(), sizeof(double) * np);
+        put(o_cen, ctx->centers.data(), sizeof(double) * 3 * ctx->ncen);
+        CU(cudaMalloc(&ctx->d_basis, img.size()));
+        CU(cudaMemcpy(ctx->d_basis, img.data(), img.size(), cudaMemcpyHostToDevice));
+        char* base = ctx->d_basis;
+        ctx->d_status = reinterpret_cast<int*>(base + o_status);
+        ctx->d_soff = reinterpret_cast<int*>(base + o_soff);
+        ctx->d_sl = reinterpret_cast<int*>(base + o_sl);
+        ctx->d_snp = reinterpret_cast<int*>(base + o_snp);
+        ctx->d_scen = reinterpret_cast<int*>(base + o_scen);
+        ctx->d_sprim = reinterpret_cast<int*>(base + o_sprim);
+        ctx->d_alpha = reinterpret_cast<double*>(base + o_alpha);
+        ctx->d_coef = reinterpret_cast<double*>(base + o_coef);
+        ctx->d_centers = reinterpret_cast<double*>(base + o_cen);
+    }
+    return build_setup(ctx);
+}
+
 }  // namespace
 
 extern "C" {
@@ -956,47 +1000,9 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
     ctx->coef.assign(b->coef, b->coef + np);
     ctx->centers.assign(b->centers, b->centers + 3 * b->ncen);
     build_norms(ctx->nt);
-    CU(cudaGetDevice(&ctx->dev));
-    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
-    {
-        const int rc = rys_tables(ctx->dev, ctx->d_rys, ctx->d_rys32, ctx->err);
-        if (rc) return fail(nullptr, rc, ctx->err);
-    }
-    // the basis in one allocation (status flag, shell arrays, exponents, coefficients, centres), from a
-    // host image of the same layout
-    {
-        const int ns = ctx->nshell;
-        Carve lay;
-        const size_t o_status = lay.next(sizeof(int)), o_soff = lay.next(sizeof(int) * ns), o_sl = lay.next(sizeof(int) * ns),
-                     o_snp = lay.next(sizeof(int) * ns), o_scen = lay.next(sizeof(int) * ns),
-                     o_sprim = lay.next(sizeof(int) * ns), o_alpha = lay.next(sizeof(double) * np),
-                     o_coef = lay.next(sizeof(double) * np), o_cen = lay.next(sizeof(double) * 3 * ctx->ncen);
-        std::vector<char> img(lay.used, 0);
-        auto put = [&](size_t off, const void* src, size_t bytes) { std::memcpy(img.data() + off, src, bytes); };
-        put(o_soff, ctx->soff.data(), sizeof(int) * ns);
-        put(o_sl, ctx->sl.data(), sizeof(int) * ns);
-        put(o_snp, ctx->snp.data(), sizeof(int) * ns);
-        put(o_scen, ctx->scen.data(), sizeof(int) * ns);
-        put(o_sprim, ctx->sprim.data(), sizeof(int) * ns);
-        put(o_alpha, ctx->alpha.data(), sizeof(double) * np);
-        put(o_coef, ctx->coef.data(), sizeof(double) * np);
-        put(o_cen, ctx->centers.data(), sizeof(double) * 3 * ctx->ncen);
-        CU(cudaMalloc(&ctx->d_basis, img.size()));
-        CU(cudaMemcpy(ctx->d_basis, img.data(), img.size(), cudaMemcpyHostToDevice));
-        char* base = ctx->d_basis;
-        ctx->d_status = reinterpret_cast<int*>(base + o_status);
-        ctx->d_soff = reinterpret_cast<int*>(base + o_soff);
-        ctx->d_sl = reinterpret_cast<int*>(base + o_sl);
-        ctx->d_snp = reinterpret_cast<int*>(base + o_snp);
-        ctx->d_scen = reinterpret_cast<int*>(base + o_scen);
-        ctx->d_sprim = reinterpret_cast<int*>(base + o_sprim);
-        ctx->d_alpha = reinterpret_cast<double*>(base + o_alpha);
-        ctx->d_coef = reinterpret_cast<double*>(base + o_coef);
-        ctx->d_centers = reinterpret_cast<double*>(base + o_cen);
-    }
     ctx->stats.nbf = ctx->nbf;
-    int rc = build_setup(ctx);
+    // device resources and the set-up; on failure everything created so far is released
+    const int rc = init_device(ctx, np);
     if (rc) {
         g_last_error = ctx->err;
         unomol_gpu_destroy(c.release());
