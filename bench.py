@@ -212,6 +212,23 @@ def timed_builds(ctx, inputs, steps, dev, stream, flush):
     return [a.elapsed_time(b_) for a, b_ in ev], eri
 
 
+def timed_batch_builds(bat, inputs, steps, dev, stream, flush):
+    """The same builds through the batched path (one-molecule batch: persistent kernels, CUDA graph):
+    per step an L2 flush, the input copied into the batch's density buffer, the graph replayed."""
+    import torch
+    from unomol_gb300 import native
+    sp = stream.cuda_stream
+    dIn = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for _, x in inputs]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        ev[k][0].record(stream)
+        bat.fock_device(dIn[k % len(inputs)].data_ptr(), 0, native.BATCH_GRAPH, sp)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    return [a.elapsed_time(b_) for a, b_ in ev]
+
+
 def counted_flops(ctx, inputs, dev, stream):
     """Algorithmic flops (FP64, FP32) and launches of every build of the sequence (untimed)."""
     import torch
@@ -298,11 +315,33 @@ def run_ours(args):
     clk = clocks.stop()
     total_s = replicas.max_over_ranks(sum(step_ms) / 1e3, ws, dev)
     value = ws * args.steps / total_s
+    # max |dF|: the form's full build and the plain build of the converged plain-FP64 density
+    max_dF = float(np.max(np.abs(mixed.form_g(r64["P"]) - plain.form_g(r64["P"]))))
     # the plain FP64 path on the same densities (full builds)
     plain_inputs = [(True, D) for D in rm["densities"]]
     timed_builds(plain, plain_inputs, 2, dev, stream, flush)
     p_ms, p_eri = timed_builds(plain, plain_inputs, min(args.steps, len(plain_inputs)), dev, stream, flush)
     plain_rate = len(p_ms) / (sum(p_ms) / 1e3)
+    # the same builds through the batched path (a one-molecule batch: persistent kernels per class,
+    # autotuned launch shapes, each build one CUDA-graph replay), same precision form
+    bat = native.Batch([b])
+    if args.form == "mixed":
+        bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, 1e-12)
+    bat.set_densities([inputs[0][1]])
+    tuned = bat.autotune(2)
+    timed_batch_builds(bat, inputs, max(args.warmup, 3), dev, stream, flush)
+    b_ms = timed_batch_builds(bat, inputs, args.steps, dev, stream, flush)
+    batched_rate = args.steps / (sum(b_ms) / 1e3)
+    kchk = 1 % len(inputs)
+    bat.set_densities([inputs[kchk][1]])
+    bat.fock(native.BATCH_GRAPH)
+    Gb = bat.get_focks()[0]
+    Gs = mixed.form_g(inputs[kchk][1])
+    batched = {"value": batched_rate, "unit": UNIT, "ms_per_build": statistics.mean(b_ms),
+               "speedup_vs_plain_fp64": batched_rate / plain_rate, "autotune": [list(c) for c in tuned],
+               "max_abs_dG_vs_single_context": float(np.max(np.abs(Gb - Gs))),
+               "note": "one-molecule batch: persistent kernels per quartet class, CUDA graph per build, L2 flushed per build"}
+    bat.close()
     # end to end through the host entry point, pinned host buffers
     pin_in = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for _, x in inputs]
     Gh = torch.zeros(b.no2, dtype=torch.float64).pin_memory()
@@ -353,10 +392,13 @@ def run_ours(args):
                          "flops_fp64": fl64 / args.steps, "flops_fp32": fl32 / args.steps, "kernel_ms": 1e3 * eri_s / args.steps,
                          "peak_fp64": peak64, "peak_fp32": peak32,
                          "peak_source": "FMA microbenchmark of this library (unomol_gpu_fma_peak), this run"},
+            "batched_form": batched,
             "plain_fp64": {"value": plain_rate, "unit": UNIT, "ms_per_build": statistics.mean(p_ms),
                            "kernel_ms": statistics.mean(p_eri), "speedup_of_value": value / plain_rate},
             "scf": {"energy_plain_fp64": r64["energy"], "energy_form": rm["energy"],
-                    "abs_dE": abs(rm["energy"] - r64["energy"]), "iterations_plain": r64["iterations"],
+                    "abs_dE": abs(rm["energy"] - r64["energy"]), "max_abs_dF": max_dF,
+                    "max_abs_dF_note": "G of the converged plain-FP64 density: full build of the form against the plain build",
+                    "iterations_plain": r64["iterations"],
                     "iterations_form": rm["iterations"], "converged": bool(r64["converged"] and rm["converged"]),
                     "scf_wall_s_plain_fp64": r64["seconds"], "scf_wall_s_form": rm["seconds"],
                     "fock_ms_plain_fp64": r64["fock_ms"], "fock_ms_form": rm["fock_ms"], "guess_s": t_guess,

@@ -185,11 +185,20 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
 int unomol_gpu_batch_buffers(UnomolBatch* batch, double** dP, double** dG, const long long** packed_offsets,
                              int64_t* packed_total);
 int unomol_gpu_batch_fock(UnomolBatch* batch, int mode, void* stream);
+/* The same on caller-owned device buffers: packed densities of all molecules in (dP, copied into the
+ * batch's buffer on `stream`), packed G out (dG, copied from it); either may be the batch's own buffer
+ * or NULL (use the batch's buffer). */
+int unomol_gpu_batch_fock_device(UnomolBatch* batch, const double* dP, double* dG, int mode, void* stream);
 int unomol_gpu_batch_size(const UnomolBatch* batch);  /* molecules in the batch */
 /* Autotuner: times every (CTA size 64/128/256, CTAs per SM 1/2/4/8) per class launch on the current P
  * and keeps the fastest; chosen (optional, 3 ints per launch): class id, CTA size, CTAs per SM.
  * Returns the number of launches (>= 0) or an error code. */
 int unomol_gpu_batch_autotune(UnomolBatch* batch, int reps, int* chosen);
+/* Precision form of the batched build, as unomol_gpu_set_precision and unomol_gpu_set_density_screening
+ * for one context: UNOMOL_PREC_MIXED splits every molecule's quartets per build into FP64 (Schwarz bound
+ * x max|P| of its six density blocks >= fp32_cutoff), FP32 (>= skip_cutoff) and skipped parts; the
+ * persistent kernels run both parts.  The batch's CUDA graph is captured again on its next use. */
+int unomol_gpu_batch_set_precision(UnomolBatch* batch, int mode, double fp32_cutoff, double skip_cutoff);
 /* host copies of the batch's packed P (in) and G (out), all molecules concatenated */
 int unomol_gpu_batch_set_density(UnomolBatch* batch, const double* P);
 int unomol_gpu_batch_get_fock(UnomolBatch* batch, double* G);

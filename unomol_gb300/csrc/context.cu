@@ -23,6 +23,7 @@
 #include "fock_dispatch.cuh"
 #include "fock_kernels.cuh"
 #include "setup.h"
+#include "worklists.h"
 
 using namespace ugb;
 
@@ -497,12 +498,6 @@ __global__ void expand_packed(const double* __restrict__ pk, double* __restrict_
     full[t] = pk[(long long)hi * (hi + 1) / 2 + lo];
 }
 
-// FP32 copy of a dense density (the FP32 kernels contract with it)
-__global__ void to_float(const double* __restrict__ full, float* __restrict__ f32, long long n2) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n2) f32[t] = (float)full[t];
-}
-
 // G_packed[ij] += T[i][j] + T[j][i]
 __global__ void fold_packed(const double* __restrict__ T, double* __restrict__ G, int n) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -514,124 +509,6 @@ __global__ void fold_packed(const double* __restrict__ T, double* __restrict__ G
     while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
     const int j = (int)(t - (long long)i * (i + 1) / 2);
     G[t] += T[(long long)i * n + j] + T[(long long)j * n + i];
-}
-
-// max |P| over every shell pair block (and over all blocks into dmax[0]), for density screening
-__global__ void shell_pmax(const double* __restrict__ Pa, const double* __restrict__ Pb, const int* __restrict__ soff,
-                           const int* __restrict__ sl, int nshell, int n, float* __restrict__ out, float* dmax) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nshell * nshell) return;
-    const int a = t / nshell, b = t % nshell;
-    const int na = (sl[a] + 1) * (sl[a] + 2) / 2, nb = (sl[b] + 1) * (sl[b] + 2) / 2;
-    double m = 0.0;
-    for (int i = 0; i < na; ++i)
-        for (int j = 0; j < nb; ++j) {
-            const long long ix = (long long)(soff[a] + i) * n + soff[b] + j;
-            double v = fabs(Pa[ix]);
-            if (Pb) v = fmax(v, fabs(Pb[ix]));
-            m = fmax(m, v);
-        }
-    // round up so that the float bound never undercuts the double one
-    const float mf = __double2float_ru(m);
-    out[t] = mf;
-    atomicMax(reinterpret_cast<unsigned*>(dmax), __float_as_uint(mf));  // non-negative floats order as uints
-}
-
-// Per bra row of every block pair: lengths of the FP64 segment (bound * max|P| >= cut64) and of the
-// FP32 segment (>= skip) of the row's Schwarz staircase, for this build's density.
-__global__ void split_rows(const ShellPair* __restrict__ pairs, const BlockPair* __restrict__ bps,
-                           const int* __restrict__ row_bp, const long long* __restrict__ prefix, long long nrows,
-                           const float* __restrict__ dmax, double cut64, double skip, long long* __restrict__ c64,
-                           long long* __restrict__ c32, int* __restrict__ mseg) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nrows) return;
-    const int bpi = row_bp[t];
-    if (bpi < 0) return;  // end-of-block-pair sentinel
-    const BlockPair bp = bps[bpi];
-    const int i = (int)(t - bp.prefix_off);
-    const int nstat = (int)(prefix[t + 1] - prefix[t]);  // static (integral-bound) staircase of the row
-    const double qd = pairs[bp.bra_begin + i].q * (double)dmax[0];
-    const ShellPair* kp = pairs + bp.ket_begin;
-    auto count = [&](double cut) {  // ket pairs j < nstat with q_i q_j max|P| >= cut (q descending)
-        if (!(qd > 0.0)) return 0;
-        const double thr = cut / qd;
-        int lo = 0, hi = nstat;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (kp[mid].q >= thr) lo = mid + 1; else hi = mid;
-        }
-        return lo;
-    };
-    const int n64 = count(cut64);
-    const int nall = cut64 <= skip ? n64 : count(skip);
-    c64[t] = n64;
-    c32[t] = nall - n64;
-    mseg[t] = n64;
-}
-
-// Exclusive scan of the two row counts within every block pair (one CUDA block per block pair).
-__global__ void __launch_bounds__(1024) scan_rows(const BlockPair* __restrict__ bps, const long long* __restrict__ c64,
-                                                  const long long* __restrict__ c32, long long* __restrict__ p64,
-                                                  long long* __restrict__ p32, long long* __restrict__ n64,
-                                                  long long* __restrict__ n32) {
-    __shared__ long long warp_a[32], warp_b[32];
-    __shared__ long long run_a, run_b;
-    const BlockPair bp = bps[blockIdx.x];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0) {
-        run_a = 0;
-        run_b = 0;
-    }
-    __syncthreads();
-    for (int base = 0; base < bp.bra_count; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const long long va = i < bp.bra_count ? c64[bp.prefix_off + i] : 0;
-        const long long vb = i < bp.bra_count ? c32[bp.prefix_off + i] : 0;
-        long long sa = va, sb = vb;  // inclusive warp scan
-        for (int o = 1; o < 32; o <<= 1) {
-            const long long xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
-            if (lane >= o) {
-                sa += xa;
-                sb += xb;
-            }
-        }
-        if (lane == 31) {
-            warp_a[wid] = sa;
-            warp_b[wid] = sb;
-        }
-        __syncthreads();
-        if (wid == 0) {
-            const int nw = blockDim.x >> 5;
-            long long ta = lane < nw ? warp_a[lane] : 0, tb = lane < nw ? warp_b[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                const long long xa = __shfl_up_sync(0xffffffffu, ta, o), xb = __shfl_up_sync(0xffffffffu, tb, o);
-                if (lane >= o) {
-                    ta += xa;
-                    tb += xb;
-                }
-            }
-            if (lane < nw) {
-                warp_a[lane] = ta;  // inclusive sums of the warps
-                warp_b[lane] = tb;
-            }
-        }
-        __syncthreads();
-        const long long wa = wid > 0 ? warp_a[wid - 1] : 0, wb = wid > 0 ? warp_b[wid - 1] : 0;
-        if (i < bp.bra_count) {
-            p64[bp.prefix_off + i] = run_a + wa + sa - va;
-            p32[bp.prefix_off + i] = run_b + wb + sb - vb;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            run_a += warp_a[(blockDim.x >> 5) - 1];
-            run_b += warp_b[(blockDim.x >> 5) - 1];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        n64[blockIdx.x] = run_a;
-        n32[blockIdx.x] = run_b;
-    }
 }
 
 int ensure_density_buffers(UnomolCtx* ctx, bool uhf) {
@@ -698,28 +575,22 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         if (!ctx->d_pmax) CU(cudaMalloc(&ctx->d_pmax, sizeof(float) * ctx->nshell * ctx->nshell));
         if (!ctx->d_dmax) CU(cudaMalloc(&ctx->d_dmax, sizeof(float)));
         A.pmax = ctx->d_pmax;
-        const int ns2 = ctx->nshell * ctx->nshell;
         CU(cudaMemsetAsync(ctx->d_dmax, 0, sizeof(float), s));
-        shell_pmax<<<(ns2 + 255) / 256, 256, 0, s>>>(ctx->d_Pa, A.Pb, ctx->d_soff, ctx->d_sl, ctx->nshell, n, ctx->d_pmax,
-                                                     ctx->d_dmax);
-        const long long nr = ctx->nrows;
-        split_rows<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(ctx->d_pairs, ctx->d_bps, ctx->d_rowbp, ctx->d_prefix, nr,
-                                                                ctx->d_dmax, std::max(ctx->fp32_cut, ctx->skip_cut),
-                                                                ctx->skip_cut, ctx->d_c64, ctx->d_c32, ctx->d_mseg);
-        scan_rows<<<(unsigned)ctx->bps.size(), 512, 0, s>>>(ctx->d_bps, ctx->d_c64, ctx->d_c32, ctx->d_pre64, ctx->d_pre32,
-                                                             ctx->d_cnt64, ctx->d_cnt32);
-        CU(cudaGetLastError());
+        CU(wl_shell_pmax(ctx->d_Pa, A.Pb, ctx->d_soff, ctx->d_sl, ctx->nshell, n, ctx->d_pmax, ctx->d_dmax, s));
+        CU(wl_split_rows(ctx->d_pairs, ctx->d_bps, ctx->d_rowbp, ctx->d_prefix, ctx->nrows, ctx->d_dmax,
+                         std::max(ctx->fp32_cut, ctx->skip_cut), ctx->skip_cut, ctx->d_c64, ctx->d_c32, ctx->d_mseg, s));
+        CU(wl_scan_rows(ctx->d_bps, (int)ctx->bps.size(), ctx->d_c64, ctx->d_c32, ctx->d_pre64, ctx->d_pre32, ctx->d_cnt64,
+                        ctx->d_cnt32, s));
         launches += 3;
         A.dmax = ctx->d_dmax;
         A.skip_cut = ctx->skip_cut;
         A.dyn_mseg = ctx->d_mseg;
-        to_float<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(ctx->d_Pa, ctx->d_Pa32, n2);
+        CU(wl_to_float(ctx->d_Pa, ctx->d_Pa32, n2, s));
         A.Pa32 = ctx->d_Pa32;
         if (uhf) {
-            to_float<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(ctx->d_Pb, ctx->d_Pb32, n2);
+            CU(wl_to_float(ctx->d_Pb, ctx->d_Pb32, n2, s));
             A.Pb32 = ctx->d_Pb32;
         }
-        CU(cudaGetLastError());
     }
     const int ncls = NPAIRCLASS * NPAIRCLASS;
     A.counters = nullptr;
@@ -835,6 +706,7 @@ CtxView ctx_view(const UnomolCtx* c) {
     v.d_pairs = c->d_pairs;
     v.npairs = c->npairs;
     v.d_prims = c->d_prims;
+    v.d_prims32 = c->d_prims32;
     v.nprims = c->nprims;
     v.d_prefix = c->d_prefix;
     v.nrows = c->nrows;
@@ -842,10 +714,13 @@ CtxView ctx_view(const UnomolCtx* c) {
     v.block_begin = &c->block_begin;
     v.block_count = &c->block_count;
     v.block_class = &c->block_class;
+    v.soff = &c->soff;
+    v.sl = &c->sl;
     v.stream = c->stream;
     for (const ClassLaunch& L : c->launches) v.launches.push_back({L.bc, L.kc, L.bp_begin, L.nbp, L.nwork, L.quartets});
     v.nt = c->nt;
     v.d_rys = c->d_rys;
+    v.d_rys32 = c->d_rys32;
     return v;
 }
 

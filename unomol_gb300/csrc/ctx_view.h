@@ -22,6 +22,7 @@ struct CtxView {
     const ShellPair* d_pairs = nullptr;  // device arrays of the setup
     int npairs = 0;
     const PrimPair* d_prims = nullptr;
+    const PrimPair32* d_prims32 = nullptr;
     long long nprims = 0;
     const long long* d_prefix = nullptr;
     long long nrows = 0;
@@ -29,10 +30,13 @@ struct CtxView {
     const std::vector<int>* block_begin = nullptr;
     const std::vector<int>* block_count = nullptr;
     const std::vector<int>* block_class = nullptr;
+    const std::vector<int>* soff = nullptr;  // host: first AO and L of every shell
+    const std::vector<int>* sl = nullptr;
     cudaStream_t stream = nullptr;  // the context's stream (its setup ran there)
     std::vector<ClassLaunchInfo> launches;
     NormTable nt{};
     const double* d_rys = nullptr;
+    const float* d_rys32 = nullptr;
 };
 
 CtxView ctx_view(const UnomolCtx* ctx);

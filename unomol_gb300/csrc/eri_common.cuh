@@ -108,6 +108,8 @@ struct FockArgs {
     // have mol_nbf rows (nullptr: one molecule, A.nbf rows at offset 0)
     const int* mol_nbf;
     const long long* mol_base;
+    const int* mol_nshell;        // batches in the screened build: shells of the molecule and the first
+    const long long* mol_pmax;    // entry of its shell-pair max|P| blocks in pmax
     unsigned long long* tile_counter;  // persistent launches: next tile of this launch
     int* status;                // device error flag
 };

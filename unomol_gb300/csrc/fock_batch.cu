@@ -12,28 +12,33 @@
 #include "ctx_view.h"
 #include "fock_dispatch.cuh"
 #include "setup.h"
+#include "worklists.h"
 
 using namespace ugb;
 
 namespace {
 
-template <int BC, int KC>
-cudaError_t persistent_one(const FockArgs& A, const NormTable& nt, const double* rys, int grid, int block, cudaStream_t s) {
+template <int BC, int KC, typename R>
+cudaError_t persistent_one(const FockArgs& A, const NormTable& nt, const R* rys, int grid, int block, cudaStream_t s) {
     constexpr int LA = pc_la(BC), LB = pc_lb(BC), LC = pc_la(KC), LD = pc_lb(KC);
     if constexpr (QClass<LA, LB, LC, LD>::NF <= 81) {
-        fock_jk_persistent<LA, LB, LC, LD, false, double><<<grid, block, 0, s>>>(A, nt, rys);
-    } else {
+        fock_jk_persistent<LA, LB, LC, LD, false, R><<<grid, block, 0, s>>>(A, nt, rys);
+    } else if constexpr (sizeof(R) == 8) {
         // large classes: one item per thread over the whole launch
         fock_jk_generic<false, double, PrimPair><<<(unsigned)((A.nwork + 63) / 64), 64, 0, s>>>(A, nt, rys, A.prims, LA, LB, LC, LD);
+    } else {
+        fock_jk_generic<false, float, PrimPair32><<<(unsigned)((A.nwork + 63) / 64), 64, 0, s>>>(A, nt, rys, A.prims32, LA, LB, LC, LD);
     }
     return cudaGetLastError();
 }
 
 #define UGB_CASE(BC, KC) \
     case (BC) * 8 + (KC): \
-        return persistent_one<BC, KC>(A, nt, rys, grid, block, s);
+        return persistent_one<BC, KC, R>(A, nt, rys, grid, block, s);
 
-cudaError_t launch_persistent(int bc, int kc, const FockArgs& A, const NormTable& nt, const double* rys, int grid,
+// FP64 (R = double, FP64 tables) or FP32 (R = float, FP32 tables) persistent launch of one class
+template <typename R>
+cudaError_t launch_persistent(int bc, int kc, const FockArgs& A, const NormTable& nt, const R* rys, int grid,
                               int block, cudaStream_t s) {
     switch (bc * 8 + kc) {
 #include "fock_cases.inc"
@@ -108,10 +113,24 @@ struct UnomolBatch {
     int* d_nbf = nullptr;
     long long *d_doff = nullptr, *d_poff = nullptr;
     double *d_P = nullptr, *d_G = nullptr, *d_Pfull = nullptr, *d_T = nullptr;
-    unsigned long long* d_tiles = nullptr;
+    unsigned long long* d_tiles = nullptr;  // two per class launch (FP64 part, FP32 part)
     std::vector<BLaunch> launches;
     NormTable nt{};
     const double* rys = nullptr;
+    const float* rys32 = nullptr;
+    // precision form (UNOMOL_PREC_MIXED): per-build work lists as for one context, over all molecules
+    int prec_mode = UNOMOL_PREC_FP64;
+    double fp32_cut = 1e-10, skip_cut = 1e-12;
+    long long nrows = 0, pmax_total = 0;
+    int nbps = 0;
+    PrimPair32* d_prims32 = nullptr;
+    float* d_Pfull32 = nullptr;
+    float *d_pmax = nullptr, *d_dmax = nullptr;
+    int *d_nshell = nullptr, *d_shell0 = nullptr, *d_soff = nullptr, *d_sl = nullptr;
+    long long* d_pmax_off = nullptr;
+    int *d_rowbp = nullptr, *d_mseg = nullptr;
+    long long *d_c64 = nullptr, *d_c32 = nullptr, *d_pre64 = nullptr, *d_pre32 = nullptr;
+    long long *d_cnt64 = nullptr, *d_cnt32 = nullptr;
     int rys_compat = 1;
     int nsm = 152;
     cudaStream_t stream = nullptr;
@@ -151,8 +170,17 @@ FockArgs batch_args(UnomolBatch* b, const BLaunch& L, int k) {
     A.rys_compat = b->rys_compat;
     A.mol_nbf = b->d_nbf;
     A.mol_base = b->d_doff;
-    A.tile_counter = b->d_tiles + k;
+    A.tile_counter = b->d_tiles + 2 * k;
     A.mode = 0;
+    A.prims32 = b->d_prims32;
+    A.Pa32 = b->d_Pfull32;
+    A.pmax = b->d_pmax;
+    A.dmax = b->d_dmax;
+    A.skip_cut = b->skip_cut;
+    A.fp32_cut = b->fp32_cut;
+    A.dyn_mseg = b->d_mseg;
+    A.mol_nshell = b->d_nshell;
+    A.mol_pmax = b->d_pmax_off;
     return A;
 }
 
@@ -163,11 +191,37 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
                                                                           nmol, b->dense_total);
     BCU(cudaGetLastError());
     BCU(cudaMemsetAsync(b->d_T, 0, sizeof(double) * b->dense_total, s));
-    BCU(cudaMemsetAsync(b->d_tiles, 0, sizeof(unsigned long long) * std::max<size_t>(1, b->launches.size()), s));
+    BCU(cudaMemsetAsync(b->d_tiles, 0, sizeof(unsigned long long) * 2 * std::max<size_t>(1, b->launches.size()), s));
+    const bool mixed = b->prec_mode == UNOMOL_PREC_MIXED;
+    if (mixed) {
+        // this build's work lists: max|P| per shell-pair block and per molecule, split of every staircase
+        // row into FP64 / FP32 / skipped segments, scan per block pair; FP32 copy of the densities
+        BCU(cudaMemsetAsync(b->d_dmax, 0, sizeof(float) * nmol, s));
+        BCU(wl_shell_pmax_batch(b->d_Pfull, b->d_doff, b->d_nbf, b->d_shell0, b->d_nshell, b->d_pmax_off, b->d_soff, b->d_sl,
+                                nmol, b->pmax_total, b->d_pmax, b->d_dmax, s));
+        BCU(wl_split_rows(b->d_pairs, b->d_bps, b->d_rowbp, b->d_prefix, b->nrows, b->d_dmax,
+                          std::max(b->fp32_cut, b->skip_cut), b->skip_cut, b->d_c64, b->d_c32, b->d_mseg, s));
+        BCU(wl_scan_rows(b->d_bps, (int)b->nbps, b->d_c64, b->d_c32, b->d_pre64, b->d_pre32, b->d_cnt64, b->d_cnt32, s));
+        BCU(wl_to_float(b->d_Pfull, b->d_Pfull32, b->dense_total, s));
+    }
     for (size_t k = 0; k < b->launches.size(); ++k) {
         const BLaunch& L = b->launches[k];
-        const FockArgs A = batch_args(b, L, (int)k);
+        FockArgs A = batch_args(b, L, (int)k);
+        if (!mixed) {
+            BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, s));
+            continue;
+        }
+        A.mode = 1;  // FP64 part
+        A.dyn_prefix = b->d_pre64;
+        A.dyn_count = b->d_cnt64 + L.bp_begin;
         BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, s));
+        if (b->fp32_cut > b->skip_cut) {
+            A.mode = 2;  // FP32 part
+            A.dyn_prefix = b->d_pre32;
+            A.dyn_count = b->d_cnt32 + L.bp_begin;
+            A.tile_counter = b->d_tiles + 2 * k + 1;
+            BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys32, b->nsm * L.ctas_per_sm, L.block, s));
+        }
     }
     batch_fold<<<(unsigned)((b->packed_total + 255) / 256), 256, 0, s>>>(b->d_T, b->d_doff, b->d_G, b->d_poff, b->d_nbf,
                                                                          nmol, b->packed_total);
@@ -175,9 +229,88 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
     return UNOMOL_OK;
 }
 
+// Buffers of the precision form, made on first use: the molecules' FP32 primitive pairs side by side,
+// the shell arrays of all molecules (for max|P| per shell-pair block), the FP32 dense densities and the
+// per-build row lists of the merged staircases.
+int ensure_mixed(UnomolBatch* b) {
+    if (b->d_prims32) return UNOMOL_OK;
+    const int nmol = (int)b->mols.size();
+    std::vector<int> nshell(nmol), shell0(nmol), soff, sl;
+    std::vector<long long> pmax_off(nmol);
+    long long nprim_tot = 0, ptot = 0;
+    for (int m = 0; m < nmol; ++m) {
+        const CtxView v = ctx_view(b->mols[m]);
+        nshell[m] = v.nshell;
+        shell0[m] = (int)soff.size();
+        soff.insert(soff.end(), v.soff->begin(), v.soff->end());
+        sl.insert(sl.end(), v.sl->begin(), v.sl->end());
+        pmax_off[m] = ptot;
+        ptot += (long long)v.nshell * v.nshell;
+        nprim_tot += v.nprims;
+    }
+    b->pmax_total = ptot;
+    const size_t nr = (size_t)std::max<long long>(1, b->nrows), nbp = (size_t)std::max(1, b->nbps);
+    BCU(cudaMalloc(&b->d_prims32, sizeof(PrimPair32) * std::max<long long>(1, nprim_tot)));
+    BCU(cudaMalloc(&b->d_Pfull32, sizeof(float) * std::max<long long>(1, b->dense_total)));
+    BCU(cudaMalloc(&b->d_pmax, sizeof(float) * std::max<long long>(1, ptot)));
+    BCU(cudaMalloc(&b->d_dmax, sizeof(float) * nmol));
+    BCU(cudaMalloc(&b->d_nshell, sizeof(int) * nmol));
+    BCU(cudaMalloc(&b->d_shell0, sizeof(int) * nmol));
+    BCU(cudaMalloc(&b->d_pmax_off, sizeof(long long) * nmol));
+    BCU(cudaMalloc(&b->d_soff, sizeof(int) * std::max<size_t>(1, soff.size())));
+    BCU(cudaMalloc(&b->d_sl, sizeof(int) * std::max<size_t>(1, sl.size())));
+    BCU(cudaMalloc(&b->d_rowbp, sizeof(int) * nr));
+    BCU(cudaMalloc(&b->d_mseg, sizeof(int) * nr));
+    for (long long** p : {&b->d_c64, &b->d_c32, &b->d_pre64, &b->d_pre32}) BCU(cudaMalloc(p, sizeof(long long) * nr));
+    BCU(cudaMalloc(&b->d_cnt64, sizeof(long long) * nbp));
+    BCU(cudaMalloc(&b->d_cnt32, sizeof(long long) * nbp));
+    cudaStream_t s = b->stream;
+    long long p0 = 0;
+    for (int m = 0; m < nmol; ++m) {
+        const CtxView v = ctx_view(b->mols[m]);
+        if (v.nprims > 0)
+            BCU(cudaMemcpyAsync(b->d_prims32 + p0, v.d_prims32, sizeof(PrimPair32) * v.nprims, cudaMemcpyDeviceToDevice, s));
+        p0 += v.nprims;
+    }
+    BCU(cudaMemcpyAsync(b->d_nshell, nshell.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice, s));
+    BCU(cudaMemcpyAsync(b->d_shell0, shell0.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice, s));
+    BCU(cudaMemcpyAsync(b->d_pmax_off, pmax_off.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice, s));
+    if (!soff.empty()) {
+        BCU(cudaMemcpyAsync(b->d_soff, soff.data(), sizeof(int) * soff.size(), cudaMemcpyHostToDevice, s));
+        BCU(cudaMemcpyAsync(b->d_sl, sl.data(), sizeof(int) * sl.size(), cudaMemcpyHostToDevice, s));
+    }
+    // row -> block pair of the merged list (-1 on end-of-block-pair entries and rows of empty block pairs)
+    BCU(cudaMemsetAsync(b->d_rowbp, 0xff, sizeof(int) * nr, s));
+    BCU(setup_row_bp(b->d_bps, b->nbps, b->d_rowbp, s));
+    BCU(cudaMemsetAsync(b->d_c64, 0, sizeof(long long) * nr, s));
+    BCU(cudaMemsetAsync(b->d_c32, 0, sizeof(long long) * nr, s));
+    BCU(cudaMemsetAsync(b->d_mseg, 0, sizeof(int) * nr, s));
+    BCU(cudaStreamSynchronize(s));
+    return UNOMOL_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int unomol_gpu_batch_set_precision(UnomolBatch* b, int mode, double fp32_cut, double skip_cut) {
+    if (!b) return bfail(b, UNOMOL_EINVAL, "null batch");
+    if (mode != UNOMOL_PREC_FP64 && mode != UNOMOL_PREC_MIXED) return bfail(b, UNOMOL_EINVAL, "unknown precision mode");
+    if (!(fp32_cut >= 0.0) || !(skip_cut >= 0.0)) return bfail(b, UNOMOL_EINVAL, "bad cutoff");
+    if (mode == UNOMOL_PREC_MIXED) {
+        const int rc = ensure_mixed(b);
+        if (rc) return rc;
+    }
+    b->prec_mode = mode;
+    b->fp32_cut = fp32_cut;
+    b->skip_cut = skip_cut;
+    if (b->graph) {  // the captured build has the previous form's launches: capture again on next use
+        BCU(cudaStreamSynchronize(b->stream));
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return UNOMOL_OK;
+}
 
 int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch** out) {
     UnomolBatch* b = nullptr;
@@ -205,6 +338,7 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
         if (m == 0) {
             b->nt = v.nt;
             b->rys = v.d_rys;
+            b->rys32 = v.d_rys32;
             b->rys_compat = v.rys_compat;
         }
         if (npair_tot + v.npairs >= INT_MAX || nprim_tot + v.nprims >= INT_MAX || nrow_tot + v.nrows >= INT_MAX) {
@@ -286,8 +420,10 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
     BCU(cudaMalloc(&b->d_G, sizeof(double) * packed));
     BCU(cudaMalloc(&b->d_Pfull, sizeof(double) * dense));
     BCU(cudaMalloc(&b->d_T, sizeof(double) * dense));
-    BCU(cudaMalloc(&b->d_tiles, sizeof(unsigned long long) * std::max<size_t>(1, b->launches.size())));
+    BCU(cudaMalloc(&b->d_tiles, sizeof(unsigned long long) * 2 * std::max<size_t>(1, b->launches.size())));
     BCU(cudaMemcpy(b->d_bps, bps.data(), sizeof(BlockPair) * bps.size(), cudaMemcpyHostToDevice));
+    b->nbps = (int)bps.size();
+    b->nrows = nrow_tot;
     BCU(cudaMemcpy(b->d_nbf, b->nbf.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->d_doff, b->doff.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->d_poff, b->poff.data(), sizeof(long long) * nmol, cudaMemcpyHostToDevice));
@@ -348,6 +484,18 @@ int unomol_gpu_batch_fock(UnomolBatch* b, int mode, void* stream) {
     return bfail(b, UNOMOL_EINVAL, "unknown batch mode");
 }
 
+int unomol_gpu_batch_fock_device(UnomolBatch* b, const double* dP, double* dG, int mode, void* stream) {
+    if (!b) return bfail(b, UNOMOL_EINVAL, "null batch");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    if (dP && dP != b->d_P)
+        BCU(cudaMemcpyAsync(b->d_P, dP, sizeof(double) * b->packed_total, cudaMemcpyDeviceToDevice, s));
+    const int rc = unomol_gpu_batch_fock(b, mode, stream);
+    if (rc) return rc;
+    if (dG && dG != b->d_G)
+        BCU(cudaMemcpyAsync(dG, b->d_G, sizeof(double) * b->packed_total, cudaMemcpyDeviceToDevice, s));
+    return UNOMOL_OK;
+}
+
 // Autotuner: for every class launch, time each (CTA size, CTAs per SM) and keep the fastest; the
 // CUDA graph is rebuilt on the next graph launch.  Uses the densities currently in the P buffer.
 int unomol_gpu_batch_autotune(UnomolBatch* b, int reps, int* chosen) {
@@ -369,7 +517,7 @@ int unomol_gpu_batch_autotune(UnomolBatch* b, int reps, int* chosen) {
             for (int c : ctas) {
                 float tot = 0.f;
                 for (int r = 0; r < reps; ++r) {
-                    BCU(cudaMemsetAsync(b->d_tiles + k, 0, sizeof(unsigned long long), s));
+                    BCU(cudaMemsetAsync(b->d_tiles + 2 * k, 0, sizeof(unsigned long long), s));
                     FockArgs A = batch_args(b, L, (int)k);
                     BCU(cudaEventRecord(e0, s));
                     BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * c, blk, s));
@@ -433,6 +581,18 @@ void unomol_gpu_batch_destroy(UnomolBatch* b) {
     dfree(b->d_G);
     dfree(b->d_Pfull);
     dfree(b->d_T);
+    dfree(b->d_prims32);
+    dfree(b->d_Pfull32);
+    dfree(b->d_pmax);
+    dfree(b->d_dmax);
+    dfree(b->d_nshell);
+    dfree(b->d_shell0);
+    dfree(b->d_pmax_off);
+    dfree(b->d_soff);
+    dfree(b->d_sl);
+    dfree(b->d_rowbp);
+    dfree(b->d_mseg);
+    for (long long** p : {&b->d_c64, &b->d_c32, &b->d_pre64, &b->d_pre32, &b->d_cnt64, &b->d_cnt32}) dfree(*p);
     dfree(b->d_tiles);
     for (UnomolCtx* c : b->mols) unomol_gpu_destroy(c);
     if (b->stream) cudaStreamDestroy(b->stream);

@@ -389,6 +389,8 @@ __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g,
     const BlockPair& bp = A.bps[lo];
     const long long* pre = (DYN ? A.dyn_prefix : A.prefix) + bp.prefix_off;
     const long long w0 = g0 - bp.work_begin;
+    const long long count = DYN ? A.dyn_count[lo] : bp.work_count;
+    if (w0 >= count) return false;  // the whole warp lies past this part's quartets of the block pair
     int a = 0, b = bp.bra_count - 1;  // largest row with pre[row] <= w0 (pre[0] = 0)
     while (a < b) {
         const int step = (b - a + 32) >> 5;
@@ -398,7 +400,7 @@ __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g,
         b = min(b, a + step - 1);
     }
     const long long w = w0 + lane;
-    if (w >= (DYN ? A.dyn_count[lo] : bp.work_count)) return false;
+    if (w >= count) return false;
     while (a + 1 < bp.bra_count && pre[a + 1] <= w) ++a;
     bra_idx = bp.bra_begin + a;
     int j = (int)(w - pre[a]);
@@ -410,9 +412,15 @@ __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g,
 // Density screening of one quartet: Schwarz bound times the largest |P| of the six shell-pair blocks
 // the quartet contracts with (J: ab, cd; K: ac, ad, bc, bd).
 __device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellPair& bra, const ShellPair& ket) {
-    const int a = bra.ish, b = bra.jsh, c = ket.ish, d = ket.jsh, n = A.nshell;
-    float m = fmaxf(fmaxf(A.pmax[a * n + b], A.pmax[c * n + d]), fmaxf(A.pmax[a * n + c], A.pmax[a * n + d]));
-    m = fmaxf(m, fmaxf(A.pmax[b * n + c], A.pmax[b * n + d]));
+    const int a = bra.ish, b = bra.jsh, c = ket.ish, d = ket.jsh;
+    int n = A.nshell;
+    const float* pm = A.pmax;
+    if (A.mol_nshell) {  // batch: the blocks of the quartet's molecule
+        n = A.mol_nshell[bra.pad];
+        pm += A.mol_pmax[bra.pad];
+    }
+    float m = fmaxf(fmaxf(pm[a * n + b], pm[c * n + d]), fmaxf(pm[a * n + c], pm[a * n + d]));
+    m = fmaxf(m, fmaxf(pm[b * n + c], pm[b * n + d]));
     return (float)(bra.q * ket.q) * m < (float)A.skip_cut;
 }
 

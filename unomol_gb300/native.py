@@ -34,7 +34,7 @@ EXPORTS = [
     "unomol_guess_get_params", "unomol_guess_set_params", "unomol_guess_destroy", "unomol_guess_last_error",
     "unomol_gpu_one_electron", "unomol_gpu_one_electron_last_error", "unomol_gpu_l2_peak", "unomol_gpu_batch_scf",
     "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
-    "unomol_gpu_moment_ints",
+    "unomol_gpu_moment_ints", "unomol_gpu_batch_set_precision", "unomol_gpu_batch_fock_device",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -395,6 +395,8 @@ class Batch:
                                                C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]
         L.unomol_gpu_batch_fock.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.unomol_gpu_batch_autotune.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.unomol_gpu_batch_set_precision.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
+        L.unomol_gpu_batch_fock_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         L.unomol_gpu_batch_set_density.argtypes = [C.c_void_p, _dp]
         L.unomol_gpu_batch_get_fock.argtypes = [C.c_void_p, _dp]
         L.unomol_gpu_batch_destroy.argtypes = [C.c_void_p]
@@ -423,11 +425,21 @@ class Batch:
             raise UnomolError(f"unomol_gb300 batch error {rc}: {msg}")
         return rc
 
+    def set_precision(self, mode: int, fp32_cutoff: float = 1e-10, skip_cutoff: float = 1e-12):
+        """Precision form of the batched build (PREC_FP64 or PREC_MIXED with the FP32 and density-skip
+        cutoffs), as set_precision + set_density_screening of one context."""
+        self._chk(lib().unomol_gpu_batch_set_precision(self._h, int(mode), float(fp32_cutoff), float(skip_cutoff)))
+
     def set_densities(self, Ps):
         self._chk(lib().unomol_gpu_batch_set_density(self._h, np.ascontiguousarray(np.concatenate(Ps), np.float64)))
 
     def fock(self, mode: int = BATCH_GRAPH, stream: int = 0):
         self._chk(lib().unomol_gpu_batch_fock(self._h, int(mode), C.c_void_p(stream)))
+
+    def fock_device(self, dP_ptr: int = 0, dG_ptr: int = 0, mode: int = BATCH_GRAPH, stream: int = 0):
+        """Batched build on device buffers (packed P of all molecules in, packed G out; 0: the batch's own)."""
+        self._chk(lib().unomol_gpu_batch_fock_device(self._h, C.c_void_p(dP_ptr or None), C.c_void_p(dG_ptr or None),
+                                                     int(mode), C.c_void_p(stream)))
 
     def get_focks(self):
         G = np.zeros(self.total)
