@@ -54,6 +54,7 @@ struct UnomolCtx {
     std::vector<char> block_new;
     std::vector<BlockPair> bps;
     std::vector<ClassLaunch> launches;
+    std::vector<int> launch_bp;
     // the basis on the device (centres refreshed by recalculate) and the setup's scratch
     int *d_snp = nullptr, *d_scen = nullptr, *d_sprim = nullptr;
     double *d_alpha = nullptr, *d_coef = nullptr, *d_centers = nullptr;
@@ -72,6 +73,8 @@ struct UnomolCtx {
     int *d_rowbp = nullptr, *d_mseg = nullptr;
     long long *d_c64 = nullptr, *d_c32 = nullptr, *d_pre64 = nullptr, *d_pre32 = nullptr;
     long long *d_cnt64 = nullptr, *d_cnt32 = nullptr;
+    long long *d_begin64 = nullptr, *d_begin32 = nullptr, *d_total64 = nullptr, *d_total32 = nullptr;
+    int* d_launch_bp = nullptr;  // per class launch: first block pair, block pairs
     float* d_dmax = nullptr;
     double skip_cut = 1e-12;
     // device buffers
@@ -275,6 +278,11 @@ int build_worklists(UnomolCtx* ctx) {
             ctx->d_pre32 = c.take<long long>(nrows);
             ctx->d_rowbp = c.take<int>(nrows);
             ctx->d_mseg = c.take<int>(nrows);
+            ctx->d_begin64 = c.take<long long>(nall);
+            ctx->d_begin32 = c.take<long long>(nall);
+            ctx->d_total64 = c.take<long long>(NPAIRCLASS * NPAIRCLASS);
+            ctx->d_total32 = c.take<long long>(NPAIRCLASS * NPAIRCLASS);
+            ctx->d_launch_bp = c.take<int>(2 * NPAIRCLASS * NPAIRCLASS);
         };
         Carve lay;
         lists(lay);
@@ -339,6 +347,12 @@ int build_worklists(UnomolCtx* ctx) {
         const size_t nr = (size_t)nrows;
         CU(cudaMemsetAsync(ctx->d_rowbp, 0xff, sizeof(int) * nr, s));
         CU(setup_row_bp(ctx->d_bps, (int)nbp, ctx->d_rowbp, s));
+        ctx->launch_bp.clear();
+        for (const ClassLaunch& L : ctx->launches) {
+            ctx->launch_bp.push_back(L.bp_begin);
+            ctx->launch_bp.push_back(L.nbp);
+        }
+        CU(cudaMemcpyAsync(ctx->d_launch_bp, ctx->launch_bp.data(), sizeof(int) * ctx->launch_bp.size(), cudaMemcpyHostToDevice, s));
         CU(cudaMemsetAsync(ctx->d_c64, 0, sizeof(long long) * nr, s));
         CU(cudaMemsetAsync(ctx->d_c32, 0, sizeof(long long) * nr, s));
         CU(cudaMemsetAsync(ctx->d_mseg, 0, sizeof(int) * nr, s));
@@ -581,7 +595,9 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                          std::max(ctx->fp32_cut, ctx->skip_cut), ctx->skip_cut, ctx->d_c64, ctx->d_c32, ctx->d_mseg, s));
         CU(wl_scan_rows(ctx->d_bps, (int)ctx->bps.size(), ctx->d_c64, ctx->d_c32, ctx->d_pre64, ctx->d_pre32, ctx->d_cnt64,
                         ctx->d_cnt32, s));
-        launches += 3;
+        CU(wl_scan_launches(ctx->d_launch_bp, (int)ctx->launches.size(), ctx->d_cnt64, ctx->d_cnt32, ctx->d_begin64,
+                            ctx->d_begin32, ctx->d_total64, ctx->d_total32, s));
+        launches += 4;
         A.dmax = ctx->d_dmax;
         A.skip_cut = ctx->skip_cut;
         A.dyn_mseg = ctx->d_mseg;
@@ -609,7 +625,8 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                         : launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s);
         return launch_fock_generic(la, lb, lc, ld, uhf, fp32, A, ctx->nt, ctx->d_rys, ctx->d_rys32, s);
     };
-    for (const ClassLaunch& L : ctx->launches) {
+    for (size_t li = 0; li < ctx->launches.size(); ++li) {
+        const ClassLaunch& L = ctx->launches[li];
         A.bps = ctx->d_bps + L.bp_begin;
         A.prefix = ctx->d_prefix;
         A.nbp = L.nbp;
@@ -623,11 +640,15 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             A.mode = 1;
             A.dyn_prefix = ctx->d_pre64;
             A.dyn_count = ctx->d_cnt64 + L.bp_begin;
+            A.dyn_begin = ctx->d_begin64 + L.bp_begin;
+            A.dyn_total = ctx->d_total64 + li;
             CU(launch_class(L, false));
             if (ctx->fp32_cut > ctx->skip_cut) {
                 A.mode = 2;
                 A.dyn_prefix = ctx->d_pre32;
                 A.dyn_count = ctx->d_cnt32 + L.bp_begin;
+                A.dyn_begin = ctx->d_begin32 + L.bp_begin;
+                A.dyn_total = ctx->d_total32 + li;
                 A.counter_base += ncls * 32;
                 CU(launch_class(L, true));
                 ++launches;

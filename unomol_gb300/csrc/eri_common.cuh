@@ -101,6 +101,9 @@ struct FockArgs {
     // work lists made on the device (split_rows + scan_rows)
     const long long* dyn_prefix;  // per bra row, exclusive prefix of this part's quartets (prefix layout)
     const long long* dyn_count;   // per block pair of this launch: quartets of this part
+    const long long* dyn_begin;   // per block pair of this launch: its first item in this part's compact
+                                  // numbering (counts rounded up to 32 and summed over the launch)
+    const long long* dyn_total;   // [0]: items of this part in the launch (the compact numbering's end)
     const int* dyn_mseg;          // per bra row: length of its FP64 segment (the FP32 segment follows it)
     const float* dmax;            // [0]: max |P| over all shell-pair blocks
     double skip_cut;              // quartets with bound * max|P| below this are skipped

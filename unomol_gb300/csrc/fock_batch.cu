@@ -131,6 +131,8 @@ struct UnomolBatch {
     int *d_rowbp = nullptr, *d_mseg = nullptr;
     long long *d_c64 = nullptr, *d_c32 = nullptr, *d_pre64 = nullptr, *d_pre32 = nullptr;
     long long *d_cnt64 = nullptr, *d_cnt32 = nullptr;
+    long long *d_begin64 = nullptr, *d_begin32 = nullptr, *d_total64 = nullptr, *d_total32 = nullptr;
+    int* d_launch_bp = nullptr;
     int rys_compat = 1;
     int nsm = 152;
     cudaStream_t stream = nullptr;
@@ -202,6 +204,8 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
         BCU(wl_split_rows(b->d_pairs, b->d_bps, b->d_rowbp, b->d_prefix, b->nrows, b->d_dmax,
                           std::max(b->fp32_cut, b->skip_cut), b->skip_cut, b->d_c64, b->d_c32, b->d_mseg, s));
         BCU(wl_scan_rows(b->d_bps, (int)b->nbps, b->d_c64, b->d_c32, b->d_pre64, b->d_pre32, b->d_cnt64, b->d_cnt32, s));
+        BCU(wl_scan_launches(b->d_launch_bp, (int)b->launches.size(), b->d_cnt64, b->d_cnt32, b->d_begin64, b->d_begin32,
+                             b->d_total64, b->d_total32, s));
         BCU(wl_to_float(b->d_Pfull, b->d_Pfull32, b->dense_total, s));
     }
     for (size_t k = 0; k < b->launches.size(); ++k) {
@@ -214,11 +218,15 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
         A.mode = 1;  // FP64 part
         A.dyn_prefix = b->d_pre64;
         A.dyn_count = b->d_cnt64 + L.bp_begin;
+        A.dyn_begin = b->d_begin64 + L.bp_begin;
+        A.dyn_total = b->d_total64 + k;
         BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, s));
         if (b->fp32_cut > b->skip_cut) {
             A.mode = 2;  // FP32 part
             A.dyn_prefix = b->d_pre32;
             A.dyn_count = b->d_cnt32 + L.bp_begin;
+            A.dyn_begin = b->d_begin32 + L.bp_begin;
+            A.dyn_total = b->d_total32 + k;
             A.tile_counter = b->d_tiles + 2 * k + 1;
             BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys32, b->nsm * L.ctas_per_sm, L.block, s));
         }
@@ -264,7 +272,20 @@ int ensure_mixed(UnomolBatch* b) {
     for (long long** p : {&b->d_c64, &b->d_c32, &b->d_pre64, &b->d_pre32}) BCU(cudaMalloc(p, sizeof(long long) * nr));
     BCU(cudaMalloc(&b->d_cnt64, sizeof(long long) * nbp));
     BCU(cudaMalloc(&b->d_cnt32, sizeof(long long) * nbp));
+    BCU(cudaMalloc(&b->d_begin64, sizeof(long long) * nbp));
+    BCU(cudaMalloc(&b->d_begin32, sizeof(long long) * nbp));
+    const size_t nl = std::max<size_t>(1, b->launches.size());
+    BCU(cudaMalloc(&b->d_total64, sizeof(long long) * nl));
+    BCU(cudaMalloc(&b->d_total32, sizeof(long long) * nl));
+    BCU(cudaMalloc(&b->d_launch_bp, sizeof(int) * 2 * nl));
+    std::vector<int> launch_bp;
+    for (const BLaunch& L : b->launches) {
+        launch_bp.push_back(L.bp_begin);
+        launch_bp.push_back(L.nbp);
+    }
     cudaStream_t s = b->stream;
+    if (!launch_bp.empty())
+        BCU(cudaMemcpyAsync(b->d_launch_bp, launch_bp.data(), sizeof(int) * launch_bp.size(), cudaMemcpyHostToDevice, s));
     long long p0 = 0;
     for (int m = 0; m < nmol; ++m) {
         const CtxView v = ctx_view(b->mols[m]);
@@ -592,7 +613,10 @@ void unomol_gpu_batch_destroy(UnomolBatch* b) {
     dfree(b->d_sl);
     dfree(b->d_rowbp);
     dfree(b->d_mseg);
-    for (long long** p : {&b->d_c64, &b->d_c32, &b->d_pre64, &b->d_pre32, &b->d_cnt64, &b->d_cnt32}) dfree(*p);
+    for (long long** p : {&b->d_c64, &b->d_c32, &b->d_pre64, &b->d_pre32, &b->d_cnt64, &b->d_cnt32, &b->d_begin64,
+                          &b->d_begin32, &b->d_total64, &b->d_total32})
+        dfree(*p);
+    dfree(b->d_launch_bp);
     dfree(b->d_tiles);
     for (UnomolCtx* c : b->mols) unomol_gpu_destroy(c);
     if (b->stream) cudaStreamDestroy(b->stream);

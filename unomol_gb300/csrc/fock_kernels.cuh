@@ -341,19 +341,19 @@ __device__ __forceinline__ bool decode_work(const FockArgs& A, long long g, int&
     return true;
 }
 
-// Decode for the per-build work lists of the density-screened / mixed-precision build: the launch
-// covers the static staircase of every block pair; this part (FP64: mode 1, FP32: mode 2) uses the
-// first dyn_count quartets of it.  Bra row i's FP64 segment is ket [0, mseg_i), its FP32 segment
-// ket [mseg_i, mseg_i + n32_i).
+// Decode for the per-build work lists of the density-screened / mixed-precision build: this part
+// (FP64: mode 1, FP32: mode 2) has dyn_count quartets in every block pair, numbered compactly over the
+// launch (block pair k from dyn_begin[k], counts rounded up to 32), so that items past dyn_total end at
+// once.  Bra row i's FP64 segment is ket [0, mseg_i), its FP32 segment ket [mseg_i, mseg_i + n32_i).
 __device__ __forceinline__ bool decode_work_dyn(const FockArgs& A, long long g, int& bra_idx, int& ket_idx) {
-    if (g >= A.nwork) return false;
-    int lo = 0, hi = A.nbp - 1;
+    if (g >= *A.dyn_total) return false;
+    int lo = 0, hi = A.nbp - 1;  // largest block pair with dyn_begin <= g (dyn_begin[0] = 0)
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (A.bps[mid].work_begin <= g) lo = mid; else hi = mid - 1;
+        if (A.dyn_begin[mid] <= g) lo = mid; else hi = mid - 1;
     }
     const BlockPair& bp = A.bps[lo];
-    const long long w = g - bp.work_begin;
+    const long long w = g - A.dyn_begin[lo];
     if (w >= A.dyn_count[lo]) return false;
     const long long* pre = A.dyn_prefix + bp.prefix_off;
     int a = 0, b = bp.bra_count - 1;
@@ -377,18 +377,20 @@ template <bool DYN>
 __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g, int& bra_idx, int& ket_idx) {
     const int lane = threadIdx.x & 31;
     const long long g0 = g - lane;
-    if (g0 >= A.nwork) return false;  // uniform over the warp
-    int lo = 0, hi = A.nbp - 1;       // largest block pair with work_begin <= g0 (bps[0].work_begin = 0)
+    if (g0 >= (DYN ? *A.dyn_total : A.nwork)) return false;  // uniform over the warp
+    int lo = 0, hi = A.nbp - 1;  // largest block pair whose first item is <= g0 (block pair 0 starts at 0)
     while (lo < hi) {
         const int step = (hi - lo + 32) >> 5;
         const int idx = lo + lane * step;
-        const unsigned m = __ballot_sync(0xffffffffu, idx <= hi && A.bps[idx].work_begin <= g0);
+        bool le = false;
+        if (idx <= hi) le = (DYN ? A.dyn_begin[idx] : A.bps[idx].work_begin) <= g0;
+        const unsigned m = __ballot_sync(0xffffffffu, le);
         lo += (31 - __clz(m)) * step;
         hi = min(hi, lo + step - 1);
     }
     const BlockPair& bp = A.bps[lo];
     const long long* pre = (DYN ? A.dyn_prefix : A.prefix) + bp.prefix_off;
-    const long long w0 = g0 - bp.work_begin;
+    const long long w0 = g0 - (DYN ? A.dyn_begin[lo] : bp.work_begin);
     const long long count = DYN ? A.dyn_count[lo] : bp.work_count;
     if (w0 >= count) return false;  // the whole warp lies past this part's quartets of the block pair
     int a = 0, b = bp.bra_count - 1;  // largest row with pre[row] <= w0 (pre[0] = 0)
@@ -600,12 +602,13 @@ __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const No
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __global__ void __launch_bounds__(256) fock_jk_persistent(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
     __shared__ long long tile;
+    const long long end = A.mode != 0 ? *A.dyn_total : A.nwork;  // screened parts: their compact numbering
     for (;;) {
         if (threadIdx.x == 0) tile = (long long)atomicAdd(A.tile_counter, 1ull);
         __syncthreads();
         const long long g0 = tile * blockDim.x;
         __syncthreads();
-        if (g0 >= A.nwork) return;
+        if (g0 >= end) return;
         fock_item<LA, LB, LC, LD, UHF, R>(A, nt, rys, g0 + threadIdx.x);
     }
 }

@@ -132,6 +132,74 @@ __global__ void __launch_bounds__(1024) scan_rows(const BlockPair* __restrict__ 
 }
 
 
+// Compact numbering of both parts per class launch: for the block pairs of launch l (first
+// launch_bp[2l], count launch_bp[2l+1]) begin[k] = sum over the launch's earlier block pairs of their
+// part's quartets rounded up to 32 (warps never straddle block pairs); total[l] = the sum over all.
+// One CTA per launch.
+__global__ void __launch_bounds__(1024) scan_launches(const int* __restrict__ launch_bp, const long long* __restrict__ n64,
+                                                      const long long* __restrict__ n32, long long* __restrict__ b64,
+                                                      long long* __restrict__ b32, long long* __restrict__ t64,
+                                                      long long* __restrict__ t32) {
+    __shared__ long long warp_a[32], warp_b[32];
+    __shared__ long long run_a, run_b;
+    const int first = launch_bp[2 * blockIdx.x], count = launch_bp[2 * blockIdx.x + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        run_a = 0;
+        run_b = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < count; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const long long va = i < count ? (n64[first + i] + 31) / 32 * 32 : 0;
+        const long long vb = i < count ? (n32[first + i] + 31) / 32 * 32 : 0;
+        long long sa = va, sb = vb;  // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
+            if (lane >= o) {
+                sa += xa;
+                sb += xb;
+            }
+        }
+        if (lane == 31) {
+            warp_a[wid] = sa;
+            warp_b[wid] = sb;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            const int nw = blockDim.x >> 5;
+            long long ta = lane < nw ? warp_a[lane] : 0, tb = lane < nw ? warp_b[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long xa = __shfl_up_sync(0xffffffffu, ta, o), xb = __shfl_up_sync(0xffffffffu, tb, o);
+                if (lane >= o) {
+                    ta += xa;
+                    tb += xb;
+                }
+            }
+            if (lane < nw) {
+                warp_a[lane] = ta;
+                warp_b[lane] = tb;
+            }
+        }
+        __syncthreads();
+        const long long wa = wid > 0 ? warp_a[wid - 1] : 0, wb = wid > 0 ? warp_b[wid - 1] : 0;
+        if (i < count) {
+            b64[first + i] = run_a + wa + sa - va;
+            b32[first + i] = run_b + wb + sb - vb;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            run_a += warp_a[(blockDim.x >> 5) - 1];
+            run_b += warp_b[(blockDim.x >> 5) - 1];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        t64[blockIdx.x] = run_a;
+        t32[blockIdx.x] = run_b;
+    }
+}
+
 // max |P| per shell-pair block for every molecule of a batch (one thread per block)
 __global__ void shell_pmax_batch(const double* __restrict__ P, const long long* __restrict__ doff, const int* __restrict__ nbf,
                                  const int* __restrict__ shell0, const int* __restrict__ nshell,
@@ -198,6 +266,14 @@ cudaError_t wl_scan_rows(const BlockPair* bps, int nbp, const long long* c64, co
                          long long* p32, long long* n64, long long* n32, cudaStream_t s) {
     if (nbp <= 0) return cudaSuccess;
     scan_rows<<<(unsigned)nbp, 512, 0, s>>>(bps, c64, c32, p64, p32, n64, n32);
+    return cudaGetLastError();
+}
+
+cudaError_t wl_scan_launches(const int* launch_bp, int nlaunch, const long long* n64, const long long* n32,
+                             long long* begin64, long long* begin32, long long* total64, long long* total32,
+                             cudaStream_t s) {
+    if (nlaunch <= 0) return cudaSuccess;
+    scan_launches<<<(unsigned)nlaunch, 1024, 0, s>>>(launch_bp, n64, n32, begin64, begin32, total64, total32);
     return cudaGetLastError();
 }
 

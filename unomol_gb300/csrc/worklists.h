@@ -23,5 +23,10 @@ cudaError_t wl_split_rows(const ShellPair* pairs, const BlockPair* bps, const in
                           int* mseg, cudaStream_t s);
 cudaError_t wl_scan_rows(const BlockPair* bps, int nbp, const long long* c64, const long long* c32, long long* p64,
                          long long* p32, long long* n64, long long* n32, cudaStream_t s);
+// compact numbering of both parts per class launch (launch l: block pairs launch_bp[2l] ..
+// + launch_bp[2l+1]): first item of every block pair and the launch's total, counts rounded up to 32
+cudaError_t wl_scan_launches(const int* launch_bp, int nlaunch, const long long* n64, const long long* n32,
+                             long long* begin64, long long* begin32, long long* total64, long long* total32,
+                             cudaStream_t s);
 
 }  // namespace ugb
