@@ -93,6 +93,10 @@ struct UnomolCtx {
     int* d_status = nullptr;
     unsigned long long* d_counters = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // mixed builds: the FP64 and the FP32 parts on two side streams forked from and joined back into
+    // the build's stream, so that the two kinds of kernels (FP64 pipe / FP32 pipe and loads) share the SMs
+    cudaStream_t part_stream[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
     // options
     double schwarz_cut = STORE_CUT;
     int prec_mode = UNOMOL_PREC_FP64;
@@ -617,7 +621,16 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     }
     // one class: the reference's integral method (Rys for la+lb+lc+ld <= 8, MD above:
     // TwoElectronInts.cpp:658-666; MD everywhere in the MD mode), templated kernels for s/p/d
-    auto launch_class = [&](const ClassLaunch& L, bool fp32) -> cudaError_t {
+    cudaStream_t ls[2] = {s, s};  // streams of the FP64 and FP32 launches (plain builds: alternate classes)
+    if (!ctx->counting) {
+        CU(cudaEventRecord(ctx->fork, s));
+        for (int k = 0; k < 2; ++k) {
+            CU(cudaStreamWaitEvent(ctx->part_stream[k], ctx->fork, 0));
+            ls[k] = ctx->part_stream[k];
+        }
+    }
+    auto launch_class = [&](const ClassLaunch& L, bool fp32, bool side = false) -> cudaError_t {
+        const cudaStream_t s = ls[(fp32 || side) ? 1 : 0];
         const int la = pc_la(L.bc), lb = pc_lb(L.bc), lc = pc_la(L.kc), ld = pc_lb(L.kc);
         if (ctx->eri_method == UNOMOL_ERI_MD || la + lb + lc + ld > 8) return launch_fock_md(la, lb, lc, ld, uhf, A, ctx->nt, s);
         if (L.bc < NTMPLCLASS && L.kc < NTMPLCLASS)
@@ -634,7 +647,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         A.counter_base = (L.bc * NPAIRCLASS + L.kc) * 32;  // FP32 launches use the second half
         if (!mixed) {
             A.mode = 0;
-            CU(launch_class(L, false));
+            CU(launch_class(L, false, (li & 1) != 0));
             ++launches;
         } else {
             A.mode = 1;
@@ -654,6 +667,12 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                 ++launches;
             }
             ++launches;
+        }
+    }
+    if (ls[0] != s) {  // join the two parts back into the build's stream
+        for (int k = 0; k < 2; ++k) {
+            CU(cudaEventRecord(ctx->join[k], ls[k]));
+            CU(cudaStreamWaitEvent(s, ctx->join[k], 0));
         }
     }
     CU(cudaEventRecord(ctx->ev[2], s));
@@ -808,6 +827,9 @@ int init_device(UnomolCtx* ctx, int np) {
     CU(cudaGetDevice(&ctx->dev));
     CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
+    for (auto& st : ctx->part_stream) CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+    for (auto& e : ctx->join) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     {
         const int rc = rys_tables(ctx->dev, ctx->d_rys, ctx->d_rys32, ctx->err);
         if (rc) return fail(ctx, rc, ctx->err);
@@ -1036,6 +1058,13 @@ void unomol_gpu_destroy(UnomolCtx* ctx) {
     dfree(ctx->d_Pb32);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ctx->fork, ctx->join[0], ctx->join[1]})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : ctx->part_stream)
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
