@@ -136,6 +136,8 @@ struct UnomolBatch {
     int rys_compat = 1;
     int nsm = 152;
     cudaStream_t stream = nullptr;
+    cudaStream_t part_stream[2] = {nullptr, nullptr};  // mixed builds: FP64 / FP32 parts side by side
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
     cudaGraphExec_t graph = nullptr;
     std::string err;
 };
@@ -208,6 +210,17 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
                              b->d_total64, b->d_total32, s));
         BCU(wl_to_float(b->d_Pfull, b->d_Pfull32, b->dense_total, s));
     }
+    // the FP64 and the FP32 parts on two streams forked from s (joined before the fold): their persistent
+    // CTAs share the SMs, one kind on the FP64 pipe, the other on the FP32 pipe and the loads
+    const bool split = mixed && b->fp32_cut > b->skip_cut;
+    cudaStream_t ls[2] = {s, s};
+    if (split) {
+        BCU(cudaEventRecord(b->fork, s));
+        for (int q = 0; q < 2; ++q) {
+            BCU(cudaStreamWaitEvent(b->part_stream[q], b->fork, 0));
+            ls[q] = b->part_stream[q];
+        }
+    }
     for (size_t k = 0; k < b->launches.size(); ++k) {
         const BLaunch& L = b->launches[k];
         FockArgs A = batch_args(b, L, (int)k);
@@ -220,7 +233,7 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
         A.dyn_count = b->d_cnt64 + L.bp_begin;
         A.dyn_begin = b->d_begin64 + L.bp_begin;
         A.dyn_total = b->d_total64 + k;
-        BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, s));
+        BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, ls[0]));
         if (b->fp32_cut > b->skip_cut) {
             A.mode = 2;  // FP32 part
             A.dyn_prefix = b->d_pre32;
@@ -228,9 +241,14 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
             A.dyn_begin = b->d_begin32 + L.bp_begin;
             A.dyn_total = b->d_total32 + k;
             A.tile_counter = b->d_tiles + 2 * k + 1;
-            BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys32, b->nsm * L.ctas_per_sm, L.block, s));
+            BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys32, b->nsm * L.ctas_per_sm, L.block, ls[1]));
         }
     }
+    if (split)
+        for (int q = 0; q < 2; ++q) {
+            BCU(cudaEventRecord(b->join[q], ls[q]));
+            BCU(cudaStreamWaitEvent(s, b->join[q], 0));
+        }
     batch_fold<<<(unsigned)((b->packed_total + 255) / 256), 256, 0, s>>>(b->d_T, b->d_doff, b->d_G, b->d_poff, b->d_nbf,
                                                                          nmol, b->packed_total);
     BCU(cudaGetLastError());
@@ -416,6 +434,9 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
     BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    for (auto& st : b->part_stream) BCU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    BCU(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    for (auto& e : b->join) BCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     BCU(cudaMalloc(&b->d_pairs, sizeof(ShellPair) * std::max<long long>(1, npair_tot)));
     BCU(cudaMalloc(&b->d_prims, sizeof(PrimPair) * std::max<long long>(1, nprim_tot)));
     BCU(cudaMalloc(&b->d_bps, sizeof(BlockPair) * std::max<size_t>(1, bps.size())));
@@ -619,6 +640,13 @@ void unomol_gpu_batch_destroy(UnomolBatch* b) {
     dfree(b->d_launch_bp);
     dfree(b->d_tiles);
     for (UnomolCtx* c : b->mols) unomol_gpu_destroy(c);
+    for (cudaEvent_t e : {b->fork, b->join[0], b->join[1]})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : b->part_stream)
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
