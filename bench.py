@@ -47,6 +47,11 @@ UNIT = "Fock builds/s"
 WORKLOAD = "32-water cluster, 6-31G, RHF, 416 basis functions (seed 0): Fock builds of the converging SCF"
 CPU_STRIDE = 64
 FP32_CUTOFF = 1e-3  # swept 1e-7..1e0 in profiles/fp32_cutoff_sweep_water32.md; |dE| stays ~1e-9 Eh here
+# quartets with Schwarz bound x max|dP| below this are skipped in a build: at 1e-12 the skipped parts of
+# ~1e8 quartets left 1e-9..1e-8 Eh of energy noise per incremental build, which stalled the 1e-10 Eh
+# test at FP32 cutoffs of 1e-6 and below; at 1e-13 every cutoff of the sweep converges in 11-12
+# iterations, for 1 % more build time at 1e-3
+SKIP_CUTOFF = 1e-13
 REBUILD = 8
 
 
@@ -278,7 +283,7 @@ def run_ours(args):
     mixed = native.TwoElectronInts(b)
     if args.form == "mixed":
         mixed.set_precision(native.PREC_MIXED, args.fp32_cutoff)
-        mixed.set_density_screening(1e-12)
+        mixed.set_density_screening(SKIP_CUTOFF)
         rm = native.scf(mixed, b, incremental=True, rebuild_every=REBUILD, **kw)
         inputs = step_inputs(rm["densities"])
     else:
@@ -326,7 +331,7 @@ def run_ours(args):
     # autotuned launch shapes, each build one CUDA-graph replay), same precision form
     bat = native.Batch([b])
     if args.form == "mixed":
-        bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, 1e-12)
+        bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, SKIP_CUTOFF)
     bat.set_densities([inputs[0][1]])
     tuned = bat.autotune(2)
     timed_batch_builds(bat, inputs, max(args.warmup, 3), dev, stream, flush)
@@ -383,7 +388,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if args.form == "mixed" else "f64",
             "data": "synthetic (generated 32-water geometry; densities of its own SCF)",
             "config": {"workload": WORKLOAD, "form": args.form, "fp32_cutoff": args.fp32_cutoff if args.form == "mixed" else None,
-                       "density_skip_cutoff": 1e-12 if args.form == "mixed" else None, "rebuild_every": REBUILD,
+                       "density_skip_cutoff": SKIP_CUTOFF if args.form == "mixed" else None, "rebuild_every": REBUILD,
                        "rys_mode": "reference-compatible", "schwarz_cutoff": 1e-14,
                        "l2": "flushed: 256 MiB write before every timed build", "nbf": b.norb,
                        "builds_in_sequence": len(inputs), "parallelism": f"replicas x{ws}",

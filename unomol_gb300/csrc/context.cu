@@ -76,7 +76,7 @@ struct UnomolCtx {
     long long *d_begin64 = nullptr, *d_begin32 = nullptr, *d_total64 = nullptr, *d_total32 = nullptr;
     int* d_launch_bp = nullptr;  // per class launch: first block pair, block pairs
     float* d_dmax = nullptr;
-    double skip_cut = 1e-12;
+    double skip_cut = 1e-13;
     // device buffers
     ShellPair* d_pairs = nullptr;
     PrimPair* d_prims = nullptr;

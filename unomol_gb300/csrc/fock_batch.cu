@@ -120,7 +120,7 @@ struct UnomolBatch {
     const float* rys32 = nullptr;
     // precision form (UNOMOL_PREC_MIXED): per-build work lists as for one context, over all molecules
     int prec_mode = UNOMOL_PREC_FP64;
-    double fp32_cut = 1e-10, skip_cut = 1e-12;
+    double fp32_cut = 1e-10, skip_cut = 1e-13;
     long long nrows = 0, pmax_total = 0;
     int nbps = 0;
     PrimPair32* d_prims32 = nullptr;

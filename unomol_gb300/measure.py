@@ -79,8 +79,8 @@ def _batch(reps: int, scf: bool = True) -> dict:
     bat.fock(native.BATCH_SEQUENTIAL)
     Gq = bat.get_focks()
     out["max_abs_dG_batch_vs_sequential"] = float(max(np.abs(a - c).max() for a, c in zip(Gb, Gq)))
-    # the precision form in the batched build (FP32 cutoff 1e-3, density skip 1e-12), same densities
-    bat.set_precision(native.PREC_MIXED, 1e-3, 1e-12)
+    # the precision form in the batched build (FP32 cutoff 1e-3, density skip 1e-13), same densities
+    bat.set_precision(native.PREC_MIXED, 1e-3, 1e-13)
     out["modes"]["mixed_graph"] = timeit(native.BATCH_GRAPH)
     Gm = bat.get_focks()
     out["mixed_max_abs_dG_vs_fp64"] = float(max(np.abs(a - c).max() for a, c in zip(Gm, Gb)))
@@ -152,7 +152,7 @@ def _sweep() -> dict:
     for cut in (1e0, 1e-1, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7):
         tm = native.TwoElectronInts(b)
         tm.set_precision(native.PREC_MIXED, cut)
-        tm.set_density_screening(1e-12)
+        tm.set_density_screening(1e-13)
         rm = native.scf(tm, b, incremental=True, **kw)
         Gm = tm.form_g(r64["P"])
         ms = rm["fock_ms"] / rm["fock_builds"]

@@ -425,7 +425,7 @@ class Batch:
             raise UnomolError(f"unomol_gb300 batch error {rc}: {msg}")
         return rc
 
-    def set_precision(self, mode: int, fp32_cutoff: float = 1e-10, skip_cutoff: float = 1e-12):
+    def set_precision(self, mode: int, fp32_cutoff: float = 1e-10, skip_cutoff: float = 1e-13):
         """Precision form of the batched build (PREC_FP64 or PREC_MIXED with the FP32 and density-skip
         cutoffs), as set_precision + set_density_screening of one context."""
         self._chk(lib().unomol_gpu_batch_set_precision(self._h, int(mode), float(fp32_cutoff), float(skip_cutoff)))
