@@ -434,7 +434,12 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
     BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-    for (auto& st : b->part_stream) BCU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    {
+        int lo = 0, hi = 0;  // the FP64 part first on the SMs, the FP32 part fills in (as for one context)
+        BCU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        BCU(cudaStreamCreateWithPriority(&b->part_stream[0], cudaStreamNonBlocking, hi));
+        BCU(cudaStreamCreateWithPriority(&b->part_stream[1], cudaStreamNonBlocking, lo));
+    }
     BCU(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     for (auto& e : b->join) BCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     BCU(cudaMalloc(&b->d_pairs, sizeof(ShellPair) * std::max<long long>(1, npair_tot)));
