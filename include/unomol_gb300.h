@@ -111,7 +111,8 @@ int unomol_gpu_fock_uhf_device(UnomolCtx* ctx, const double* dPa, const double* 
  *   build. */
 int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cutoff);
 
-/* skip_cut of the density-screened build (default 1e-12). */
+/* skip_cut of the density-screened build (default 1e-13: at 1e-12 the skipped quartets of a 416-function
+ * cluster left ~1e-9 Eh of noise per incremental build, too much for a 1e-10 Eh convergence test). */
 int unomol_gpu_set_density_screening(UnomolCtx* ctx, double skip_cut);
 
 /* Rys quadrature of the two-root classes (unomol_gpu_set_rys_mode).
