@@ -409,6 +409,10 @@ int build_setup(UnomolCtx* ctx) {
         ShellPair *raw, *sorted1;
         double *q, *q2;
         unsigned long long* qbits;
+        PrimPair* prims_c;      // primitive pairs in canonical order (before the interleave by block)
+        PrimPair32* prims32_c;
+        int *bbegin, *bcount;
+        long long* bprim;
         char* tmp;
     } a{};
     auto carve = [&](Carve& w) {
@@ -428,6 +432,11 @@ int build_setup(UnomolCtx* ctx) {
         a.q = w.take<double>(P);
         a.q2 = w.take<double>(P);
         a.qbits = w.take<unsigned long long>(P);
+        a.prims_c = w.take<PrimPair>(nprims);
+        a.prims32_c = w.take<PrimPair32>(nprims);
+        a.bbegin = w.take<int>(P);
+        a.bcount = w.take<int>(P);
+        a.bprim = w.take<long long>(P);
         a.tmp = w.take<char>(t_max);
     };
     Carve sizing;
@@ -442,7 +451,7 @@ int build_setup(UnomolCtx* ctx) {
     size_t tb = t_max;
     CU(setup_pair_keys(sh, P, a.key0, a.np, a.iota, s));
     CU(setup_exclusive_sum(a.tmp, tb, a.np, a.poff, P, s));
-    CU(setup_build_pairs(sh, P, a.poff, a.raw, ctx->d_prims, ctx->d_prims32, s));
+    CU(setup_build_pairs(sh, P, a.poff, a.raw, a.prims_c, a.prims32_c, s));
     tb = t_max;
     CU(setup_sort_keys(a.tmp, tb, a.key0, a.key1, a.iota, a.perm1, P, s));
     tb = t_max;
@@ -490,9 +499,9 @@ int build_setup(UnomolCtx* ctx) {
         const int cls = ctx->block_class[k], begin = ctx->block_begin[k];
         const int count = ctx->block_begin[k2 - 1] + ctx->block_count[k2 - 1] - begin;
         if (cls < NTMPLCLASS)
-            CU(launch_schwarz(cls, a.sorted1, ctx->d_prims, begin, count, ctx->nt, ctx->d_rys, a.q, s));
+            CU(launch_schwarz(cls, a.sorted1, a.prims_c, begin, count, ctx->nt, ctx->d_rys, a.q, s));
         else
-            CU(launch_schwarz_high(pc_la(cls), pc_lb(cls), a.sorted1, ctx->d_prims, begin, count, ctx->nt, ctx->d_rys, a.q,
+            CU(launch_schwarz_high(pc_la(cls), pc_lb(cls), a.sorted1, a.prims_c, begin, count, ctx->nt, ctx->d_rys, a.q,
                                    a.qbits, s));
         k = k2;
     }
@@ -504,6 +513,22 @@ int build_setup(UnomolCtx* ctx) {
     tb = t_max;
     CU(setup_sort_desc_segments(a.tmp, tb, a.q, a.q2, a.iota, a.perm2, P, nb, a.seg, a.seg + 1, s));
     CU(setup_gather_pairs(a.sorted1, a.perm2, a.q2, P, ctx->d_pairs, s));
+    // primitive pairs interleaved by block in the final order: adjacent pairs, adjacent records
+    {
+        std::vector<long long> bprim(nb);
+        long long o = 0;
+        for (int k = 0; k < nb; ++k) {
+            bprim[k] = o;
+            o += (long long)ctx->block_count[k] * ctx->block_nprim[k];
+        }
+        if (o != nprims) return fail(ctx, UNOMOL_ECUDA, "primitive pairs of the blocks do not add up");
+        CU(cudaMemcpyAsync(a.bbegin, ctx->block_begin.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(a.bcount, ctx->block_count.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(a.bprim, bprim.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice, s));
+        CU(setup_interleave_prims(ctx->d_pairs, P, a.bbegin, a.bcount, a.bprim, nb, a.prims_c, a.prims32_c, ctx->d_prims,
+                                  ctx->d_prims32, s));
+        CU(cudaStreamSynchronize(s));  // the host arrays above are copied from pageable memory
+    }
     return build_worklists(ctx);
 }
 

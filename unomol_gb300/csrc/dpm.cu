@@ -37,6 +37,7 @@ __global__ void __launch_bounds__(128) gdpm_kernel(const ShellPair* __restrict__
     ShellPair ket{};
     ket.prim_begin = gbegin;
     ket.nprim = GDPM_N;
+    ket.prim_stride = 1;
     double acc[Q::NF];
     shell_quartet_eri<LA, LB, 0, 0, double, PrimPair>(bra, ket, prims, rys, 0.0, compat != 0, acc);
 #pragma unroll

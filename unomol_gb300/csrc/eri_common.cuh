@@ -29,7 +29,7 @@ __host__ __device__ constexpr int cart_ly(int l, int c) {
 __host__ __device__ constexpr int cart_lz(int l, int c) { return l - cart_lx(l, c) - cart_ly(l, c); }
 
 // One primitive pair of a shell pair (a has the larger L after the swap of
-// TwoElectronInts.cpp:563-579).  72 bytes; the kernels read it through the read-only path.
+// TwoElectronInts.cpp:563-579); the kernels read it through the read-only path.
 struct __align__(16) PrimPair {
     double p;          // alpha_a + alpha_b
     double rp;         // 1 / p
@@ -38,7 +38,7 @@ struct __align__(16) PrimPair {
     double E;          // exp(-alpha_a alpha_b |AB|^2 / p) / p, coefficient free (prefactor screen)
     double cc;         // c_a c_b, times 2 for the i != j half of a same-shell pair
                        // (TwoElectronInts.cpp:444-449)
-    float pf, Ef;      // p and E in FP32, for a cheap pre-screen (80 bytes: five 16-byte loads)
+    float pf, Ef;      // p and E in FP32, for a cheap pre-screen (96 bytes: six 16-byte loads)
 };
 
 struct __align__(16) PrimPair32 {
@@ -51,8 +51,9 @@ struct __align__(16) PrimPair32 {
 struct ShellPair {
     int a_off, b_off;      // first AO of shell a (larger L) and of shell b
     int la, lb;            // la >= lb
-    int prim_begin, nprim; // range in the PrimPair array
-    int canon;             // canonical pair id ish*(ish+1)/2 + jsh (ish >= jsh, original order)
+    int prim_begin, nprim; // primitive pair ik of this pair at prim_begin + ik * prim_stride
+    int prim_stride;       // pairs of one block (equal nprim) interleave their primitive pairs: the
+                           // stride is the block's pair count, so consecutive pairs' records are adjacent
     int same;              // ish == jsh
     double AB[3];          // A - B
     double q;              // Schwarz bound: max over functions of sqrt|(ab|ab)|

@@ -213,7 +213,7 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     const R CDx = R(ket.AB[0]), CDy = R(ket.AB[1]), CDz = R(ket.AB[2]);
     const PP* pb = prims + bra.prim_begin;
     const PP* pk = prims + ket.prim_begin;
-    const int nb = bra.nprim, nk = ket.nprim;
+    const int nb = bra.nprim, nk = ket.nprim, sb = bra.prim_stride, sk = ket.prim_stride;
     // one surviving primitive quartet: bra record bp, ket record kp, rs = 1/sqrt(p+q), sr its prefactor
     auto primitive = [&](const PP& bp, const PP& kp, R rs, R sr) {
         const R p = bp.p, rp = bp.rp, cab = bp.cc;
@@ -258,8 +258,8 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     if (nparts > 1) {
         for (int t = part; t < nb * nk; t += nparts) {
             const int ib = t / nk, ik = t - ib * nk;
-            const PP bp = pb[ib];
-            const PP kp = pk[ik];
+            const PP bp = pb[ib * sb];
+            const PP kp = pk[ik * sk];
             const R rs = rsqrt(bp.p + kp.p);
             const R sr = R(SRTERM) * bp.E * kp.E * rs;
             if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
@@ -283,10 +283,10 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
             bool found = false;
             while (ib < nb) {
                 if (ib != cb) {
-                    bp = pb[ib];  // whole 16-byte-aligned records: vector loads
+                    bp = pb[ib * sb];  // whole 16-byte-aligned records: vector loads
                     cb = ib;
                 }
-                kp = pk[ik];
+                kp = pk[ik * sk];
                 if (++ik == nk) {
                     ik = 0;
                     ++ib;
@@ -307,9 +307,9 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     } else {
         // FP32 (bound by its loads, not by divergence): the plain nested loops
         for (int ib = 0; ib < nb; ++ib) {
-            const PP bp = pb[ib];
+            const PP bp = pb[ib * sb];
             for (int ik = 0; ik < nk; ++ik) {
-                const PP kp = pk[ik];
+                const PP kp = pk[ik * sk];
                 const R rs = rsqrt(bp.p + kp.p);
                 const R sr = R(SRTERM) * bp.E * kp.E * rs;
                 if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
@@ -718,16 +718,16 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
     const PP* pb = prims + bra.prim_begin;
     const PP* pk = prims + ket.prim_begin;
     for (int ib = 0; ib < bra.nprim; ++ib) {
-        const R p = pb[ib].p, rp = pb[ib].rp, Eab = pb[ib].E, cab = pb[ib].cc;
+        const R p = pb[ib * bra.prim_stride].p, rp = pb[ib * bra.prim_stride].rp, Eab = pb[ib * bra.prim_stride].E, cab = pb[ib * bra.prim_stride].cc;
         for (int ik = 0; ik < ket.nprim; ++ik) {
-            const R q = pk[ik].p, rq = pk[ik].rp, Ecd = pk[ik].E, ccd = pk[ik].cc;
+            const R q = pk[ik * ket.prim_stride].p, rq = pk[ik * ket.prim_stride].rp, Ecd = pk[ik * ket.prim_stride].E, ccd = pk[ik * ket.prim_stride].cc;
             const R rpq = R(1) / (p + q);
             R sr = R(SRTERM) * Eab * Ecd * sqrt(rpq);
             if (sr < prim_cut) continue;
             sr *= cab * ccd;
             ++npass;
             R PQ[3], x[5], w[5];
-            for (int k = 0; k < 3; ++k) PQ[k] = R(pb[ib].P[k]) - R(pk[ik].P[k]);
+            for (int k = 0; k < 3; ++k) PQ[k] = R(pb[ib * bra.prim_stride].P[k]) - R(pk[ik * ket.prim_stride].P[k]);
             const R T = p * q * rpq * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
             rys_roots_rt<R>(nr, T, rys, x, w, A.rys_compat != 0);
             for (int r = 0; r < nr; ++r) {
@@ -737,8 +737,8 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
                 const R B1p = (R(0.5) - B00 * p) * rq;
                 R I[3][GEN_NI];
                 for (int k = 0; k < 3; ++k)
-                    rys_axis_rt<R>(la, lb, lc, ld, k == 2 ? w[r] * sr : R(1), R(pb[ib].PA[k]) - q * fff * PQ[k],
-                                   R(pk[ik].PA[k]) + p * fff * PQ[k], B00, B1, B1p, R(bra.AB[k]), R(ket.AB[k]), I[k]);
+                    rys_axis_rt<R>(la, lb, lc, ld, k == 2 ? w[r] * sr : R(1), R(pb[ib * bra.prim_stride].PA[k]) - q * fff * PQ[k],
+                                   R(pk[ik * ket.prim_stride].PA[k]) + p * fff * PQ[k], B00, B1, B1p, R(bra.AB[k]), R(ket.AB[k]), I[k]);
                 int f = 0;
                 for (int ia = 0; ia < NA; ++ia)
                     for (int ibb = 0; ibb < NB; ++ibb)
@@ -830,13 +830,13 @@ static __global__ void __launch_bounds__(64) schwarz_generic(const ShellPair* __
     for (int f = 0; f < NA * NB; ++f) acc[f] = 0.0;
     const PrimPair* pp = prims + sp.prim_begin;
     for (int ib = 0; ib < sp.nprim; ++ib) {
-        const double p = pp[ib].p, rp = pp[ib].rp;
+        const double p = pp[ib * sp.prim_stride].p, rp = pp[ib * sp.prim_stride].rp;
         for (int ik = 0; ik < sp.nprim; ++ik) {
-            const double q = pp[ik].p, rq = pp[ik].rp;
+            const double q = pp[ik * sp.prim_stride].p, rq = pp[ik * sp.prim_stride].rp;
             const double rpq = 1.0 / (p + q);
-            const double sr = SRTERM * pp[ib].E * pp[ik].E * sqrt(rpq) * pp[ib].cc * pp[ik].cc;
+            const double sr = SRTERM * pp[ib * sp.prim_stride].E * pp[ik * sp.prim_stride].E * sqrt(rpq) * pp[ib * sp.prim_stride].cc * pp[ik * sp.prim_stride].cc;
             double PQ[3], x[5], w[5];
-            for (int k = 0; k < 3; ++k) PQ[k] = pp[ib].P[k] - pp[ik].P[k];
+            for (int k = 0; k < 3; ++k) PQ[k] = pp[ib * sp.prim_stride].P[k] - pp[ik * sp.prim_stride].P[k];
             const double T = p * q * rpq * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
             rys_roots_rt<double>(nr, T, rys, x, w);
             for (int r = 0; r < nr; ++r) {
@@ -844,8 +844,8 @@ static __global__ void __launch_bounds__(64) schwarz_generic(const ShellPair* __
                 const double B1 = (0.5 - B00 * q) * rp, B1p = (0.5 - B00 * p) * rq;
                 double I[3][GEN_NI];
                 for (int k = 0; k < 3; ++k)
-                    rys_axis_rt<double>(la, lb, la, lb, k == 2 ? w[r] * sr : 1.0, pp[ib].PA[k] - q * fff * PQ[k],
-                                        pp[ik].PA[k] + p * fff * PQ[k], B00, B1, B1p, sp.AB[k], sp.AB[k], I[k]);
+                    rys_axis_rt<double>(la, lb, la, lb, k == 2 ? w[r] * sr : 1.0, pp[ib * sp.prim_stride].PA[k] - q * fff * PQ[k],
+                                        pp[ik * sp.prim_stride].PA[k] + p * fff * PQ[k], B00, B1, B1p, sp.AB[k], sp.AB[k], I[k]);
                 for (int ia = 0; ia < NA; ++ia)
                     for (int ibb = 0; ibb < NB; ++ibb) {
                         const int ix = ((cart_lx(la, ia) * (lb + 1) + cart_lx(lb, ibb)) * (la + 1) + cart_lx(la, ia)) * (lb + 1) + cart_lx(lb, ibb);

@@ -87,16 +87,16 @@ __device__ double md_function_quartet(const ShellPair& bra, const ShellPair& ket
     const PrimPair* pb = prims + bra.prim_begin;
     const PrimPair* pk = prims + ket.prim_begin;
     for (int i = 0; i < bra.nprim; ++i) {
-        const double p = pb[i].p;
+        const double p = pb[i * bra.prim_stride].p;
         double Eab[3][2 * MD_LMAX + 1];
-        for (int k = 0; k < 3; ++k) md_hermite(va[k], vb[k], 0.5 * pb[i].rp, pb[i].PA[k], pb[i].PA[k] + bra.AB[k], Eab[k]);
+        for (int k = 0; k < 3; ++k) md_hermite(va[k], vb[k], 0.5 * pb[i * bra.prim_stride].rp, pb[i * bra.prim_stride].PA[k], pb[i * bra.prim_stride].PA[k] + bra.AB[k], Eab[k]);
         for (int j = 0; j < ket.nprim; ++j) {
-            const double q = pk[j].p;
+            const double q = pk[j * ket.prim_stride].p;
             double Ecd[3][2 * MD_LMAX + 1];
-            for (int k = 0; k < 3; ++k) md_hermite(vc[k], vd[k], 0.5 * pk[j].rp, pk[j].PA[k], pk[j].PA[k] + ket.AB[k], Ecd[k]);
-            const double sr = SRTERM * pb[i].E * pk[j].E * pb[i].cc * pk[j].cc / sqrt(p + q);
+            for (int k = 0; k < 3; ++k) md_hermite(vc[k], vd[k], 0.5 * pk[j * ket.prim_stride].rp, pk[j * ket.prim_stride].PA[k], pk[j * ket.prim_stride].PA[k] + ket.AB[k], Ecd[k]);
+            const double sr = SRTERM * pb[i * bra.prim_stride].E * pk[j * ket.prim_stride].E * pb[i * bra.prim_stride].cc * pk[j * ket.prim_stride].cc / sqrt(p + q);
             const double rho = p * q / (p + q);
-            const double PQ[3] = {pb[i].P[0] - pk[j].P[0], pb[i].P[1] - pk[j].P[1], pb[i].P[2] - pk[j].P[2]};
+            const double PQ[3] = {pb[i * bra.prim_stride].P[0] - pk[j * ket.prim_stride].P[0], pb[i * bra.prim_stride].P[1] - pk[j * ket.prim_stride].P[1], pb[i * bra.prim_stride].P[2] - pk[j * ket.prim_stride].P[2]};
             double F[MD_LT + 1];
             md_boys_reference(L, rho * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]), F);
             // R^{(n)}_{tuv} for n = L .. 0 inside the box, t + u + v <= L - n

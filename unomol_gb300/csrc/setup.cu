@@ -53,7 +53,7 @@ __global__ void k_build_pairs(const ShellsDev sh, int npairs, const int* __restr
     sp.ish = ish;
     sp.jsh = jsh;
     sp.maxsh = ish;
-    sp.canon = c;
+    sp.prim_stride = 1;  // canonical layout until the pairs are interleaved by block
     sp.same = ish == jsh;
     sp.la = sh.sl[a];
     sp.lb = sh.sl[b];
@@ -146,6 +146,33 @@ __global__ void k_row_bp(const BlockPair* __restrict__ bps, int* __restrict__ ro
     for (int i = threadIdx.x; i < bp.bra_count; i += blockDim.x) row_bp[bp.prefix_off + i] = (int)blockIdx.x;
 }
 
+// Final layout of the primitive pairs: block b (pairs bbegin[b] .. + bcount[b], all with the same
+// primitive-pair count) owns records bprim[b] .. + bcount[b] * nprim, and primitive ik of its j-th pair
+// sits at bprim[b] + ik * bcount[b] + j, so that the lanes of a warp, which hold consecutive pairs of a
+// block, read adjacent records.  One thread per pair; src is the canonical layout.
+__global__ void k_interleave_prims(ShellPair* __restrict__ pairs, int n, const int* __restrict__ bbegin,
+                                   const int* __restrict__ bcount, const long long* __restrict__ bprim, int nb,
+                                   const PrimPair* __restrict__ src, const PrimPair32* __restrict__ src32,
+                                   PrimPair* __restrict__ dst, PrimPair32* __restrict__ dst32) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int lo = 0, hi = nb - 1;  // the block: last with bbegin <= k
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bbegin[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    const int j = k - bbegin[lo], cnt = bcount[lo];
+    ShellPair sp = pairs[k];
+    const long long first = bprim[lo] + j;
+    for (int ik = 0; ik < sp.nprim; ++ik) {
+        dst[first + (long long)ik * cnt] = src[sp.prim_begin + ik];
+        dst32[first + (long long)ik * cnt] = src32[sp.prim_begin + ik];
+    }
+    sp.prim_begin = (int)first;
+    sp.prim_stride = cnt;
+    pairs[k] = sp;
+}
+
 __global__ void k_offset_pairs(ShellPair* __restrict__ pairs, int n, int prim0, int mol) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -192,6 +219,14 @@ cudaError_t setup_prefix_fix(const BlockPair* bps, int nbp, const long long* S, 
 cudaError_t setup_row_bp(const BlockPair* bps, int nbp, int* row_bp, cudaStream_t s) {
     if (nbp <= 0) return cudaSuccess;
     k_row_bp<<<(unsigned)nbp, 128, 0, s>>>(bps, row_bp);
+    return cudaGetLastError();
+}
+
+cudaError_t setup_interleave_prims(ShellPair* pairs, int n, const int* bbegin, const int* bcount, const long long* bprim,
+                                   int nb, const PrimPair* src, const PrimPair32* src32, PrimPair* dst, PrimPair32* dst32,
+                                   cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_interleave_prims<<<blocks_for(n, 128), 128, 0, s>>>(pairs, n, bbegin, bcount, bprim, nb, src, src32, dst, dst32);
     return cudaGetLastError();
 }
 

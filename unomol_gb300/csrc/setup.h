@@ -41,6 +41,12 @@ cudaError_t setup_prefix_fix(const BlockPair* bps, int nbp, const long long* S, 
                              cudaStream_t s);
 // row_bp[prefix_off + i] = k for the bra rows of block pair k (other entries untouched)
 cudaError_t setup_row_bp(const BlockPair* bps, int nbp, int* row_bp, cudaStream_t s);
+// primitive pairs of the sorted pairs moved from the canonical layout (src) into the block-interleaved
+// one (dst): block b's pairs bbegin[b] .. + bcount[b] own records bprim[b] .., primitive ik of its j-th
+// pair at bprim[b] + ik * bcount[b] + j; prim_begin / prim_stride of the pairs updated
+cudaError_t setup_interleave_prims(ShellPair* pairs, int n, const int* bbegin, const int* bcount, const long long* bprim,
+                                   int nb, const PrimPair* src, const PrimPair32* src32, PrimPair* dst, PrimPair32* dst32,
+                                   cudaStream_t s);
 // ShellPair::prim_begin += prim0 and ShellPair::pad = mol for n pairs (merging molecules into a batch)
 cudaError_t setup_offset_pairs(ShellPair* pairs, int n, int prim0, int mol, cudaStream_t s);
 
