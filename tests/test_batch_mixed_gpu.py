@@ -74,3 +74,31 @@ def test_batch_all_fp32_within_fp32_accuracy(gpu, batch_case):
     bat.fock(native.BATCH_GRAPH)
     for name, g, G in zip(NAMES, gs, bat.get_focks()):
         assert np.abs(G - g["G_rand"]).max() <= 1e-10, name
+
+
+@pytest.mark.gpu
+def test_batch_build_on_device_buffers(gpu, batch_case):
+    """unomol_gpu_batch_fock_device: the caller's packed densities in and packed G out, on the caller's
+    stream, equal to the build on the batch's own buffers."""
+    import torch
+    from unomol_gb300 import native
+    gs, bases = batch_case
+    bat = native.Batch(bases)
+    Ps = [g["P_rand"] for g in gs]
+    bat.set_precision(native.PREC_MIXED, 1e-3, 1e-13)
+    bat.set_densities(Ps)
+    bat.fock(native.BATCH_GRAPH)
+    G_own = bat.get_focks()
+    dev = torch.device("cuda", 0)
+    dP = torch.from_numpy(np.concatenate(Ps)).to(dev)
+    dG = torch.zeros_like(dP)
+    s = torch.cuda.Stream(dev)
+    bat.set_densities([np.zeros_like(P) for P in Ps])  # the batch's own buffer no longer holds the input
+    for mode in (native.BATCH_GRAPH, native.BATCH_LAUNCHES):
+        dG.zero_()
+        torch.cuda.synchronize(dev)
+        bat.fock_device(dP.data_ptr(), dG.data_ptr(), mode, s.cuda_stream)
+        torch.cuda.synchronize(dev)
+        G = dG.cpu().numpy()
+        for o, b, Go in zip(bat.offsets, bases, G_own):
+            assert np.abs(G[o:o + b.no2] - Go).max() <= 1e-12 * max(1.0, np.abs(Go).max()), mode
