@@ -646,11 +646,19 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     }
     // one class: the reference's integral method (Rys for la+lb+lc+ld <= 8, MD above:
     // TwoElectronInts.cpp:658-666; MD everywhere in the MD mode), templated kernels for s/p/d
+#ifndef UGB_FUSED_MIXED
+#define UGB_FUSED_MIXED 1
+#endif
+    // mixed builds with both parts: the FP64 and FP32 parts of a templated class in one launch
+    // (fock_jk_mixed), classes alternating over two equal-priority streams; otherwise the FP64 part on a
+    // high-priority stream and the FP32 part on a second one
+    const bool split = mixed && ctx->fp32_cut > ctx->skip_cut;
+    const bool fused = split && UGB_FUSED_MIXED && ctx->eri_method != UNOMOL_ERI_MD;
     cudaStream_t ls[2] = {s, s};  // streams of the FP64 and FP32 launches (plain builds: alternate classes)
     if (!ctx->counting) {
         CU(cudaEventRecord(ctx->fork, s));
-        ls[0] = ctx->part_stream[mixed ? 0 : 1];
-        ls[1] = ctx->part_stream[mixed ? 1 : 2];
+        ls[0] = ctx->part_stream[mixed && !fused ? 0 : 1];
+        ls[1] = ctx->part_stream[mixed && !fused ? 1 : 2];
         for (int k = 0; k < 2; ++k) CU(cudaStreamWaitEvent(ls[k], ctx->fork, 0));
     }
     auto launch_class = [&](const ClassLaunch& L, bool fp32, bool side = false) -> cudaError_t {
@@ -679,6 +687,18 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             A.dyn_count = ctx->d_cnt64 + L.bp_begin;
             A.dyn_begin = ctx->d_begin64 + L.bp_begin;
             A.dyn_total = ctx->d_total64 + li;
+            if (fused && fock_mixed_fused(L.bc, L.kc) && pc_la(L.bc) + pc_lb(L.bc) + pc_la(L.kc) + pc_lb(L.kc) <= 8) {
+                FockArgs A32 = A;
+                A32.mode = 2;
+                A32.dyn_prefix = ctx->d_pre32;
+                A32.dyn_count = ctx->d_cnt32 + L.bp_begin;
+                A32.dyn_begin = ctx->d_begin32 + L.bp_begin;
+                A32.dyn_total = ctx->d_total32 + li;
+                A32.counter_base += ncls * 32;
+                CU(launch_fock_mixed(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ls[li & 1]));
+                ++launches;
+                continue;
+            }
             CU(launch_class(L, false));
             if (ctx->fp32_cut > ctx->skip_cut) {
                 A.mode = 2;

@@ -17,6 +17,11 @@ cudaError_t launch_fock_fp64(int bc, int kc, bool uhf, const FockArgs& A, const 
                              const double* rys, cudaStream_t stream);
 cudaError_t launch_fock_fp32(int bc, int kc, bool uhf, const FockArgs& A, const NormTable& nt,
                              const float* rys, cudaStream_t stream);
+// Both parts of a mixed build of one class in one launch (their CTAs alternate); only for the classes
+// that fock_mixed_fused accepts (templated, at most 81 function quartets).
+bool fock_mixed_fused(int bc, int kc);
+cudaError_t launch_fock_mixed(int bc, int kc, bool uhf, const FockArgs& A64, const FockArgs& A32, const NormTable& nt,
+                              const double* rys64, const float* rys32, cudaStream_t stream);
 cudaError_t launch_schwarz(int pc, const ShellPair* pairs, const PrimPair* prims, int begin, int count,
                            const NormTable& nt, const double* rys, double* q_out, cudaStream_t stream);
 

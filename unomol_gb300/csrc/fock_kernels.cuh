@@ -595,6 +595,22 @@ __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const No
     fock_item<LA, LB, LC, LD, UHF, R>(A, nt, rys, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// Mixed builds: the FP64 part (A64, mode 1) and the FP32 part (A32, mode 2) of one class in one launch
+// of 2 x nblk CTAs, alternating (even CTAs FP64, odd CTAs FP32).  Both parts number their quartets
+// compactly from 0, so their working CTAs come first in the grid and an SM holds both kinds at once:
+// warps on the FP64 pipe beside warps on the FP32 pipe and the loads.  CTAs past a part's total end at
+// their first load.
+template <int LA, int LB, int LC, int LD, bool UHF>
+__global__ void __launch_bounds__(128) fock_jk_mixed(const FockArgs A64, const FockArgs A32, const NormTable nt,
+                                                      const double* __restrict__ rys64,
+                                                      const float* __restrict__ rys32) {
+    const long long g = (long long)(blockIdx.x >> 1) * blockDim.x + threadIdx.x;
+    if (blockIdx.x & 1)
+        fock_item<LA, LB, LC, LD, UHF, float>(A32, nt, rys32, g);
+    else
+        fock_item<LA, LB, LC, LD, UHF, double>(A64, nt, rys64, g);
+}
+
 // Persistent form for batches of molecules: a fixed grid of CTAs (a few per SM) pulls tiles of
 // blockDim consecutive work items from an atomic counter until the launch's work is done, so that
 // molecules of uneven size balance across the GPU in one launch per class.  Tiles follow the work
