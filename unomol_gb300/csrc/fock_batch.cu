@@ -233,6 +233,19 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
         A.dyn_count = b->d_cnt64 + L.bp_begin;
         A.dyn_begin = b->d_begin64 + L.bp_begin;
         A.dyn_total = b->d_total64 + k;
+        // both parts of a templated class in one grid launch with alternating CTAs (fock_jk_mixed, as for
+        // one molecule; the merged work lists balance the molecules): 14 % faster than the two persistent
+        // parts for the 32-water cluster, the same for 256 molecules
+        if (split && fock_mixed_fused(L.bc, L.kc)) {
+            FockArgs A32 = A;
+            A32.mode = 2;
+            A32.dyn_prefix = b->d_pre32;
+            A32.dyn_count = b->d_cnt32 + L.bp_begin;
+            A32.dyn_begin = b->d_begin32 + L.bp_begin;
+            A32.dyn_total = b->d_total32 + k;
+            BCU(launch_fock_mixed(L.bc, L.kc, false, A, A32, b->nt, b->rys, b->rys32, ls[k & 1]));
+            continue;
+        }
         BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, ls[0]));
         if (b->fp32_cut > b->skip_cut) {
             A.mode = 2;  // FP32 part
