@@ -7,7 +7,9 @@
 // of blocks the Schwarz "staircase" (bra i keeps the first n_i ket pairs) gives a compact work list per
 // quartet class.  The host keeps the block boundaries and the block-pair list.
 // Fock build (fock_rhf / fock_uhf): expand packed P to a dense N x N copy, zero the accumulators,
-// launch one kernel per quartet class, fold G += T + T^T into packed storage.
+// launch one kernel per quartet class (classes alternating over two streams forked from the build's
+// stream; in the mixed-precision build both parts of a class in one launch), fold G += T + T^T into
+// packed storage.
 #include <algorithm>
 #include <climits>
 #include <memory>

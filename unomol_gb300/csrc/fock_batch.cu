@@ -1,7 +1,9 @@
 // Batched Fock build over many molecules (the batching form): merged work lists, one persistent kernel
 // per quartet class pulling tiles from an atomic counter, the whole build captured as a CUDA graph,
 // and an autotuner choosing the CTA size (quartets per tile) and the CTAs per SM of every class.
-// FP64, RHF, shells up to d (the batch workload is s/p).
+// RHF, shells up to d (the batch workload is s/p); FP64, or the precision form (per-build FP64 / FP32 /
+// skipped parts with each molecule's own density bound), whose two parts of a templated class run as
+// one grid launch with alternating CTAs.
 #include <algorithm>
 #include <climits>
 #include <cstring>
