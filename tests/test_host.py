@@ -49,6 +49,27 @@ def test_bad_basis_rejected_before_device_use():
     assert L.unomol_gpu_create(None, 0, C.byref(h)) == -1
 
 
+@pytest.mark.parametrize("field,index,value,message", [
+    ("l", 0, 5, "angular momentum above 4"),
+    ("np", 0, 0, "no primitives"),
+    ("np", 1, 256, "more than 255 primitives"),
+    ("c", 0, 99, "centre out of range"),
+    ("o", 1, 0, "offsets must follow shell order"),
+])
+def test_malformed_basis_is_reported_on_any_machine(field, index, value, message):
+    """A malformed basis description is rejected (UNOMOL_EINVAL, with the reason) before any device use."""
+    from unomol_gb300 import native
+    L = native.lib()
+    g = load_golden("h2o_631g")
+    d, keep = native.basis_desc(basis_of(g))
+    keep[field][index] = value
+    h = C.c_void_p()
+    L.unomol_gpu_create.argtypes = [C.POINTER(native.BasisDesc), C.c_int, C.POINTER(C.c_void_p)]
+    assert L.unomol_gpu_create(C.byref(d), 0, C.byref(h)) == -1
+    assert message in L.unomol_gpu_last_error(None).decode()
+    assert not h.value
+
+
 @pytest.mark.parametrize("name", golden_cases())
 def test_one_electron_matches_reference(name):
     from unomol_gb300 import native

@@ -942,9 +942,6 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
     if (b->nshell <= 0 || b->ncen <= 0 || b->norb <= 0 || !b->shell_l || !b->shell_nprim || !b->shell_center ||
         !b->shell_offset || !b->alpha || !b->coef || !b->centers)
         return fail(nullptr, UNOMOL_EINVAL, "incomplete basis description");
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-        return fail(nullptr, UNOMOL_ENODEV, "no CUDA device: the GB300 Fock build has no CPU fallback");
     std::unique_ptr<UnomolCtx> c(new UnomolCtx());
     ctx = c.get();
     ctx->nshell = b->nshell;
@@ -969,6 +966,10 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
         ctx->maxl = std::max(ctx->maxl, l);
     }
     if (off != b->norb) return fail(nullptr, UNOMOL_EINVAL, "norb does not match the shells");
+    // the basis is checked first, so that a bad description is reported as such on any machine
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, UNOMOL_ENODEV, "no CUDA device: the GB300 Fock build has no CPU fallback");
     ctx->alpha.assign(b->alpha, b->alpha + np);
     ctx->coef.assign(b->coef, b->coef + np);
     ctx->centers.assign(b->centers, b->centers + 3 * b->ncen);
