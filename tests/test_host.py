@@ -130,3 +130,19 @@ def test_molecule_generators():
 def test_oracle_port_builds_without_reference():
     r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_batch_workload_generator():
+    """The 256-molecule batching workload: half alkanes C1-C8, half clusters of 1-6 waters, STO-3G or
+    6-31G per molecule, reproducible from its seed; 7 to 108 basis functions (C8H18/6-31G is the
+    largest molecule the rules allow)."""
+    from unomol_gb300 import molecules
+    from unomol_gb300.basis import Basis
+    work = molecules.batch_workload(seed=0)
+    assert len(work) == 256
+    labels = [l for l, _ in work]
+    assert all(l.startswith("C") for l in labels[:128]) and all(l.startswith("(H2O)") for l in labels[128:])
+    assert {l.split("/")[1] for l in labels} == {"STO-3G", "6-31G"}
+    nbf = [Basis(text=t).norb for _, t in work]
+    assert min(nbf) >= 7 and max(nbf) <= 108 and sum(nbf) == 11246
+    assert [l for l, _ in molecules.batch_workload(seed=0)] == labels
