@@ -19,7 +19,8 @@ k = 0, 8, ..., else the density change), cycled for K steps.
   plain_fp64   the plain FP64 path on the same densities (full builds), device-timed the same way;
   roofline the ERI + J/K kernels of one build against the FP64 and FP32 FMA peaks measured by the
            library's own microbenchmark (the kernels are bound by those pipes, not by HBM or tensor
-           cores): peak = flops / (flops64/peak64 + flops32/peak32);
+           cores): peak = flops / max(flops64/peak64, flops32/peak32), the two pipes busy at once
+           (peak_one_after_other = flops / (flops64/peak64 + flops32/peak32) beside it);
   cpu_baseline the C restatement of the reference algorithm (oracle/) on the host cores, on a strided
            sample of the shell quartets of one full build.
 --impl reference: that CPU implementation as the reference arm (same metric and workload).
@@ -29,6 +30,7 @@ Multi-GPU: replicas only (every rank runs the whole workload; value sums over ra
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import statistics
@@ -67,47 +69,80 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling of the timed region.
 
-    def __init__(self, index: int):
+    The sampler is started before the warm-up, so that it is live when the timed region opens
+    (start()); it is stopped only after a sample taken at or after the region's end, so that even a
+    region shorter than the sampling period has a sample.  The reported figures use the samples taken
+    after start(): those inside the region and the first one after it, while the clocks of the load
+    still hold."""
+
+    PERIOD_MS = 100
+    FIELDS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, index: int, exe: str = "nvidia-smi"):
         self.p = None
+        self.first = 0
         self.path = os.path.join(os.environ.get("UNOMOL_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_{os.getpid()}.csv")
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(
-                ["nvidia-smi", f"--id={index}", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                [exe, f"--id={index}", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
                  "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+            return
+        atexit.register(self._end)  # no sampler outlives the process, whatever path it leaves by
+
+    def _end(self):
+        if self.p is not None and self.p.poll() is None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return [l for l in f.read().splitlines() if l.count(",") >= 8]
+        except OSError:
+            return []
+
+    def _wait_for(self, n: int, timeout_s: float):
+        t_end = time.monotonic() + timeout_s
+        while len(self._lines()) < n and time.monotonic() < t_end and self.p.poll() is None:
+            time.sleep(0.01)
+
+    def start(self):
+        """Marks the opening of the timed region (call right before it)."""
+        if self.p is not None:
+            self._wait_for(1, 3.0)  # the sampler is live
+            self.first = len(self._lines())
 
     def stop(self):
+        """Ends sampling after the timed region and summarises the samples taken since start()."""
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.p.terminate()
-        try:
-            self.p.wait(timeout=5)
-        except Exception:
-            self.p.kill()
+        self._wait_for(len(self._lines()) + 1, 2.0)  # one sample at or after the region's end
+        self._end()
         self.f.close()
         sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in self._lines()[self.first:]:
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
-                continue
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
+            for nm, v in zip(self.FIELDS, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "period_ms": self.PERIOD_MS}
 
 
 def ensure_oracle():
@@ -307,13 +342,14 @@ def run_ours(args):
         print(json.dumps({"profile_builds": args.steps, "form": args.form}), flush=True)
         return 0
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    clocks = Clocks(local)
     # warm-up, then the counted (untimed) pass for the algorithmic flops
     timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
     f64, f32, launches, nq, nq32, nfq = counted_flops(mixed, inputs, dev, stream)
     # timed region
     replicas.barrier(ws)
     torch.cuda.synchronize(dev)
-    clocks = Clocks(local)
+    clocks.start()
     step_ms, eri_ms = timed_builds(mixed, inputs, args.steps, dev, stream, flush)
     torch.cuda.synchronize(dev)
     replicas.barrier(ws)

@@ -24,3 +24,46 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+FAKE_SMI = r'''#!{python}
+import sys, time
+period = float(sys.argv[sys.argv.index("-lms") + 1]) / 1e3
+k = 0
+while True:
+    mhz = 1500 if k == 0 else 2070  # the first sample: before the load
+    print(f"0, {{mhz}}, 2070, 900.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active", flush=True)
+    k += 1
+    time.sleep(period)
+'''
+
+
+def test_clock_sampler_brackets_short_region(tmp_path, monkeypatch):
+    """The sampler is live before the timed region opens and keeps a sample taken at or after its end,
+    so a region shorter than the sampling period still has one; samples from before the region are not
+    counted; throttle reasons reported Active are listed."""
+    sys.path.insert(0, ROOT)
+    import bench
+    exe = tmp_path / "nvidia-smi"
+    exe.write_text(FAKE_SMI.format(python=sys.executable))
+    exe.chmod(0o755)
+    monkeypatch.setenv("UNOMOL_CLOCKS_DIR", str(tmp_path))
+    c = bench.Clocks(0, exe=str(exe))
+    import time
+    time.sleep(0.35)  # warm-up
+    c.start()
+    time.sleep(0.01)  # a region far shorter than the period
+    clk = c.stop()
+    assert clk["samples"] >= 1
+    assert clk["sm_mhz"] == 2070.0 and clk["sm_max_mhz"] == 2070.0
+    assert clk["reasons"] == ["sw_power_cap"]
+    assert c.p.poll() is not None  # the sampler has ended
+
+
+def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("UNOMOL_CLOCKS_DIR", str(tmp_path))
+    c = bench.Clocks(0, exe=str(tmp_path / "absent"))
+    c.start()
+    assert c.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
