@@ -49,6 +49,39 @@ def test_bad_basis_rejected_before_device_use():
     assert L.unomol_gpu_create(None, 0, C.byref(h)) == -1
 
 
+def _header_declarations():
+    txt = open(os.path.join(ROOT, "include", "unomol_gb300.h")).read()
+    out = []
+    for ret, name, params in re.findall(r"^(int|void|const char\*)\s+(unomol_\w+)\(([^;]*?)\);", txt, re.M | re.S):
+        out.append((ret, name, len([p for p in params.split(",") if p.strip() and p.strip() != "void"])))
+    return out
+
+
+def test_every_entry_point_rejects_null_arguments():
+    """Every entry point called with null handles and pointers (zero sizes) returns UNOMOL_EINVAL
+    (-1), destroys are no-ops and the error-string getters return a string: nothing dereferences a
+    null argument or reaches the device first."""
+    from unomol_gb300 import native
+    L = native.lib()
+    decls = _header_declarations()
+    assert len(decls) >= 50
+    for ret, name, n in decls:
+        f = getattr(L, name)
+        f.argtypes = [C.c_void_p] * n
+        if ret == "int":
+            f.restype = C.c_int
+            if name in ("unomol_gpu_batch_size", "unomol_guess_num_molecules"):
+                assert f(*([None] * n)) < 0, name
+            else:
+                assert f(*([None] * n)) == -1, name
+        elif ret == "void":
+            f.restype = None
+            f(*([None] * n))
+        else:
+            f.restype = C.c_char_p
+            assert isinstance(f(*([None] * n)), bytes), name
+
+
 @pytest.mark.parametrize("field,index,value,message", [
     ("l", 0, 5, "angular momentum above 4"),
     ("np", 0, 0, "no primitives"),
