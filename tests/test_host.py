@@ -41,9 +41,26 @@ def test_create_without_gpu_fails_loudly():
         native.TwoElectronInts(basis_of(g))
 
 
-def test_bad_basis_rejected_before_device_use():
+def _private_handle():
+    """A CDLL object of its own, so that argument types set by a test leave the bindings' untouched."""
     from unomol_gb300 import native
-    L = native.lib()
+    native.lib()
+    return C.CDLL(native.LIB_PATH)
+
+
+def test_missing_library_fails_loudly(monkeypatch):
+    """Without the built library every binding raises: there is no CPU fallback."""
+    from unomol_gb300 import native
+    monkeypatch.setattr(native, "_LIB", None)
+    monkeypatch.setattr(native, "LIB_PATH", os.path.join(ROOT, "no_such_dir", "libunomol_gb300.so"))
+    with pytest.raises(native.UnomolError, match="no CPU fallback"):
+        native.lib()
+    with pytest.raises(native.UnomolError, match="is missing"):
+        native.TwoElectronInts(basis_of(load_golden("h2o_sto3g_c0")))
+
+
+def test_bad_basis_rejected_before_device_use():
+    L = _private_handle()
     L.unomol_gpu_create.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     h = C.c_void_p()
     assert L.unomol_gpu_create(None, 0, C.byref(h)) == -1
@@ -61,8 +78,7 @@ def test_every_entry_point_rejects_null_arguments():
     """Every entry point called with null handles and pointers (zero sizes) returns UNOMOL_EINVAL
     (-1), destroys are no-ops and the error-string getters return a string: nothing dereferences a
     null argument or reaches the device first."""
-    from unomol_gb300 import native
-    L = native.lib()
+    L = _private_handle()
     decls = _header_declarations()
     assert len(decls) >= 50
     for ret, name, n in decls:
