@@ -69,7 +69,7 @@ def test_bad_basis_rejected_before_device_use():
 def _header_declarations():
     txt = open(os.path.join(ROOT, "include", "unomol_gb300.h")).read()
     out = []
-    for ret, name, params in re.findall(r"^(int|void|const char\*)\s+(unomol_\w+)\(([^;]*?)\);", txt, re.M | re.S):
+    for ret, name, params in re.findall(r"^(int|long long|void|const char\*)\s+(unomol_\w+)\(([^;]*?)\);", txt, re.M | re.S):
         out.append((ret, name, len([p for p in params.split(",") if p.strip() and p.strip() != "void"])))
     return out
 
@@ -80,13 +80,13 @@ def test_every_entry_point_rejects_null_arguments():
     null argument or reaches the device first."""
     L = _private_handle()
     decls = _header_declarations()
-    assert len(decls) >= 50
+    assert sorted(n for _, n, _ in decls) == _header_symbols()  # every declared entry point is called
     for ret, name, n in decls:
         f = getattr(L, name)
         f.argtypes = [C.c_void_p] * n
-        if ret == "int":
-            f.restype = C.c_int
-            if name in ("unomol_gpu_batch_size", "unomol_guess_num_molecules"):
+        if ret in ("int", "long long"):
+            f.restype = C.c_int if ret == "int" else C.c_longlong
+            if name in ("unomol_gpu_batch_size", "unomol_guess_num_molecules", "unomol_mlp_num_params"):
                 assert f(*([None] * n)) < 0, name
             else:
                 assert f(*([None] * n)) == -1, name
