@@ -18,9 +18,10 @@ k = 0, 8, ..., else the density change), cycled for K steps.
            G out, copies inside the timing);
   plain_fp64   the plain FP64 path on the same densities (full builds), device-timed the same way;
   roofline the ERI + J/K kernels of one build against the FP64 and FP32 FMA peaks measured by the
-           library's own microbenchmark (the kernels are bound by those pipes, not by HBM or tensor
-           cores): peak = flops / max(flops64/peak64, flops32/peak32), the two pipes busy at once
-           (peak_one_after_other = flops / (flops64/peak64 + flops32/peak32) beside it);
+           library's own microbenchmark (scalar work: no tensor-core ceiling applies, and the data
+           stays in L2): peak = flops / max(flops64/peak64, flops32/peak32), the two pipes busy at
+           once (peak_one_after_other = flops / (flops64/peak64 + flops32/peak32) beside it); flops
+           of each part booked to the pipe that does them, at the quartets of the build's own lists;
   cpu_baseline the C restatement of the reference algorithm (oracle/) on the host cores, on a strided
            sample of the shell quartets of one full build.
 --impl reference: that CPU implementation as the reference arm (same metric and workload).
@@ -274,7 +275,7 @@ def counted_flops(ctx, inputs, dev, stream):
     import torch
     ctx.set_counting(True)
     dG = None
-    f64, f32, launches, q32, q, fq = [], [], [], [], [], []
+    f64, f32, launches, q32, q, fq, pq = [], [], [], [], [], [], []
     for full, x in inputs:
         dx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
         if full or dG is None:
@@ -287,9 +288,10 @@ def counted_flops(ctx, inputs, dev, stream):
         launches.append(st["kernel_launches"])
         q.append(st["shell_quartets"])
         q32.append(st["shell_quartets_fp32"])
-        fq.append(st["function_quartets"])
+        fq.append(st["function_quartets_computed"])
+        pq.append(st["primitive_quartets_computed"])
     ctx.set_counting(False)
-    return f64, f32, launches, q, q32, fq
+    return f64, f32, launches, q, q32, fq, pq
 
 
 def run_ours(args):
@@ -345,7 +347,7 @@ def run_ours(args):
     clocks = Clocks(local)
     # warm-up, then the counted (untimed) pass for the algorithmic flops
     timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
-    f64, f32, launches, nq, nq32, nfq = counted_flops(mixed, inputs, dev, stream)
+    f64, f32, launches, nq, nq32, nfq, npq = counted_flops(mixed, inputs, dev, stream)
     # timed region
     replicas.barrier(ws)
     torch.cuda.synchronize(dev)
@@ -416,7 +418,9 @@ def run_ours(args):
     # J/K scatter: 144 algorithmic bytes per computed function quartet (6 density reads and 6 Fock
     # read-modify-writes of 8 bytes), fused into the ERI kernels, against HBM and the L2 figures
     l2_read, l2_atom = native.l2_peak()
-    scatter_bytes = 144.0 * sum(nfq[k % len(inputs)] for k in range(args.steps))
+    fq_steps = sum(nfq[k % len(inputs)] for k in range(args.steps))
+    pq_steps = sum(npq[k % len(inputs)] for k in range(args.steps))
+    scatter_bytes = 144.0 * fq_steps
     scatter_gbs = scatter_bytes / eri_s / 1e9
     hbm = measured_hbm()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -437,7 +441,10 @@ def run_ours(args):
                          "peak_fp64": peak64, "peak_fp32": peak32,
                          "peak_note": "peak = (flops64 + flops32) / max(flops64 / peak64, flops32 / peak32): both pipes busy at once",
                          "peak_one_after_other": peak_serial,
-                         "peak_source": "FMA microbenchmark of this library (unomol_gpu_fma_peak), this run"},
+                         "peak_source": "FMA microbenchmark of this library (unomol_gpu_fma_peak), this run",
+                         "flops_note": "per primitive quartet from device counters per class and precision; "
+                                       "per shell quartet (density contraction) at the FP64 and FP32 parts of "
+                                       "each build's own work lists"},
             "batched_form": batched,
             "plain_fp64": {"value": plain_rate, "unit": UNIT, "ms_per_build": statistics.mean(p_ms),
                            "kernel_ms": statistics.mean(p_eri), "speedup_of_value": value / plain_rate},
@@ -455,6 +462,11 @@ def run_ours(args):
                         "l2_read_gbs": l2_read, "frac_of_l2_read": scatter_gbs / l2_read,
                         "l2_fp64_atomics_per_s": l2_atom * 1e9,
                         "note": "fused into the ERI kernels (the J/K epilogue); time = ERI kernel time"},
+            "eri_rate": {"function_quartets_per_s": fq_steps / eri_s, "primitive_quartets_per_s": pq_steps / eri_s,
+                         "function_quartets_per_build": fq_steps / args.steps,
+                         "primitive_quartets_per_build": pq_steps / args.steps,
+                         "note": "unique canonical quartets of each build's work lists (FP64 and FP32 parts), primitive "
+                                 "quartets past the 1e-12 prefactor cut, over the ERI kernel time"},
             "clocks": clk, "gpu_launches": launches_total}
     if rank == 0 and ws == 1:
         ensure_oracle()

@@ -74,8 +74,12 @@ typedef struct UnomolStats {
     int pad_;
     /* filled only while counting is on (unomol_gpu_set_counting): */
     int64_t primitive_quartets_computed; /* primitive quartets past the 1e-12 prefactor cut */
-    double eri_flops;              /* algorithmic flops of the ERI + J/K kernels (FMA = 2), see DESIGN */
+    double eri_flops;              /* algorithmic flops of the ERI + J/K kernels (FMA = 2): per primitive
+                                      quartet its setup, roots, recurrences and transfers, per shell
+                                      quartet its density contraction, counted from the kernels' steps */
     double eri_flops_fp32;         /* of which in the FP32 kernels (mixed mode) */
+    int64_t function_quartets_computed; /* function quartets of the last build's work lists (in the
+                                           density-screened and mixed builds: its FP64 and FP32 parts) */
 } UnomolStats;
 
 /* TwoElectronInts(basis, start_shell, label) -- TwoElectronInts.hpp:83-88.

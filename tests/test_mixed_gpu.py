@@ -48,6 +48,36 @@ def test_all_fp32_within_fp32_accuracy(gpu, name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", ["water3_631g", "ref_dh95_h2"])
+def test_counted_work_belongs_to_the_part_that_does_it(gpu, name):
+    """The counting mode's algorithmic flops and function quartets: the quartet-level work
+    (normalisation and density contraction) is booked to the precision of the kernel that does it and
+    to the quartets of the build's own work lists, so a build with every quartet in FP32 books no FP64
+    work, and a density-screened FP64 build that keeps every quartet books what the plain build does."""
+    from unomol_gb300 import native
+    g = load_golden(name)
+    t = native.TwoElectronInts(basis_of(g))
+    t.set_counting(True)
+    t.form_g(g["P_rand"])
+    plain = t.stats()
+    assert plain["eri_flops"] > 0 and plain["eri_flops_fp32"] == 0
+    assert plain["function_quartets_computed"] == plain["function_quartets"]
+    t.set_precision(native.PREC_MIXED, 0.0)
+    t.set_density_screening(1e-20)
+    t.form_g(g["P_rand"])
+    st = t.stats()
+    assert st["eri_flops_fp32"] == 0
+    assert st["function_quartets_computed"] == plain["function_quartets"]
+    assert abs(st["eri_flops"] - plain["eri_flops"]) <= 1e-12 * plain["eri_flops"]
+    t.set_precision(native.PREC_MIXED, 1e30)
+    t.form_g(g["P_rand"])
+    st = t.stats()
+    assert st["eri_flops_fp32"] > 0 and st["eri_flops"] - st["eri_flops_fp32"] == 0
+    assert st["function_quartets_computed"] == plain["function_quartets"]
+    assert st["shell_quartets_fp32"] == st["shell_quartets"] == plain["shell_quartets"]
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", ["h2o_631g", "water3_631g", "ethane_631g", "propane_cation_sto3g"])
 def test_incremental_mixed_scf_energy(gpu, name):
     from unomol_gb300 import native

@@ -735,11 +735,25 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         std::vector<unsigned long long> c(2 * ncls * 32);
         CU(cudaMemcpyAsync(c.data(), ctx->d_counters, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
-        int64_t prims = 0;
+        // shell quartets of this build per block pair: in the density-screened and mixed builds the
+        // FP64 and FP32 parts of this build's lists (quartets below the skip cutoff do no work),
+        // otherwise the static staircase of every class (ClassLaunch::quartets)
+        const bool parts = mixed && !ctx->bps.empty();
+        const bool has32 = ctx->fp32_cut > ctx->skip_cut;
+        std::vector<long long> q64, q32;
+        if (parts) {
+            q64.assign(ctx->bps.size(), 0);
+            q32.assign(ctx->bps.size(), 0);
+            CU(cudaMemcpy(q64.data(), ctx->d_cnt64, sizeof(long long) * q64.size(), cudaMemcpyDeviceToHost));
+            if (has32)
+                CU(cudaMemcpy(q32.data(), ctx->d_cnt32, sizeof(long long) * q32.size(), cudaMemcpyDeviceToHost));
+        }
+        int64_t prims = 0, s64 = 0, s32 = 0, fq_done = 0;
         double fl = 0.0, fl32 = 0.0;
         for (const ClassLaunch& L : ctx->launches) {
             const int cls = L.bc * NPAIRCLASS + L.kc;
             const int la = pc_la(L.bc), lb = pc_lb(L.bc), lc = pc_la(L.kc), ld = pc_lb(L.kc);
+            const int64_t nf = (int64_t)ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
             for (int half = 0; half < 2; ++half) {
                 unsigned long long n = 0;
                 for (int k = 0; k < 32; ++k) n += c[(half * ncls + cls) * 32 + k];
@@ -747,21 +761,27 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                 const double f = (double)n * flops_per_prim(la, lb, lc, ld, half != 0);
                 if (half) fl32 += f; else fl += f;
             }
-            // quartet-level work: all quartets of the class (both halves together in mixed mode)
-            fl += (double)L.quartets * flops_per_quartet(la, lb, lc, ld);
+            // quartet-level work (normalisation and density contraction) in the precision of the
+            // kernel that does it
+            long long n64 = L.quartets, n32 = 0;
+            if (parts) {
+                n64 = 0;
+                for (int k = L.bp_begin; k < L.bp_begin + L.nbp; ++k) {
+                    n64 += q64[k];
+                    n32 += q32[k];
+                }
+            }
+            fl += (double)n64 * flops_per_quartet(la, lb, lc, ld);
+            fl32 += (double)n32 * flops_per_quartet(la, lb, lc, ld);
+            s64 += n64;
+            s32 += n32;
+            fq_done += (n64 + n32) * nf;
         }
         ctx->stats.primitive_quartets_computed = prims;
+        ctx->stats.function_quartets_computed = fq_done;
         ctx->stats.eri_flops = fl + fl32;
         ctx->stats.eri_flops_fp32 = fl32;
-        if (mixed && !ctx->bps.empty()) {
-            std::vector<long long> a(ctx->bps.size()), b(ctx->bps.size());
-            CU(cudaMemcpy(a.data(), ctx->d_cnt64, sizeof(long long) * a.size(), cudaMemcpyDeviceToHost));
-            CU(cudaMemcpy(b.data(), ctx->d_cnt32, sizeof(long long) * b.size(), cudaMemcpyDeviceToHost));
-            long long s64 = 0, s32 = 0;
-            for (size_t k = 0; k < a.size(); ++k) {
-                s64 += a[k];
-                s32 += ctx->fp32_cut > ctx->skip_cut ? b[k] : 0;
-            }
+        if (parts) {
             ctx->stats.shell_quartets = s64 + s32;
             ctx->stats.shell_quartets_fp32 = s32;
         }
