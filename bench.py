@@ -221,6 +221,16 @@ def profile_traffic(form):
     return None
 
 
+def two_pipe_ceiling(fl64, fl32, peak64, peak32):
+    """Ceiling rates (same unit as the peaks) of fl64 FP64 and fl32 FP32 flops: the two parts run
+    concurrently on their own pipes, so the work needs at least the longer of the two pipe times; the
+    second figure is the ceiling of running them one after the other (the sum of the times)."""
+    if fl64 + fl32 <= 0:
+        return peak64, peak64
+    return ((fl64 + fl32) / max(fl64 / peak64, fl32 / peak32),
+            (fl64 + fl32) / (fl64 / peak64 + fl32 / peak32))
+
+
 def step_inputs(dens):
     """Per build of the sequence: (is_full, density or density change), rebuilding every REBUILD builds."""
     out = []
@@ -410,10 +420,7 @@ def run_ours(args):
     fl32 = sum(f32[k % len(inputs)] for k in range(args.steps))
     eri_s = sum(eri_ms) / 1e3
     achieved = (fl64 + fl32) / eri_s / 1e12
-    # ceiling: the FP64 and FP32 parts run concurrently on their own pipes, so a build needs at least
-    # the longer of the two pipe times (the sum is the ceiling of running them one after the other)
-    peak = (fl64 + fl32) / max(fl64 / peak64, fl32 / peak32) if (fl64 + fl32) > 0 else peak64
-    peak_serial = (fl64 + fl32) / (fl64 / peak64 + fl32 / peak32) if (fl64 + fl32) > 0 else peak64
+    peak, peak_serial = two_pipe_ceiling(fl64, fl32, peak64, peak32)
     launches_total = sum(launches[k % len(inputs)] for k in range(args.steps))
     # J/K scatter: 144 algorithmic bytes per computed function quartet (6 density reads and 6 Fock
     # read-modify-writes of 8 bytes), fused into the ERI kernels, against HBM and the L2 figures

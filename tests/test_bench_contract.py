@@ -67,3 +67,17 @@ def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
     c = bench.Clocks(0, exe=str(tmp_path / "absent"))
     c.start()
     assert c.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+
+def test_two_pipe_ceiling():
+    """FP64-only work has the FP64 peak as ceiling; FP32-only the FP32 peak; mixed work is bounded by
+    the longer pipe time (concurrent) and by the sum (one after the other)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.two_pipe_ceiling(5.0, 0.0, 1.25, 78.5) == (1.25, 1.25)
+    assert bench.two_pipe_ceiling(0.0, 7.0, 1.25, 78.5) == (78.5, 78.5)
+    peak, serial = bench.two_pipe_ceiling(1.88, 30.48, 1.25, 78.5)
+    t64, t32 = 1.88 / 1.25, 30.48 / 78.5
+    assert abs(peak - (1.88 + 30.48) / t64) < 1e-12
+    assert abs(serial - (1.88 + 30.48) / (t64 + t32)) < 1e-12
+    assert serial < peak
