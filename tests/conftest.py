@@ -44,3 +44,48 @@ def gpu():
     from unomol_gb300 import native
     native.lib()  # fails loudly when the extension is missing
     return torch.device("cuda:0")
+
+
+def closed_form_s_basis():
+    """Four hydrogens in 6-31G (8 contracted s functions) at fixed positions, with the closed-form
+    G(P) of a random symmetric density: (ij|kl) over s Gaussians is
+    sum c c c c 2 pi^(5/2) / (p q sqrt(p+q)) exp(-ab/p |AB|^2) exp(-cd/q |CD|^2) F0(pq/(p+q) |PQ|^2)
+    with F0(T) = sqrt(pi/T) erf(sqrt(T)) / 2, and G = 2 J(P) - K(P) with P the half density, as the
+    reference's RHF scatter forms it.  Returns (basis, packed P, packed G)."""
+    import math
+
+    from scipy.special import erf
+
+    from unomol_gb300 import molecules
+    from unomol_gb300.basis import Basis, full_to_packed
+
+    atoms = [("H", (0, 0, 0)), ("H", (0, 0, 0.74)), ("H", (1.1, 0.3, 0.2)), ("H", (1.0, 0.9, 1.3))]
+    b = Basis(text=molecules.patin_text(atoms, "6-31G"))
+    n = b.norb
+    funcs = []
+    for i in range(b.nshell):
+        assert b.shell_l[i] == 0
+        a, c = b.shell_prims(i)
+        funcs.append((a, c, b.centers[b.shell_center[i]]))
+
+    def pair(i, j):
+        (ai, ci, A), (aj, cj, B) = funcs[i], funcs[j]
+        return [(x + y, (x * A + y * B) / (x + y), cx * cy * math.exp(-x * y / (x + y) * ((A - B) ** 2).sum()))
+                for x, cx in zip(ai, ci) for y, cy in zip(aj, cj)]
+
+    def f0(t):
+        return 1.0 if t < 1e-15 else 0.5 * math.sqrt(math.pi / t) * float(erf(math.sqrt(t)))
+
+    prs = {(i, j): pair(i, j) for i in range(n) for j in range(i + 1)}
+    E = np.zeros((n, n, n, n))
+    for (i, j), bra in prs.items():
+        for (k, l), ket in prs.items():
+            v = sum(kp * kq * 2 * math.pi ** 2.5 / (p * q * math.sqrt(p + q)) * f0(p * q / (p + q) * ((P - Q) ** 2).sum())
+                    for p, P, kp in bra for q, Q, kq in ket)
+            for a1, b1 in ((i, j), (j, i)):
+                for c1, d1 in ((k, l), (l, k)):
+                    E[a1, b1, c1, d1] = v
+    m = np.random.default_rng(3).uniform(-0.5, 0.5, (n, n))
+    P = 0.5 * (m + m.T)
+    G = 2 * np.einsum("ijkl,kl->ij", E, P) - np.einsum("ikjl,kl->ij", E, P)
+    return b, full_to_packed(P), full_to_packed(G)

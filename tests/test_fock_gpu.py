@@ -75,3 +75,16 @@ def test_md_mode_matches_md_reference(gpu, name):
     assert err <= TOL_G, f"{name}: max|dG| = {err:.3e}"
     Ga, Gb = t.form_g_uhf(g["Pa"], g["Pb"])
     assert max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max()) <= TOL_G
+
+
+@pytest.mark.gpu
+def test_s_integrals_match_closed_form(gpu):
+    """G(P) of a basis of s functions only against the closed form of (ss|ss) (F0 through erf),
+    independent of the reference: within the G tolerance."""
+    from conftest import closed_form_s_basis
+    from unomol_gb300 import native
+    b, P, G = closed_form_s_basis()
+    t = native.TwoElectronInts(b)
+    assert np.abs(t.form_g(P) - G).max() <= 1e-10
+    t.set_rys_mode(native.RYS_EXACT)
+    assert np.abs(t.form_g(P) - G).max() <= 1e-10

@@ -53,3 +53,14 @@ def test_fixture_energy_matches_published(name):
     """The stock reference run here reproduces the published golden energy (test/scfout.dat.*)."""
     g = load_golden(name)
     assert abs(float(g["scf_energy"]) - float(g["golden_energy"])) < 1e-10
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_oracle_matches_closed_form_s_integrals(exact):
+    """An independent pin of the restatement: G(P) of a basis of s functions only, against the closed
+    form of (ss|ss) (one Rys root, the Boys function F0 through erf)."""
+    import orc
+    from conftest import closed_form_s_basis
+    b, P, G = closed_form_s_basis()
+    Go, _ = orc.fock(b, P, exact=exact)
+    assert np.abs(Go - G).max() <= 1e-13 * np.abs(G).max()
