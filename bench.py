@@ -48,7 +48,8 @@ sys.path.insert(0, ROOT)
 METRIC = "Fock builds/sec (32-water 6-31G RHF SCF Fock builds)"
 UNIT = "Fock builds/s"
 WORKLOAD = "32-water cluster, 6-31G, RHF, 416 basis functions (seed 0): Fock builds of the converging SCF"
-CPU_STRIDE = 64
+CPU_STRIDE = 64  # per step of --impl reference (~0.6 s on 16 Grace cores)
+CPU_BASELINE_STRIDE = 4  # the cpu_baseline of the measured line: ~10 s on 16 Grace cores
 FP32_CUTOFF = 1e-3  # swept 1e-7..1e0 in profiles/fp32_cutoff_sweep_water32.md; |dE| stays ~1e-9 Eh here
 # quartets with Schwarz bound x max|dP| below this are skipped in a build: at 1e-12 the skipped parts of
 # ~1e8 quartets left 1e-9..1e-8 Eh of energy noise per incremental build, which stalled the 1e-10 Eh
@@ -478,9 +479,9 @@ def run_ours(args):
     if rank == 0 and ws == 1:
         ensure_oracle()
         threads = os.cpu_count() or 1
-        rate, dt = cpu_port_rate(b, synthetic_density(b), CPU_STRIDE, threads)
+        rate, dt = cpu_port_rate(b, synthetic_density(b), CPU_BASELINE_STRIDE, threads)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"C restatement of the reference algorithm, full FP64 build, every {CPU_STRIDE}th "
+                                "sample": f"C restatement of the reference algorithm, full FP64 build, every {CPU_BASELINE_STRIDE}th "
                                           f"canonical shell quartet ({dt:.1f} s), extrapolated to one build"}
     if rank == 0:
         print(json.dumps(line), flush=True)
