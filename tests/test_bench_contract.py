@@ -81,3 +81,19 @@ def test_two_pipe_ceiling():
     assert abs(peak - (1.88 + 30.48) / t64) < 1e-12
     assert abs(serial - (1.88 + 30.48) / (t64 + t32)) < 1e-12
     assert serial < peak
+
+
+def test_step_inputs_rebuild_every_eighth_build():
+    """The measured sequence: the full density at builds 0, 8, 16, ... and the density change since
+    the previous build otherwise, so that the incremental G sums back to G of the full density."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    dens = [np.full(3, float(k * k)) for k in range(18)]
+    steps = bench.step_inputs(dens)
+    assert len(steps) == len(dens)
+    for k, (full, x) in enumerate(steps):
+        assert full == (k % bench.REBUILD == 0)
+        base = k - k % bench.REBUILD
+        acc = sum(steps[j][1] for j in range(base, k + 1))
+        assert np.array_equal(acc, dens[k])
