@@ -150,6 +150,12 @@ int unomol_gpu_get_stats(const UnomolCtx* ctx, UnomolStats* out);
  * then synchronises its stream before returning. */
 int unomol_gpu_set_counting(UnomolCtx* ctx, int on);
 
+/* Order of the class launches of a Fock build (no reference counterpart; a diagnostic control):
+ * 0 (default) in class order, non-zero in reverse.  The J/K contributions meet in FP64 atomics, so the
+ * order of the additions, and with it the rounding of G, changes from launch order to launch order and
+ * from run to run; the determinism tests bound that difference. */
+int unomol_gpu_set_launch_order(UnomolCtx* ctx, int reversed);
+
 /* Device time of the last Fock build, from CUDA events recorded on the build's stream (no reference
  * counterpart): ms_eri covers the ERI + J/K kernels, ms_total the whole build.  Waits for the build. */
 int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total);
@@ -170,9 +176,13 @@ int unomol_gpu_l2_peak(double* read_gbs, double* atomic_gops);
  * call then allocates nothing: its per-build scratch (dense P and the N x N accumulator) lives in a
  * 16 MiB static device array of the library, which every GPU that loads the library's kernels holds
  * until exit.  Limits: at most 1024 basis functions (larger bases return UNOMOL_EINVAL with a
- * message) and the FP64 precision mode only.  The first call on a device looks up the array's device
- * address; make that first call before any stream capture.  Every call shares the one array, so calls
- * that overlap on the GPU (other streams, other host threads) race; serialise them. */
+ * message) and the FP64 precision mode only.  Every integral method of the regular build runs: the
+ * Rys kernels for s/p/d/f/g classes up to la+lb+lc+ld = 8, MD above that and in UNOMOL_ERI_MD mode.
+ * Counting mode (unomol_gpu_set_counting) is rejected with UNOMOL_EINVAL (its counters would need an
+ * allocation); the build's launch count and event timings (unomol_gpu_get_stats,
+ * unomol_gpu_last_build_ms) describe the last call.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  Every call shares the one array,
+ * so calls that overlap on the GPU (other streams, other host threads) race; serialise them. */
 int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, double* dG, void* stream);
 
 void unomol_gpu_destroy(UnomolCtx* ctx);
@@ -347,6 +357,12 @@ const char* unomol_mlp_last_error(const UnomolMlp* m);
 /* C[M x N] (fp32, device) = A[M x K] . B[N x K]^T, A and B bf16 row major on the device (the tensor-core
  * GEMM of the network); status: device int set to 1 if a bounded wait gave up. */
 int unomol_tc_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int* status, void* stream);
+/* Poll limit of the tensor-core GEMMs' pipeline waits, for every GEMM the process launches afterwards
+ * (no reference counterpart; a failure-detection control).  0 (default): 2^22 polls.  Negative: the
+ * producer's and the MMA issuer's waits give up at their first wait, so the call reports a timeout
+ * (status word 1, UNOMOL_ETIMEOUT from the network calls) after draining the copies it issued and
+ * releasing its tensor memory; the next call with the default works normally. */
+int unomol_tc_set_wait_polls(int polls);
 
 typedef struct UnomolGuess UnomolGuess;
 typedef struct UnomolGuessConfig {

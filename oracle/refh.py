@@ -14,6 +14,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
+# Where the reference sources lie (the fixture generators read its inputs and pbas.lib there):
+# $UNOMOL_REFERENCE, else the container's read-only copy that oracle/Makefile also defaults to.
+REFERENCE = os.environ.get("UNOMOL_REFERENCE", "/root/reference")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -61,6 +64,11 @@ def lib(md=False) -> C.CDLL:
     L.refh_scf.argtypes = [C.c_char_p, C.c_char_p, _dp, C.c_void_p]
     L.refh_dpm_h.restype = C.c_int
     L.refh_dpm_h.argtypes = [C.c_char_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, _ip]
+    L.refh_scf_trace.restype = C.c_int
+    L.refh_scf_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_int, _dp]
+    L.refh_scf_diis.restype = C.c_int
+    L.refh_scf_diis.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                C.c_double, _dp, _dp]
     _LIBS[name] = L
     return L
 
@@ -164,3 +172,35 @@ def run_scf(patin_path: str, md: bool = False):
         raise RuntimeError(f"refh_scf failed: {rc}")
     return {"energy": out[0], "init_energy": out[1], "iterations": int(out[2]), "ediff": out[3],
             "pdiff": out[4], "nucrep": out[5], "t_ints": out[6], "t_scf": out[7], "P": P}
+
+
+def scf_trace(basis: RefBasis, tints: RefTwoElectronInts, kmax: int) -> np.ndarray:
+    """The first kmax total energies of the stock damped SCF loop (RHF.hpp:140-166 / UHF.hpp:150-163,
+    core-Hamiltonian guess) of `basis`, with the integrals of `tints` (same shells)."""
+    e = np.zeros(kmax)
+    with tempfile.TemporaryDirectory(prefix="unomol_trace_") as wd:
+        k = basis.L.refh_scf_trace(basis.h, tints.h, wd.encode(), kmax, e)
+    if k < 0:
+        raise RuntimeError(f"refh_scf_trace failed: {k}")
+    return e[:k].copy()
+
+
+def scf_diis(basis: RefBasis, tints: RefTwoElectronInts, P0=None, maxits: int = 200, nkeep: int = 8,
+             eps_e: float = 1e-12, eps_err: float = 1e-9):
+    """Pulay DIIS SCF on the reference's own formGmatrix, one-electron integrals and eigen-solver
+    (oracle/ref_harness.cpp: diis_loop).  P0: starting density (RHF packed, UHF Pa then Pb) or None for
+    the core-Hamiltonian guess.  Returns energy, iterations, converged, max error, last |dE|, P."""
+    nP = basis.no2 * (2 if basis.nelec % 2 else 1)
+    out = np.zeros(8)
+    P = np.zeros(nP)
+    p0 = None
+    if P0 is not None:
+        p0 = np.ascontiguousarray(P0, np.float64)
+        assert p0.size == nP
+    with tempfile.TemporaryDirectory(prefix="unomol_diis_") as wd:
+        rc = basis.L.refh_scf_diis(basis.h, tints.h, wd.encode(), None if p0 is None else p0.ctypes.data,
+                                   maxits, nkeep, eps_e, eps_err, out, P)
+    if rc != 0:
+        raise RuntimeError(f"refh_scf_diis failed: {rc}")
+    return {"energy": out[0], "iterations": int(out[1]), "converged": bool(out[2]), "error": out[3],
+            "de": out[4], "nucrep": out[5], "seconds": out[6], "x_orthonormality": out[7], "P": P}

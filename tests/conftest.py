@@ -14,6 +14,11 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+# Scale fixtures (n-decane and the 32-water cluster, tests/golden/make_golden.py --big): no stored
+# densities or one-electron matrices, their own tests (tests/test_scale_parity_gpu.py)
+BIG_CASES = ("decane_631g", "water32_631g")
+
+
 def golden_cases(pattern="*.npz", exclude_md=True):
     out = []
     for p in sorted(glob.glob(os.path.join(GOLDEN, pattern))):
@@ -22,8 +27,19 @@ def golden_cases(pattern="*.npz", exclude_md=True):
             continue
         if name.startswith(("dpm_", "prop_")):  # DPM grids, moments / finite field: their own tests
             continue
+        if name in BIG_CASES:
+            continue
         out.append(name)
     return out
+
+
+def rand_density(n: int, seed: int, scale: float = 0.3) -> np.ndarray:
+    """The seeded random symmetric density of the fixture generator (tests/golden/make_golden.py):
+    packed, off-diagonal uniform in (-scale, scale), diagonal uniform in (0, 1)."""
+    rng = np.random.default_rng(seed)
+    m = rng.uniform(-scale, scale, (n, n))
+    m = 0.5 * (m + m.T) + np.diag(rng.uniform(0.0, 1.0, n))
+    return np.ascontiguousarray(m[np.tril_indices(n)])
 
 
 def load_golden(name):

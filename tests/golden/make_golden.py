@@ -13,8 +13,11 @@ Per case (<name>.npz):
   golden_energy    (reference test inputs) the published energy of test/scfout.dat.*
   ints_*           (small cases) the reference's stored integral records (val, i, j, k, l)
 
---big adds the n-decane 6-31G RHF/UHF-cation G(P) fixtures (about 15 s of reference integral pass)
-and the 32-water 6-31G G(P) fixture (about 10 minutes).
+--big writes the scale fixtures (make_big_case): n-decane 6-31G (RHF and the UHF doublet cation) and
+the 32-water 6-31G cluster (seed 0).  The reference's own damped SCF does not converge on either, so
+their energies come from the test-only DIIS loop over the reference's formGmatrix (oracle/ref_harness.cpp
+diis_loop); the first iterations of the stock damped loop are recorded as well.  About 2 minutes for
+decane and 15 minutes for the cluster (its reference integral pass alone takes 10).
 """
 from __future__ import annotations
 
@@ -33,7 +36,7 @@ import refh  # noqa: E402
 
 from unomol_gb300 import molecules  # noqa: E402
 
-REF = "/root/reference"
+REF = refh.REFERENCE
 
 
 def rand_density(n: int, seed: int, scale: float = 0.3) -> np.ndarray:
@@ -83,6 +86,100 @@ def make_case(name: str, patin: str, scf: bool, golden_energy: float | None, dum
     os.remove(path)
     np.savez_compressed(os.path.join(HERE, f"{name}{'_md' if md else ''}.npz"), **out)
     print(name, "nbf", n, "stored", len(vals), "E" if scf else "", out.get("scf_energy", ""), file=sys.stderr)
+
+
+def make_big_case(name: str, patin: str, cation_patin: str | None, fragments: list | None, seed: int,
+                   keep_conv: bool):
+    """A scale fixture (<name>.npz), arrays kept to what the GPU tests read:
+      patin, seed           the input and the seed of rand_density(n, seed) (P is rebuilt by the tests)
+      G_rand                the reference's G(P_rand) (TwoElectronInts.cpp:822-844)
+      n_stored              integral records the reference stored
+      diis_energy, diis_iterations, diis_error
+                            the DIIS SCF of the reference's pieces (RHF), from the core-H guess or, with
+                            `fragments`, from the superposition of the fragments' own DIIS densities
+      trace                 the first 5 total energies of the stock damped loop (core-H guess)
+      P_conv, G_conv        (keep_conv) the DIIS density and the reference's G of it
+      patin_cation, Pa/Pb seeds, Ga, Gb, uhf_diis_*, trace_uhf
+                            (cation_patin) the same basis with one electron less: UHF G of seeded
+                            densities (TwoElectronInts.cpp:846-869), its DIIS energy and stock trace
+    """
+    import time
+    t0 = time.time()
+    path = os.path.join(HERE, f"_{name}.patin")
+    with open(path, "w") as f:
+        f.write(patin)
+    b = refh.RefBasis(path)
+    t = refh.RefTwoElectronInts(b)
+    n = b.norb
+    out = {"patin": np.array(patin), "seed": np.array(seed)}
+    P = rand_density(n, seed)
+    out["G_rand"] = t.form_g(P)
+    vals, _ = t.records()
+    out["n_stored"] = np.array(len(vals))
+    del vals
+    print(name, "integrals + G", f"{time.time() - t0:.1f} s", file=sys.stderr)
+    P0 = None
+    if fragments:
+        P0 = np.zeros((n, n))
+        for k, (ftext, aos) in enumerate(fragments):
+            fp = os.path.join(HERE, f"_{name}_frag.patin")
+            with open(fp, "w") as f:
+                f.write(ftext)
+            fb = refh.RefBasis(fp)
+            ft = refh.RefTwoElectronInts(fb)
+            r = refh.scf_diis(fb, ft, eps_e=1e-8, eps_err=1e-5, maxits=60)
+            Pf = np.zeros((fb.norb, fb.norb))
+            Pf[np.tril_indices(fb.norb)] = r["P"]
+            Pf = Pf + Pf.T - np.diag(np.diag(Pf))
+            P0[np.ix_(aos, aos)] = Pf
+            del ft, fb
+            os.remove(fp)
+        P0 = np.ascontiguousarray(P0[np.tril_indices(n)])
+    r = refh.scf_diis(b, t, P0=P0, maxits=200, eps_e=1e-12, eps_err=1e-9)
+    assert r["converged"], (name, r)
+    out.update(diis_energy=np.array(r["energy"]), diis_iterations=np.array(r["iterations"]),
+               diis_error=np.array(r["error"]))
+    print(name, "DIIS", r["energy"], r["iterations"], f"{time.time() - t0:.1f} s", file=sys.stderr)
+    if keep_conv:
+        out["P_conv"] = r["P"]
+        out["G_conv"] = t.form_g(r["P"])
+    out["trace"] = refh.scf_trace(b, t, 5)
+    print(name, "trace", out["trace"], file=sys.stderr)
+    if cation_patin is not None:
+        cpath = os.path.join(HERE, f"_{name}_cation.patin")
+        with open(cpath, "w") as f:
+            f.write(cation_patin)
+        cb = refh.RefBasis(cpath)
+        assert cb.nelec % 2 == 1 and cb.norb == n
+        out["patin_cation"] = np.array(cation_patin)
+        Pa, Pb = rand_density(n, seed + 1), rand_density(n, seed + 2)
+        out["Ga"], out["Gb"] = t.form_g_uhf(Pa, Pb)
+        ru = refh.scf_diis(cb, t, maxits=300, eps_e=1e-12, eps_err=1e-9)
+        assert ru["converged"], (name, ru)
+        out.update(uhf_diis_energy=np.array(ru["energy"]), uhf_diis_iterations=np.array(ru["iterations"]),
+                   uhf_diis_error=np.array(ru["error"]))
+        out["trace_uhf"] = refh.scf_trace(cb, t, 5)
+        print(name, "UHF DIIS", ru["energy"], ru["iterations"], out["trace_uhf"], file=sys.stderr)
+        del cb
+        os.remove(cpath)
+    del t
+    os.remove(path)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(name, "nbf", n, "stored", out["n_stored"], f"{time.time() - t0:.1f} s", file=sys.stderr)
+
+
+def water_fragments(nw: int, seed: int, basis: str):
+    """Per monomer of molecules.water_cluster(nw, seed): its patin text and its AO indices in the
+    cluster's basis (shells atom after atom, 13 functions per water in 6-31G)."""
+    atoms = molecules.water_cluster(nw, seed)
+    out, off = [], 0
+    for m in range(nw):
+        mono = atoms[3 * m:3 * m + 3]
+        txt = molecules.patin_text(mono, basis, eps=1e-8)
+        nbf = int(txt.split()[1])
+        out.append((txt, list(range(off, off + nbf))))
+        off += nbf
+    return out
 
 
 def pbas_patin(atoms_bohr, key: str, nelec: int, eps: float = 1e-10) -> str:
@@ -149,8 +246,15 @@ def main():
               ("he2_ccpvqz", pbas_patin([(2, (0.0, 0.0, 0.0)), (2, (0.0, 0.0, 3.0))], "HE:CC-PVQZU", 4), False, None, False)]
     cases += fcases
     if a.big:
-        cases.append(("decane_631g", molecules.patin_text(molecules.alkane(10), "6-31G", eps=1e-10), False, None, False))
-        cases.append(("water32_631g", molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10), False, None, False))
+        big = [("decane_631g", molecules.patin_text(molecules.alkane(10), "6-31G", eps=1e-10),
+                molecules.patin_text(molecules.alkane(10), "6-31G", charge=1, eps=1e-10), None, 1010, True),
+               ("water32_631g", molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10), None,
+                water_fragments(32, 0, "6-31G"), 3232, False)]
+        for c in big:
+            if a.only and a.only not in c[0]:
+                continue
+            make_big_case(*c)
+        return
     for c in cases:
         if a.only and a.only not in c[0]:
             continue

@@ -88,6 +88,8 @@ def test_every_entry_point_rejects_null_arguments():
             f.restype = C.c_int if ret == "int" else C.c_longlong
             if name in ("unomol_gpu_batch_size", "unomol_guess_num_molecules", "unomol_mlp_num_params"):
                 assert f(*([None] * n)) < 0, name
+            elif name == "unomol_tc_set_wait_polls":  # its one argument is a number: 0 = the default limit
+                assert f(*([None] * n)) == 0, name
             else:
                 assert f(*([None] * n)) == -1, name
         elif ret == "void":

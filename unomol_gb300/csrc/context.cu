@@ -105,6 +105,7 @@ struct UnomolCtx {
     int rys_mode = UNOMOL_RYS_REFERENCE;
     int eri_method = UNOMOL_ERI_REFERENCE;
     int counting = 0;
+    int reverse_launches = 0;  // class launches in reverse order (unomol_gpu_set_launch_order)
     double fp32_cut = 1e-10;
     UnomolStats stats{};
     std::string err;
@@ -578,6 +579,19 @@ int ensure_density_buffers(UnomolCtx* ctx, bool uhf) {
     return UNOMOL_OK;
 }
 
+// One class launch with the reference's choice of integral method (TwoElectronInts.cpp:658-666): MD
+// for la+lb+lc+ld > 8 and for every class in the MD mode; otherwise Rys, by the templated kernels for
+// the s/p/d classes they cover and by the runtime-L kernel for the rest.
+static cudaError_t launch_class_kernel(const UnomolCtx* ctx, const ClassLaunch& L, bool uhf, bool fp32, const FockArgs& A,
+                                       cudaStream_t s) {
+    const int la = pc_la(L.bc), lb = pc_lb(L.bc), lc = pc_la(L.kc), ld = pc_lb(L.kc);
+    if (ctx->eri_method == UNOMOL_ERI_MD || la + lb + lc + ld > 8) return launch_fock_md(la, lb, lc, ld, uhf, A, ctx->nt, s);
+    if (L.bc < NTMPLCLASS && L.kc < NTMPLCLASS)
+        return fp32 ? launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s)
+                    : launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s);
+    return launch_fock_generic(la, lb, lc, ld, uhf, fp32, A, ctx->nt, ctx->d_rys, ctx->d_rys32, s);
+}
+
 // The Fock build proper: packed device P in, packed device G added into.
 int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa, double* dGb, cudaStream_t s) {
     const bool uhf = dPb != nullptr;
@@ -664,15 +678,10 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         for (int k = 0; k < 2; ++k) CU(cudaStreamWaitEvent(ls[k], ctx->fork, 0));
     }
     auto launch_class = [&](const ClassLaunch& L, bool fp32, bool side = false) -> cudaError_t {
-        const cudaStream_t s = ls[(fp32 || side) ? 1 : 0];
-        const int la = pc_la(L.bc), lb = pc_lb(L.bc), lc = pc_la(L.kc), ld = pc_lb(L.kc);
-        if (ctx->eri_method == UNOMOL_ERI_MD || la + lb + lc + ld > 8) return launch_fock_md(la, lb, lc, ld, uhf, A, ctx->nt, s);
-        if (L.bc < NTMPLCLASS && L.kc < NTMPLCLASS)
-            return fp32 ? launch_fock_fp32(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys32, s)
-                        : launch_fock_fp64(L.bc, L.kc, uhf, A, ctx->nt, ctx->d_rys, s);
-        return launch_fock_generic(la, lb, lc, ld, uhf, fp32, A, ctx->nt, ctx->d_rys, ctx->d_rys32, s);
+        return launch_class_kernel(ctx, L, uhf, fp32, A, ls[(fp32 || side) ? 1 : 0]);
     };
-    for (size_t li = 0; li < ctx->launches.size(); ++li) {
+    for (size_t lk = 0; lk < ctx->launches.size(); ++lk) {
+        const size_t li = ctx->reverse_launches ? ctx->launches.size() - 1 - lk : lk;
         const ClassLaunch& L = ctx->launches[li];
         A.bps = ctx->d_bps + L.bp_begin;
         A.prefix = ctx->d_prefix;
@@ -1056,6 +1065,12 @@ int unomol_gpu_last_build_ms(UnomolCtx* ctx, double* ms_eri, double* ms_total) {
     return UNOMOL_OK;
 }
 
+int unomol_gpu_set_launch_order(UnomolCtx* ctx, int reversed) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    ctx->reverse_launches = reversed ? 1 : 0;
+    return UNOMOL_OK;
+}
+
 int unomol_gpu_set_counting(UnomolCtx* ctx, int on) {
     if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
     ctx->counting = on ? 1 : 0;
@@ -1181,6 +1196,10 @@ extern "C" int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, dou
                         std::to_string(NOALLOC_MAX_NBF) + " that its static scratch holds");
     if (ctx->prec_mode != UNOMOL_PREC_FP64)
         return fail(ctx, UNOMOL_EINVAL, "unomol_gpu_fock_rhf_noalloc runs the FP64 build only");
+    if (ctx->counting)
+        return fail(ctx, UNOMOL_EINVAL,
+                    "unomol_gpu_fock_rhf_noalloc does not count work (its counters would need an allocation): "
+                    "switch counting off or use unomol_gpu_fock_rhf_device");
     int dev = -1;
     CU(cudaGetDevice(&dev));
     if (dev != ctx->dev) return fail(ctx, UNOMOL_EINVAL, "unomol_gpu_fock_rhf_noalloc: current device is not the context's");
@@ -1203,9 +1222,13 @@ extern "C" int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, dou
     const long long n2 = (long long)n * n, np = (long long)n * (n + 1) / 2;
     double* Pfull = scratch;
     double* T = scratch + n2;
+    int launches = 0;
+    CU(cudaEventRecord(ctx->ev[0], s));
     expand_packed<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(dP, Pfull, n);
+    ++launches;
     CU(cudaGetLastError());
     CU(cudaMemsetAsync(T, 0, n2 * sizeof(double), s));  // the array keeps the previous call's sums
+    CU(cudaEventRecord(ctx->ev[1], s));
     FockArgs A{};
     A.pairs = ctx->d_pairs;
     A.prims = ctx->d_prims;
@@ -1226,9 +1249,16 @@ extern "C" int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, dou
         A.prefix = ctx->d_prefix;
         A.nbp = L.nbp;
         A.nwork = L.nwork;
-        CU(launch_fock_fp64(L.bc, L.kc, false, A, ctx->nt, ctx->d_rys, s));
+        // the regular build's method selection: MD mode, runtime-L and MD classes included
+        CU(launch_class_kernel(ctx, L, false, false, A, s));
+        ++launches;
     }
+    CU(cudaEventRecord(ctx->ev[2], s));
     fold_packed<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(T, dG, n);
+    ++launches;
+    CU(cudaEventRecord(ctx->ev[3], s));
     CU(cudaGetLastError());
+    // unomol_gpu_get_stats / unomol_gpu_last_build_ms then describe this build
+    ctx->stats.kernel_launches = launches;
     return UNOMOL_OK;
 }

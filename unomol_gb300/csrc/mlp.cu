@@ -2,6 +2,7 @@
 // BF16 GEMM of tc_gemm.cuh with fused epilogues (bias + SiLU forward, SiLU derivative backward, split-K
 // atomic accumulation of the weight gradients), plus small FP32 kernels for the bias gradients, the
 // BF16 conversions and Adam.  Master weights are FP32; the GEMM operands are BF16 copies.
+#include <atomic>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -64,8 +65,12 @@ cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, const TcGemm
 
 // C = A . B^T; operands K-major, row strides multiples of 8 elements, 16-byte aligned.  Split-K (an
 // additive epilogue) when the output has fewer tiles than the GPU has SMs.
+// Poll limit of the GEMMs' pipeline waits for the whole process (unomol_tc_set_wait_polls).
+std::atomic<int> g_tc_pipeline_polls{0};
+
 cudaError_t tc_gemm_launch(TcGemmArgs g, cudaStream_t s, int num_sms) {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
+    g.pipeline_polls = g_tc_pipeline_polls.load();
     if ((g.lda & 7) || (g.ldb & 7) || (reinterpret_cast<uintptr_t>(g.A) & 15) || (reinterpret_cast<uintptr_t>(g.B) & 15))
         return cudaErrorInvalidValue;
     const int bn = g.N <= 64 ? 64 : g.N <= 128 ? 128 : 256;
@@ -436,6 +441,8 @@ int Mlp::check_status(cudaStream_t s) {
     MLP_CK(cudaStreamSynchronize(s));
     if (h) {
         err = "tensor-core GEMM: a bounded wait gave up";
+        MLP_CK(cudaMemsetAsync(status, 0, sizeof(int), s));  // reported once; later calls start clean
+        MLP_CK(cudaStreamSynchronize(s));
         return UNOMOL_ETIMEOUT;
     }
     return UNOMOL_OK;
@@ -452,6 +459,11 @@ thread_local std::string g_mlp_err;
 }
 
 extern "C" {
+
+int unomol_tc_set_wait_polls(int polls) {
+    g_tc_pipeline_polls.store(polls);
+    return UNOMOL_OK;
+}
 
 int unomol_tc_gemm_bf16(const void* A, const void* B, int M, int N, int K, float* C, int* status, void* stream) {
     if (!A || !B || !C || M < 0 || N < 0 || K < 0) return UNOMOL_EINVAL;

@@ -15,9 +15,13 @@
 //     after the last chunk it commits to the "done" barrier;
 //   * all four warps: wait for "done", read the accumulator with tcgen05.ld (warp w owns rows
 //     32w..32w+31), apply the fused epilogue and store.
-// Every wait is bounded (TC_WAIT_POLLS polls): a wait that gives up sets the CTA's error flag and the
-// kernel's status word; before returning, the CTA waits (bounded) for the TMA loads it issued and the
-// MMAs it committed, and always releases its tensor memory.
+// Every wait is bounded: a wait that gives up sets the CTA's error flag and the kernel's status word;
+// before returning, the CTA waits (bounded) for the TMA loads it issued and the MMAs it committed, and
+// always releases its tensor memory.  The pipeline waits (producer on "empty", MMA issuer on "full")
+// poll TcGemmArgs::pipeline_polls times (0: TC_WAIT_POLLS; negative: not at all, so that the first
+// of them gives up -- the host-side test of this failure path); the drain waits for work already
+// issued ("done", the outstanding "full" phases) always poll TC_WAIT_POLLS times, so nothing issued is
+// still in flight when the CTA releases its tensor memory and exits.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -51,6 +55,7 @@ struct TcGemmArgs {
     int ldc;
     int chunks_per_split;    // K chunks of one blockIdx.z
     int* status;             // set to 1 when a wait gave up
+    int pipeline_polls;      // polls of the pipeline waits: 0 = TC_WAIT_POLLS, < 0 = none (give up at once)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -78,9 +83,9 @@ __host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
            | ((uint32_t)(M >> 4) << 24);      // M / 16
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int polls = TC_WAIT_POLLS) {
     uint32_t done = 0;
-    for (int it = 0; it < TC_WAIT_POLLS && !done; ++it) {
+    for (int it = 0; it < polls && !done; ++it) {
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
@@ -143,11 +148,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
+    const int polls = g.pipeline_polls == 0 ? TC_WAIT_POLLS : max(g.pipeline_polls, 0);
     if (warp == 0 && lane == 0) {
         // producer: TMA loads into the ring
         for (int i = 0; i < nk; ++i) {
             const int s = i % TC_STAGES;
-            if (i >= TC_STAGES && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((i / TC_STAGES - 1) & 1))) {
+            if (i >= TC_STAGES && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((i / TC_STAGES - 1) & 1), polls)) {
                 atomicExch(&failed, 1);
                 break;
             }
@@ -166,7 +172,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         int i = 0;
         for (; i < nk; ++i) {
             const int s = i % TC_STAGES;
-            if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((i / TC_STAGES) & 1))) {
+            if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((i / TC_STAGES) & 1), polls)) {
                 atomicExch(&failed, 1);
                 break;
             }

@@ -35,6 +35,7 @@ EXPORTS = [
     "unomol_gpu_one_electron", "unomol_gpu_one_electron_last_error", "unomol_gpu_l2_peak", "unomol_gpu_batch_scf",
     "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
     "unomol_gpu_moment_ints", "unomol_gpu_batch_set_precision", "unomol_gpu_batch_fock_device",
+    "unomol_tc_set_wait_polls", "unomol_gpu_set_launch_order",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -88,6 +89,8 @@ def lib() -> C.CDLL:
     L.unomol_gpu_set_screening.argtypes = [C.c_void_p, C.c_double]
     L.unomol_gpu_set_rys_mode.argtypes = [C.c_void_p, C.c_int]
     L.unomol_gpu_set_counting.argtypes = [C.c_void_p, C.c_int]
+    L.unomol_gpu_set_launch_order.argtypes = [C.c_void_p, C.c_int]
+    L.unomol_tc_set_wait_polls.argtypes = [C.c_int]
     L.unomol_gpu_last_build_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.unomol_gpu_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.unomol_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
@@ -211,6 +214,9 @@ class TwoElectronInts:
 
     def set_counting(self, on: bool):
         _check(lib().unomol_gpu_set_counting(self._h, 1 if on else 0), self._h)
+
+    def set_launch_order(self, reversed_: bool):
+        _check(lib().unomol_gpu_set_launch_order(self._h, 1 if reversed_ else 0), self._h)
 
     def set_screening(self, cutoff: float):
         _check(lib().unomol_gpu_set_screening(self._h, float(cutoff)), self._h)
