@@ -22,9 +22,17 @@ k = 0, 8, ..., else the density change), cycled for K steps.
            stays in L2): peak = flops / max(flops64/peak64, flops32/peak32), the two pipes busy at
            once (peak_one_after_other = flops / (flops64/peak64 + flops32/peak32) beside it); flops
            of each part booked to the pipe that does them, at the quartets of the build's own lists;
-  cpu_baseline the C restatement of the reference algorithm (oracle/) on the host cores, on a strided
-           sample of the shell quartets of one full build.
---impl reference: that CPU implementation as the reference arm (same metric and workload).
+  fp64_incremental  the same incremental sequence with the FP32 part off (density-screened FP64
+           builds): value / fp64_incremental is the gain of FP32, fp64_incremental / plain_fp64 that of
+           the incremental build;
+  batched_form the batching workload (256 molecules, alkanes C1-C8 and 1-6 water clusters, STO-3G or
+           6-31G): batched FP64 and precision-form builds of the converged densities, and the batched
+           SCF of both forms (|dE| per molecule);
+  cpu_baseline the C restatement of the reference algorithm (oracle/) on the host cores, on a
+           pseudo-random third of the canonical shell quartets of one full build (hashed sample).
+--impl reference: that CPU implementation as the reference arm (same metric and workload): its K steps
+           are the K hashed slices of ONE full FP64 build (slice s = the quartets with hash(q) % K == s),
+           so the timed region covers exactly one whole build; one slice is timed again on one core.
 --form fp64: the plain FP64 path as the measured form.
 Multi-GPU: replicas only (every rank runs the whole workload; value sums over ranks).
 """
@@ -48,8 +56,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Fock builds/sec (32-water 6-31G RHF SCF Fock builds)"
 UNIT = "Fock builds/s"
 WORKLOAD = "32-water cluster, 6-31G, RHF, 416 basis functions (seed 0): Fock builds of the converging SCF"
-CPU_STRIDE = 64  # per step of --impl reference (~0.6 s on 16 Grace cores)
-CPU_BASELINE_STRIDE = 4  # the cpu_baseline of the measured line: ~10 s on 16 Grace cores
+CPU_BASELINE_STRIDE = 3  # the cpu_baseline of the measured line: a hashed third, ~10 s on 16 Grace cores
 FP32_CUTOFF = 1e-3  # swept 1e-7..1e0 in profiles/fp32_cutoff_sweep_water32.md; |dE| stays ~1e-9 Eh here
 # quartets with Schwarz bound x max|dP| below this are skipped in a build: at 1e-12 the skipped parts of
 # ~1e8 quartets left 1e-9..1e-8 Eh of energy noise per incremental build, which stalled the 1e-10 Eh
@@ -152,14 +159,15 @@ def ensure_oracle():
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
 
 
-def cpu_port_rate(b, P, stride, threads):
-    """Fock builds/s of the C restatement on a 1/stride sample of one full build (extrapolated)."""
+def cpu_slice(b, P, stride, offset, threads):
+    """Seconds and counts of the C restatement on the hashed slice `offset` of `stride` (a
+    pseudo-random 1/stride of the canonical shell quartets of one full build; the stride slices
+    partition the build)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import orc
     t0 = time.perf_counter()
-    orc.fock(b, P, stride=stride, offset=0, threads=threads)
-    dt = time.perf_counter() - t0
-    return 1.0 / (dt * stride), dt
+    _, cnt = orc.fock(b, P, stride=stride, offset=offset, threads=threads, hashed=True)
+    return time.perf_counter() - t0, cnt
 
 
 def synthetic_density(b):
@@ -170,6 +178,12 @@ def synthetic_density(b):
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores: the K = --steps steps are the K hashed slices of
+    one full FP64 build of the workload, so the timed region is exactly one whole build (measured, not
+    extrapolated); value = 1 build / the summed step times.  The reference's work does not depend on
+    the density (it computes every canonical quartet and keeps |v| > 1e-14), so a synthetic density
+    of the cluster's trace stands in for the SCF's densities.  Then slice 0 once more on one core
+    (the reference is a serial program): the one-core figure is that slice's time x K."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
@@ -177,20 +191,33 @@ def run_reference(args):
     b = basis()
     P = synthetic_density(b)
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_port_rate(b, P, CPU_STRIDE * 4, threads)
-    times = []
-    for _ in range(args.steps):
-        _, dt = cpu_port_rate(b, P, CPU_STRIDE, threads)
-        times.append(dt * CPU_STRIDE)
-    value = len(times) / sum(times)
-    sample = (f"C restatement of the reference algorithm (full FP64 build), every {CPU_STRIDE}th canonical shell "
-              f"quartet per step ({100.0 / CPU_STRIDE:.2f}% of a build), extrapolated")
+    K = max(1, args.steps)
+    for w in range(args.warmup):  # warm-up: tiny hashed samples (1/(64 K) of a build each)
+        cpu_slice(b, P, 64 * K, w, threads)
+    times, counts = [], np.zeros(4, np.int64)
+    for s in range(K):
+        dt, cnt = cpu_slice(b, P, K, s, threads)
+        times.append(dt)
+        counts += cnt
+    total = sum(times)
+    value = 1.0 / total
+    t1, cnt1 = cpu_slice(b, P, K, 0, 1)
+    single = 1.0 / (t1 * K)
+    sample = (f"C restatement of the reference algorithm, full FP64 build of the workload split into {K} hashed slices "
+              f"(one per step; together exactly one build: {int(counts[0])} shell quartets, {int(counts[1])} function "
+              f"quartets), {threads} threads")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "form": "reference algorithm (CPU), full FP64 builds"},
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated geometry, synthetic density)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "form": "reference algorithm (CPU), full FP64 build",
+                       "step": f"1/{K} of one full build (hashed slice); the {K} steps are one whole build",
+                       "extrapolated": False},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "single_core": {"value": single, "unit": UNIT, "cores": 1, "kind": "port", "extrapolated": True,
+                            "sample": f"hashed slice 0 of {K} ({int(cnt1[1])} function quartets) on one thread: "
+                                      f"{t1:.1f} s, x {K}"},
+            "slice_s": [round(x, 3) for x in times],
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -279,6 +306,55 @@ def timed_batch_builds(bat, inputs, steps, dev, stream, flush):
         ev[k][1].record(stream)
     torch.cuda.synchronize(dev)
     return [a.elapsed_time(b_) for a, b_ in ev]
+
+
+def batch_form(args, dev, stream, flush):
+    """The batching workload (molecules.batch_workload(0): 256 molecules, 7-108 functions): the FP64
+    batched SCF to convergence (its densities are the build inputs), then batched builds of those
+    densities in FP64 and in the precision form (autotuned, CUDA graph per build, L2 flushed per
+    build), and the batched SCF of the precision form (full builds) for |dE| per molecule."""
+    import torch
+
+    from unomol_gb300 import molecules, native
+    from unomol_gb300.basis import Basis
+    bases = [Basis(text=t) for _, t in molecules.batch_workload(0)]
+    out = {"molecules": len(bases), "nbf_total": int(sum(x.norb for x in bases)),
+           "nbf_max": int(max(x.norb for x in bases))}
+    bat = native.Batch(bases)
+    SH = [native.one_electron_gpu(x) for x in bases]
+    S, H = [x[0] for x in SH], [x[1] for x in SH]
+    bat.scf(S=S, H=H, maxits=4)  # warm-up of the batched SCF (first-use costs)
+    r64 = bat.scf(S=S, H=H)
+    Pcat = np.concatenate(r64["P"])
+    rates = {}
+    for form in ("fp64", "mixed"):
+        if form == "mixed":
+            bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, SKIP_CUTOFF)
+        bat.set_densities(r64["P"])
+        bat.autotune(2)
+        inp = [(True, Pcat)]
+        timed_batch_builds(bat, inp, 3, dev, stream, flush)
+        ms = timed_batch_builds(bat, inp, args.steps, dev, stream, flush)
+        rates[form] = (len(ms) / (sum(ms) / 1e3), statistics.mean(ms))
+    Gm = np.concatenate(bat.get_focks())
+    rm = bat.scf(S=S, H=H)  # precision form still set: every iteration's build mixed
+    bat.set_precision(native.PREC_FP64, 0.0, SKIP_CUTOFF)
+    bat.set_densities(r64["P"])
+    bat.fock(native.BATCH_GRAPH)
+    G64 = np.concatenate(bat.get_focks())
+    bat.close()
+    dE = np.abs(rm["energy"] - r64["energy"])
+    out.update({"value": rates["mixed"][0], "unit": "batch Fock builds/s (256 molecules each)",
+                "ms_per_build": rates["mixed"][1], "fp64_value": rates["fp64"][0], "fp64_ms_per_build": rates["fp64"][1],
+                "speedup_vs_fp64_batch": rates["mixed"][0] / rates["fp64"][0],
+                "molecule_builds_per_s": len(bases) * rates["mixed"][0],
+                "max_abs_dG_vs_fp64_batch": float(np.max(np.abs(Gm - G64))),
+                "scf_max_abs_dE": float(dE.max()), "scf_mean_abs_dE": float(dE.mean()),
+                "scf_converged": int(np.sum(r64["converged"] & rm["converged"])),
+                "scf_wall_s_fp64": r64["seconds"], "scf_wall_s_mixed": rm["seconds"],
+                "note": "builds of the converged FP64 densities (full builds); precision form at the value's FP32 and "
+                        "density-skip cutoffs; |dE| per molecule: batched SCF of the form against the FP64 batched SCF"})
+    return out
 
 
 def counted_flops(ctx, inputs, dev, stream):
@@ -376,26 +452,20 @@ def run_ours(args):
     timed_builds(plain, plain_inputs, 2, dev, stream, flush)
     p_ms, p_eri = timed_builds(plain, plain_inputs, min(args.steps, len(plain_inputs)), dev, stream, flush)
     plain_rate = len(p_ms) / (sum(p_ms) / 1e3)
-    # the same builds through the batched path (a one-molecule batch: persistent kernels per class,
-    # autotuned launch shapes, each build one CUDA-graph replay), same precision form
-    bat = native.Batch([b])
-    if args.form == "mixed":
-        bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, SKIP_CUTOFF)
-    bat.set_densities([inputs[0][1]])
-    tuned = bat.autotune(2)
-    timed_batch_builds(bat, inputs, max(args.warmup, 3), dev, stream, flush)
-    b_ms = timed_batch_builds(bat, inputs, args.steps, dev, stream, flush)
-    batched_rate = args.steps / (sum(b_ms) / 1e3)
-    kchk = 1 % len(inputs)
-    bat.set_densities([inputs[kchk][1]])
-    bat.fock(native.BATCH_GRAPH)
-    Gb = bat.get_focks()[0]
-    Gs = mixed.form_g(inputs[kchk][1])
-    batched = {"value": batched_rate, "unit": UNIT, "ms_per_build": statistics.mean(b_ms),
-               "speedup_vs_plain_fp64": batched_rate / plain_rate, "autotune": [list(c) for c in tuned],
-               "max_abs_dG_vs_single_context": float(np.max(np.abs(Gb - Gs))),
-               "note": "one-molecule batch: persistent kernels per quartet class, CUDA graph per build, L2 flushed per build"}
-    bat.close()
+    # the same incremental sequence with the FP32 part off: density-screened FP64 builds
+    # (fp32 cutoff <= skip cutoff), to read the gains of the incremental build and of FP32 apart
+    inc64 = native.TwoElectronInts(b)
+    inc64.set_precision(native.PREC_MIXED, 0.0)
+    inc64.set_density_screening(SKIP_CUTOFF)
+    timed_builds(inc64, inputs, 2, dev, stream, flush)
+    i_ms, _ = timed_builds(inc64, inputs, args.steps, dev, stream, flush)
+    inc_rate = len(i_ms) / (sum(i_ms) / 1e3)
+    fp64_incremental = {"value": inc_rate, "unit": UNIT, "ms_per_build": statistics.mean(i_ms),
+                        "incremental_gain": inc_rate / plain_rate, "fp32_gain": value / inc_rate,
+                        "note": "the value's build sequence, density skip cutoff as the value's, FP32 off: "
+                                "fp32_gain = value / this, incremental_gain = this / plain_fp64"}
+    inc64.close()
+    batched = batch_form(args, dev, stream, flush) if args.form == "mixed" and not args.no_batch else None
     # end to end through the host entry point, pinned host buffers
     pin_in = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for _, x in inputs]
     Gh = torch.zeros(b.no2, dtype=torch.float64).pin_memory()
@@ -456,6 +526,7 @@ def run_ours(args):
             "batched_form": batched,
             "plain_fp64": {"value": plain_rate, "unit": UNIT, "ms_per_build": statistics.mean(p_ms),
                            "kernel_ms": statistics.mean(p_eri), "speedup_of_value": value / plain_rate},
+            "fp64_incremental": fp64_incremental,
             "scf": {"energy_plain_fp64": r64["energy"], "energy_form": rm["energy"],
                     "abs_dE": abs(rm["energy"] - r64["energy"]), "max_abs_dF": max_dF,
                     "max_abs_dF_note": "G of the converged plain-FP64 density: full build of the form against the plain build",
@@ -479,10 +550,11 @@ def run_ours(args):
     if rank == 0 and ws == 1:
         ensure_oracle()
         threads = os.cpu_count() or 1
-        rate, dt = cpu_port_rate(b, synthetic_density(b), CPU_BASELINE_STRIDE, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"C restatement of the reference algorithm, full FP64 build, every {CPU_BASELINE_STRIDE}th "
-                                          f"canonical shell quartet ({dt:.1f} s), extrapolated to one build"}
+        dt, cnt = cpu_slice(b, synthetic_density(b), CPU_BASELINE_STRIDE, 0, threads)
+        line["cpu_baseline"] = {"value": 1.0 / (dt * CPU_BASELINE_STRIDE), "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"C restatement of the reference algorithm, full FP64 build: a hashed 1/{CPU_BASELINE_STRIDE} "
+                                          f"of the canonical shell quartets ({int(cnt[1])} function quartets, {dt:.1f} s), x "
+                                          f"{CPU_BASELINE_STRIDE}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -499,6 +571,7 @@ def main():
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp32-cutoff", type=float, default=FP32_CUTOFF)
     ap.add_argument("--profile", action="store_true", help="device builds only (for ncu captures)")
+    ap.add_argument("--no-batch", action="store_true", help="leave out the 256-molecule batched form")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -49,9 +49,13 @@ def _desc(b):
     return d, keep
 
 
-def fock(b, Pa, Pb=None, exact=False, stride=1, offset=0, threads=0, start=0):
+def fock(b, Pa, Pb=None, exact=False, stride=1, offset=0, threads=0, start=0, hashed=False):
     """G(P) (RHF, Pb None) or (Ga, Gb) (UHF), plus counts [shell quartets, function quartets,
-    primitive quartets, stored integrals]."""
+    primitive quartets, stored integrals].  stride > 1: only the canonical quartets q with
+    q % stride == offset; with hashed, those with hash(q) % stride == offset (a pseudo-random
+    1/stride of every class; the stride offsets partition the build)."""
+    if hashed and stride > 1:
+        stride = -stride
     d, keep = _desc(b)
     Pa = np.ascontiguousarray(Pa, np.float64)
     Ga = np.zeros(b.no2)

@@ -278,7 +278,18 @@ static void scatter(double val, int i, int j, int k, int l, const double* Pa, co
     }
 }
 
-/* Full G over the canonical quartets of TwoElectronInts::calculate, or a strided sample of them.
+/* splitmix64 finaliser: a well-mixed 64-bit hash of the quartet index (for the hashed sample) */
+static unsigned long long mix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* Full G over the canonical quartets of TwoElectronInts::calculate, or a sample of them: stride > 1
+ * keeps the quartets with q % stride == offset (q = running index of the canonical enumeration);
+ * stride < -1 keeps those with hash(q) % |stride| == offset, a pseudo-random 1/|stride| of every
+ * class, and the |stride| offsets partition the build.
  * Pb == NULL: RHF (G += 2J - K); else UHF (Ga, Gb).  rys_mode 0 = reference-compatible, 1 = exact.
  * counts (optional): [0] shell quartets done, [1] function quartets, [2] primitive quartets,
  * [3] stored integrals.  Returns 0, or -1 for an unsupported basis (L > 2). */
@@ -294,6 +305,8 @@ int orc_fock(const orc_basis* B, int start, const double* Pa, const double* Pb, 
         sp0[s] = np;
         np += B->shell_nprim[s];
     }
+    const int hashed = stride < -1;
+    if (hashed) stride = -stride;
     if (stride < 1) stride = 1;
     long long tot[4] = {0, 0, 0, 0};
 #ifdef _OPENMP
@@ -314,7 +327,9 @@ int orc_fock(const orc_basis* B, int start, const double* Pa, const double* Pb, 
             for (int jsh = 0; jsh <= ish; ++jsh) {
                 for (int ksh = 0; ksh <= ish; ++ksh) {
                     for (int lsh = 0; lsh <= ksh; ++lsh, ++q) {
-                        if (q % stride != offset) continue;
+                        if (stride > 1 && (long long)((hashed ? mix64((unsigned long long)q) : (unsigned long long)q) %
+                                                      (unsigned long long)stride) != offset)
+                            continue;
                         int sh[4] = {ish, jsh, ksh, lsh};
                         int off[4], lv[4], nls[4];
                         for (int t = 0; t < 4; ++t) {

@@ -8,22 +8,38 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_reference_arm_json_line():
-    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0"], env=env, capture_output=True, text=True, timeout=600)
-    assert r.returncode == 0, r.stderr[-2000:]
-    lines = [l for l in r.stdout.splitlines() if l.strip()]
+def test_reference_arm_json_line(monkeypatch, capsys):
+    """The reference arm's line, on a small molecule in place of the 32-water cluster (same code path):
+    the contract keys, and its K steps are exactly one full build (the hashed slices' counts add up to
+    the unsampled build's)."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bench
+    import orc
+    from unomol_gb300 import molecules
+    from unomol_gb300.basis import Basis
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    small = Basis(text=molecules.patin_text(molecules.alkane(3), "6-31G"))
+    monkeypatch.setattr(bench, "basis", lambda: small)
+    assert bench.run_reference(argparse.Namespace(steps=4, warmup=1, gpus=1)) == 0
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.strip()]
     assert len(lines) == 1
     d = json.loads(lines[0])
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
-              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e", "single_core"):
         assert k in d, k
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["config"]["workload"].startswith("32-water cluster, 6-31G")
+    assert d["config"]["extrapolated"] is False
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["single_core"]["cores"] == 1 and d["single_core"]["value"] > 0
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert len(d["slice_s"]) == 4 and abs(d["ms_per_step"] * 4 / 1e3 - sum(d["slice_s"])) < 1e-2
+    _, full = orc.fock(small, bench.synthetic_density(small))
+    assert f"{int(full[0])} shell quartets, {int(full[1])} function quartets" in d["cpu_baseline"]["sample"]
 
 
 FAKE_SMI = r'''#!{python}
