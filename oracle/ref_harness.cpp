@@ -450,7 +450,9 @@ extern "C" {
 // Stock SCF trajectory: the first kmax energies (energy + nucrep after each update) of findEnergy's
 // loop on basis `vb` with the integrals of `vt` (a TwoElectronInts over the same shells), core-H
 // guess.  Returns the number of energies written (fewer when the loop converged earlier).
-int refh_scf_trace(void* vb, void* vt, const char* workdir, int kmax, double* e_out) {
+// perturb != 0 scales the starting density by (1 + perturb): a probe of how strongly the trajectory
+// amplifies a difference in its input.
+int refh_scf_trace(void* vb, void* vt, const char* workdir, int kmax, double* e_out, double perturb) {
     char cwd[4096];
     if (!getcwd(cwd, sizeof(cwd))) return -1;
     if (chdir(workdir) != 0) return -2;
@@ -460,10 +462,12 @@ int refh_scf_trace(void* vb, void* vt, const char* workdir, int kmax, double* e_
     if (b->number_of_electrons() % 2) {
         unomol::UnRestrictedHartreeFock hf(b, t);
         scf_setup(hf, nullptr);
+        for (int i = 0; i < hf.no2; ++i) hf.PmatA[i] *= 1.0 + perturb, hf.PmatB[i] *= 1.0 + perturb;
         k = stock_trace(hf, kmax, e_out);
     } else {
         unomol::RestrictedHartreeFock hf(b, t);
         scf_setup(hf, nullptr);
+        for (int i = 0; i < hf.no2; ++i) hf.Pmat[i] *= 1.0 + perturb;
         k = stock_trace(hf, kmax, e_out);
     }
     if (chdir(cwd) != 0) return -3;

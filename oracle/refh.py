@@ -65,7 +65,7 @@ def lib(md=False) -> C.CDLL:
     L.refh_dpm_h.restype = C.c_int
     L.refh_dpm_h.argtypes = [C.c_char_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, _ip]
     L.refh_scf_trace.restype = C.c_int
-    L.refh_scf_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_int, _dp]
+    L.refh_scf_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_int, _dp, C.c_double]
     L.refh_scf_diis.restype = C.c_int
     L.refh_scf_diis.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                 C.c_double, _dp, _dp]
@@ -174,12 +174,13 @@ def run_scf(patin_path: str, md: bool = False):
             "pdiff": out[4], "nucrep": out[5], "t_ints": out[6], "t_scf": out[7], "P": P}
 
 
-def scf_trace(basis: RefBasis, tints: RefTwoElectronInts, kmax: int) -> np.ndarray:
+def scf_trace(basis: RefBasis, tints: RefTwoElectronInts, kmax: int, perturb: float = 0.0) -> np.ndarray:
     """The first kmax total energies of the stock damped SCF loop (RHF.hpp:140-166 / UHF.hpp:150-163,
-    core-Hamiltonian guess) of `basis`, with the integrals of `tints` (same shells)."""
+    core-Hamiltonian guess) of `basis`, with the integrals of `tints` (same shells).  perturb: the
+    starting density scaled by (1 + perturb), to measure how the trajectory amplifies a difference."""
     e = np.zeros(kmax)
     with tempfile.TemporaryDirectory(prefix="unomol_trace_") as wd:
-        k = basis.L.refh_scf_trace(basis.h, tints.h, wd.encode(), kmax, e)
+        k = basis.L.refh_scf_trace(basis.h, tints.h, wd.encode(), kmax, e, float(perturb))
     if k < 0:
         raise RuntimeError(f"refh_scf_trace failed: {k}")
     return e[:k].copy()

@@ -21,7 +21,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+import sys  # noqa: E402
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "oracle"))
+import refh  # noqa: E402
+
+REF = refh.REFERENCE
 CASES = [f"{b}.{m}" for b in ("3g", "431", "631") for m in ("co", "h2o", "hf", "nh3")]
 NUM = r"[-+]?\d+\.\d+(?:[eE][-+]?\d+)?"
 

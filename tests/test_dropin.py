@@ -6,6 +6,7 @@
 * GPU: a C++ driver of the drop-in class reproduces the reference's G(P) (RHF and UHF) on golden cases.
 """
 import os
+import sys
 import subprocess
 import tempfile
 
@@ -16,7 +17,10 @@ from conftest import ROOT, load_golden
 
 INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(ROOT, "unomol_gb300")
-REF = "/root/reference"
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import refh  # noqa: E402
+
+REF = refh.REFERENCE
 
 
 def _build_driver(tmp):

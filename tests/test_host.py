@@ -140,7 +140,7 @@ def test_basis_reader_normalisation_matches_reference_export():
         pytest.skip("reference build not present (oracle/_ref)")
     from unomol_gb300.basis import Basis
     for tag in ("631.h2o", "dh95.co2", "3g.ch4"):
-        path = f"/root/reference/test/patin.dat.{tag}"
+        path = os.path.join(refh.REFERENCE, "test", f"patin.dat.{tag}")
         rb = refh.RefBasis(path)
         info, a, c, cen = rb.export()
         b = Basis(path)

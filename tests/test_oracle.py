@@ -64,3 +64,27 @@ def test_oracle_matches_closed_form_s_integrals(exact):
     b, P, G = closed_form_s_basis()
     Go, _ = orc.fock(b, P, exact=exact)
     assert np.abs(Go - G).max() <= 1e-13 * np.abs(G).max()
+
+
+def test_reference_damped_trajectory_amplifies_input_differences():
+    """Why the scale tests hold the damped loop's energies to 1e-8 Eh for three iterations only: on
+    n-decane the reference's own stock loop (core-H guess) moves by more than 1e-9 Eh at its fourth
+    energy and by more than 1e-7 Eh at its fifth when its starting density is scaled by 1 + 1e-13,
+    while its first three energies move by less than 1e-9 Eh (oracle/ref_harness.cpp: refh_scf_trace)."""
+    import os
+    import tempfile
+    import refh
+    if not refh.available():
+        pytest.skip("reference build not present (oracle/_ref)")
+    g = load_golden("decane_631g")
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "patin.dat")
+        with open(p, "w") as f:
+            f.write(str(g["patin"]))
+        b = refh.RefBasis(p)
+        t = refh.RefTwoElectronInts(b)
+        e0 = refh.scf_trace(b, t, 5)
+        e1 = refh.scf_trace(b, t, 5, 1e-13)
+    assert np.abs(e0 - g["trace"]).max() == 0.0  # the fixture is this trajectory
+    d = np.abs(e1 - e0)
+    assert d[:3].max() < 1e-9 and d[3] > 1e-9 and d[4] > 1e-7, d

@@ -2,7 +2,7 @@
 torchrun) runs the whole workload; the timed region is bracketed by barriers and the job's time is the
 maximum over ranks, so the whole-job rate is world_size * steps / that time ("weak" scaling: the work
 per GPU is fixed).  The reference shards shell quartets over MPI ranks and reduces G
-(TwoElectronIntsMPI.cpp:350-354, RHF_MPI.hpp:105-108); one GB300 runs a 32-water build in ~12 ms, so
+(TwoElectronIntsMPI.cpp:350-354, RHF_MPI.hpp:105-108); one GB300 runs a 32-water build in a few milliseconds, so
 replicas (no data-path collective) are the measured multi-GPU form here.
 
 The helpers are backend-agnostic: the tensors live on `device` (CPU for gloo, the rank's GPU for NCCL).
