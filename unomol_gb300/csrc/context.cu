@@ -145,8 +145,10 @@ void build_norms(NormTable& nt) {
         dx *= (2 * i + 1);
     }
     for (int l = 0; l <= LMAX; ++l)
-        for (int c = 0; c < ncart(l); ++c)
+        for (int c = 0; c < ncart(l); ++c) {
             nt.v[l][c] = 1.0 / std::sqrt(dfact[cart_lx(l, c)] * dfact[cart_ly(l, c)] * dfact[cart_lz(l, c)]);
+            nt.f[l][c] = (float)nt.v[l][c];
+        }
 }
 
 // Algorithmic flops of the Rys kernels (FMA = 2, every +,-,*,/,sqrt = 1), counted from the steps of
@@ -622,6 +624,8 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     A.Tb = uhf ? ctx->d_Tb : nullptr;
     A.thr_int = STORE_CUT;
     A.prim_cut = PRIM_CUT;
+    A.thr_int32 = (float)STORE_CUT;
+    A.prim_cut32 = (float)PRIM_CUT;
     A.fp32_cut = ctx->fp32_cut;
     A.nshell = ctx->nshell;
     A.rys_compat = ctx->rys_mode == UNOMOL_RYS_REFERENCE;
@@ -645,6 +649,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         launches += 4;
         A.dmax = ctx->d_dmax;
         A.skip_cut = ctx->skip_cut;
+        A.skip_cut32 = (float)ctx->skip_cut;
         A.dyn_mseg = ctx->d_mseg;
         CU(wl_to_float(ctx->d_Pa, ctx->d_Pa32, n2, s));
         A.Pa32 = ctx->d_Pa32;
@@ -849,7 +854,7 @@ namespace {
 constexpr int RYS64_LEN = rys_table_len(RysStride<double>::value);
 constexpr int RYS32_LEN = rys_table_len(RysStride<float>::value);
 static __device__ __align__(16) double g_rys64[RYS64_LEN];
-static __device__ __align__(16) float g_rys32[RYS32_LEN];
+static __device__ __align__(32) float g_rys32[RYS32_LEN];  // 32-byte rows: one 256-bit load each
 constexpr int RYS_MAX_DEVICES = 64;
 double* g_rys64_ptr[RYS_MAX_DEVICES] = {nullptr};
 float* g_rys32_ptr[RYS_MAX_DEVICES] = {nullptr};
@@ -1240,6 +1245,8 @@ extern "C" int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, dou
     A.Tb = nullptr;
     A.thr_int = STORE_CUT;
     A.prim_cut = PRIM_CUT;
+    A.thr_int32 = (float)STORE_CUT;
+    A.prim_cut32 = (float)PRIM_CUT;
     A.nshell = ctx->nshell;
     A.rys_compat = ctx->rys_mode == UNOMOL_RYS_REFERENCE;
     A.counters = nullptr;

@@ -60,6 +60,8 @@ struct ShellPair {
     int ish, jsh;          // shell indices (ish >= jsh)
     int maxsh;             // max(ish, jsh)
     int pad;
+    float ABf[3];          // A - B and q in FP32, for the FP32 kernels (no FP64 work or conversion there)
+    float qf;
 };
 
 // A rectangle (or triangle, when bra block == ket block) of quartets between two pair blocks,
@@ -92,6 +94,7 @@ struct FockArgs {
     double* Tb;                 // UHF beta accumulator
     double thr_int;             // per-integral cut (1e-14)
     double prim_cut;            // primitive prefactor cut (1e-12)
+    float thr_int32, prim_cut32, skip_cut32;  // the same cuts in FP32, for the FP32 kernels
     double fp32_cut;            // mixed mode: bound*pmax below this -> FP32 kernel, else FP64
     int mode;                   // 0 all quartets; 1 only "large" (FP64 part); 2 only "small" (FP32 part)
     int nshell;

@@ -173,6 +173,8 @@ FockArgs batch_args(UnomolBatch* b, const BLaunch& L, int k) {
     A.Ta = b->d_T;
     A.thr_int = STORE_CUT;
     A.prim_cut = PRIM_CUT;
+    A.thr_int32 = (float)STORE_CUT;
+    A.prim_cut32 = (float)PRIM_CUT;
     A.rys_compat = b->rys_compat;
     A.mol_nbf = b->d_nbf;
     A.mol_base = b->d_doff;
@@ -183,6 +185,7 @@ FockArgs batch_args(UnomolBatch* b, const BLaunch& L, int k) {
     A.pmax = b->d_pmax;
     A.dmax = b->d_dmax;
     A.skip_cut = b->skip_cut;
+    A.skip_cut32 = (float)b->skip_cut;
     A.fp32_cut = b->fp32_cut;
     A.dyn_mseg = b->d_mseg;
     A.mol_nshell = b->d_nshell;

@@ -46,23 +46,67 @@ __device__ __forceinline__ void load_row(const double* __restrict__ c, double (&
         v[2 * q + 1] = t.y;
     }
 }
+// FP32 rows are 8 floats (32 bytes, 32-byte aligned): one 256-bit load, half the load instructions of
+// two 16-byte loads (the FP32 kernels are bound by the L1 wavefronts of these per-lane rows)
+static_assert(RysStride<float>::value == 8, "one 256-bit load per FP32 row");
 __device__ __forceinline__ void load_row(const float* __restrict__ c, float (&v)[RysStride<float>::value]) {
-#pragma unroll
-    for (int q = 0; q < RysStride<float>::value / 4; ++q) {
-        const float4 t = __ldg(reinterpret_cast<const float4*>(c) + q);
-        v[4 * q] = t.x;
-        v[4 * q + 1] = t.y;
-        v[4 * q + 2] = t.z;
-        v[4 * q + 3] = t.w;
-    }
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(c));
 }
 
 // |v| > cut (cut >= 0) compared as IEEE bit patterns: integer pipe, no FP64 compare
 __device__ __forceinline__ bool above_cut(double v, double cut) {
     return (__double_as_longlong(v) & 0x7fffffffffffffffLL) > __double_as_longlong(cut);
 }
-__device__ __forceinline__ bool above_cut(float v, double cut) {
-    return (__float_as_int(v) & 0x7fffffff) > __float_as_int((float)cut);
+__device__ __forceinline__ bool above_cut(float v, float cut) {
+    return (__float_as_int(v) & 0x7fffffff) > __float_as_int(cut);
+}
+
+// FP32 -> FP64 on the integer pipe.  The FP64 pipe of this GPU runs at 1/64 of the FP32 rate and also
+// executes the F2F conversions, so the FP32 kernels convert their J/K sums by moving the fields: the
+// sign in place, the exponent rebiased by 1023 - 127, the 23 mantissa bits to the top of the 52.  Exact
+// for every normal float; zero and subnormal floats (|f| < 1.2e-38, below every cut of the build) give
+// a signed zero.  (The kernels produce no infinities or NaN from finite inputs.)
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned hi = (u & 0x80000000u) | (e ? (((e + 896u) << 20) | ((u >> 3) & 0xfffffu)) : 0u);
+    const unsigned lo = e ? (u << 29) : 0u;
+    return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(float v) { return f32_to_f64(v); }
+
+// Taylor coefficients of F1(T) = int_0^1 t^2 e^{-T t^2} dt = sum_k (-T)^k / (k! (2k + 3))
+__host__ __device__ constexpr double boys1_coef(int k) {
+    double f = 1.0;
+    for (int i = 2; i <= k; ++i) f *= i;
+    return (k & 1 ? -1.0 : 1.0) / (f * (2 * k + 3));
+}
+
+// One-root Rys rule in FP32 without tables: weight w = F0(T) and node x = t^2 = F1(T) / F0(T), from
+// the Boys functions F_m(T) = int_0^1 t^{2m} e^{-T t^2} dt.  For T >= 1, F0 = sqrt(pi / T) erf(sqrt T) / 2
+// and F1 = (F0 - e^{-T}) / (2 T) (at T >= 1 the difference loses at most a factor 2); below 1, F1 from
+// its Taylor series (12 terms: the first one left out is below 1e-8 of F1) and F0 = 2 T F1 + e^{-T}
+// (the same relation, now a sum of two positive terms).  About 2e-7 relative, as the FP32 tables
+// (1.1e-7), with no table row read per lane.
+template <bool NEED_X>
+__device__ __forceinline__ void rys1_f32(float T, float& x, float& w) {
+    const float e = expf(-T);
+    float F0, F1 = 0.f;
+    if (T < 1.f) {
+        F1 = float(boys1_coef(11));
+#pragma unroll
+        for (int k = 10; k >= 0; --k) F1 = fmaf(F1, T, float(boys1_coef(k)));
+        F0 = fmaf(2.f * T, F1, e);
+    } else {
+        const float r = rsqrtf(T);
+        F0 = 0.886226925452758f * r * erff(T * r);  // sqrt(pi) / 2 / sqrt(T) * erf(sqrt(T))
+        if (NEED_X) F1 = (F0 - e) * (0.5f * r * r);
+    }
+    w = F0;
+    if (NEED_X) x = __fdividef(F1, F0);
 }
 
 // Reference-compatible two-root regime.  For 15 < T <= 40 the reference's Rys::root2 evaluates a
@@ -91,6 +135,10 @@ template <int NR, typename R>
 __device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, R* w, bool compat = false) {
     constexpr int DEG = RysDeg<R>::value;
     constexpr R TMAX = R(rys_tmax(NR));
+    if constexpr (NR == 1 && sizeof(R) == 4) {  // one root in FP32: closed form, no table
+        rys1_f32<true>(T, x[0], w[0]);
+        return;
+    }
     if constexpr (NR == 2 && sizeof(R) == 8) {
         if (compat && T > R(15) && T <= R(40)) {
             rys2_reference_regime(T, x, w);
@@ -209,8 +257,14 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     constexpr int NR = Q::NR;
 #pragma unroll
     for (int f = 0; f < Q::NF; ++f) acc[f] = R(0);
-    const R ABx = R(bra.AB[0]), ABy = R(bra.AB[1]), ABz = R(bra.AB[2]);
-    const R CDx = R(ket.AB[0]), CDy = R(ket.AB[1]), CDz = R(ket.AB[2]);
+    R ABx, ABy, ABz, CDx, CDy, CDz;
+    if constexpr (sizeof(R) == 4) {  // the pairs' FP32 copies: no conversion on the FP64 pipe
+        ABx = bra.ABf[0], ABy = bra.ABf[1], ABz = bra.ABf[2];
+        CDx = ket.ABf[0], CDy = ket.ABf[1], CDz = ket.ABf[2];
+    } else {
+        ABx = bra.AB[0], ABy = bra.AB[1], ABz = bra.AB[2];
+        CDx = ket.AB[0], CDy = ket.AB[1], CDz = ket.AB[2];
+    }
     const PP* pb = prims + bra.prim_begin;
     const PP* pk = prims + ket.prim_begin;
     const int nb = bra.nprim, nk = ket.nprim, sb = bra.prim_stride, sk = ket.prim_stride;
@@ -262,7 +316,7 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
             const PP kp = pk[ik * sk];
             const R rs = rsqrt(bp.p + kp.p);
             const R sr = R(SRTERM) * bp.E * kp.E * rs;
-            if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
+            if (!above_cut(sr, prim_cut)) continue;  // TwoElectronInts.cpp:478-479
             primitive(bp, kp, rs, sr);
         }
         return;
@@ -296,7 +350,7 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
                 // GPU is 1/64 of the FP32 one: a division and a square root cost twice as much)
                 rs = rsqrt(bp.p + kp.p);
                 sr = R(SRTERM) * bp.E * kp.E * rs;
-                if (above_cut(sr, (double)prim_cut)) {
+                if (above_cut(sr, prim_cut)) {
                     found = true;
                     break;
                 }
@@ -312,7 +366,7 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
                 const PP kp = pk[ik * sk];
                 const R rs = rsqrt(bp.p + kp.p);
                 const R sr = R(SRTERM) * bp.E * kp.E * rs;
-                if (!above_cut(sr, (double)prim_cut)) continue;  // TwoElectronInts.cpp:478-479
+                if (!above_cut(sr, prim_cut)) continue;  // TwoElectronInts.cpp:478-479
                 primitive(bp, kp, rs, sr);
             }
         }
@@ -423,7 +477,7 @@ __device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellP
     }
     float m = fmaxf(fmaxf(pm[a * n + b], pm[c * n + d]), fmaxf(pm[a * n + c], pm[a * n + d]));
     m = fmaxf(m, fmaxf(pm[b * n + c], pm[b * n + d]));
-    return (float)(bra.q * ket.q) * m < (float)A.skip_cut;
+    return bra.qf * ket.qf * m < A.skip_cut32;
 }
 
 // Density contraction of one shell quartet and scatter into T (G = T + T^T):
@@ -433,10 +487,15 @@ __device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellP
 // the sum over the 8 index permutations of every function quartet of the rectangle a x b x c x d
 // then counts every ordered (ij|kl) exactly once.  UHF (UHF = true): Ta collects J(Pa + Pb) - K(Pa)
 // and Tb collects J(Pa + Pb) - K(Pb) in the same T + T^T form (TwoElectronInts.cpp:749-820).
+struct NormTable {
+    double v[LMAX + 1][15];
+    float f[LMAX + 1][15];  // the same in FP32, for the FP32 kernels
+};
+
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& bra, const ShellPair& ket,
                                           bool same_pair, const R (&acc)[QClass<LA, LB, LC, LD>::NF],
-                                          const double (&nrm)[LMAX + 1][15]) {
+                                          const NormTable& nt) {
     // The density contraction runs in the kernel's own type R (FP32 in the FP32 kernels, on an FP32
     // copy of P); only the partial sums reach the FP64 accumulator T.  The degeneracy factor is applied
     // to those sums, and the storage cut compares magnitudes as integers (no FP64 compare).
@@ -464,6 +523,9 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
         Pb = UHF ? reinterpret_cast<const R*>(A.Pb32) + base : nullptr;
     }
     const R jf = UHF ? R(2) : R(4);
+    R thr;
+    if constexpr (sizeof(R) == 4) thr = A.thr_int32;
+    else thr = A.thr_int;
     R jcd[Q::NC * Q::ND];
     R kbc[Q::NB * Q::NC], kbd[Q::NB * Q::ND];
     R kbcB[UHF ? Q::NB * Q::NC : 1], kbdB[UHF ? Q::NB * Q::ND : 1];
@@ -495,8 +557,11 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
                     const int d = ket.b_off + id;
                     const int f = ((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id;
                     R v = acc[f];
-                    if constexpr (!UNIT_NORMS) v *= R(nrm[LA][ia] * nrm[LB][ib] * nrm[LC][ic] * nrm[LD][id]);
-                    if (!above_cut(v, A.thr_int)) continue;  // TwoElectronInts.cpp:668
+                    if constexpr (!UNIT_NORMS) {
+                        if constexpr (sizeof(R) == 4) v *= nt.f[LA][ia] * nt.f[LB][ib] * nt.f[LC][ic] * nt.f[LD][id];
+                        else v *= nt.v[LA][ia] * nt.v[LB][ib] * nt.v[LC][ic] * nt.v[LD][id];
+                    }
+                    if (!above_cut(v, thr)) continue;  // TwoElectronInts.cpp:668
                     R Pcd = __ldg(Pa + c * N + d);
                     if constexpr (UHF) Pcd += __ldg(Pb + c * N + d);
                     jab = fma(v, Pcd, jab);
@@ -513,21 +578,21 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
                     }
                 }
             }
-            const double j = double(jf * deg * jab);
+            const double j = to_f64(jf * deg * jab);
             atomicAdd(Ta +a * N + b, j);
             if constexpr (UHF) atomicAdd(Tb +a * N + b, j);
         }
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic) {
             const int c = ket.a_off + ic;
-            atomicAdd(Ta +a * N + c, double(-deg * kac[ic]));
-            if constexpr (UHF) atomicAdd(Tb +a * N + c, double(-deg * kacB[ic]));
+            atomicAdd(Ta +a * N + c, to_f64(-deg * kac[ic]));
+            if constexpr (UHF) atomicAdd(Tb +a * N + c, to_f64(-deg * kacB[ic]));
         }
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int d = ket.b_off + id;
-            atomicAdd(Ta +a * N + d, double(-deg * kad[id]));
-            if constexpr (UHF) atomicAdd(Tb +a * N + d, double(-deg * kadB[id]));
+            atomicAdd(Ta +a * N + d, to_f64(-deg * kad[id]));
+            if constexpr (UHF) atomicAdd(Tb +a * N + d, to_f64(-deg * kadB[id]));
         }
     }
 #pragma unroll
@@ -535,7 +600,7 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int c = ket.a_off + ic, d = ket.b_off + id;
-            const double j = double(jf * deg * jcd[ic * Q::ND + id]);
+            const double j = to_f64(jf * deg * jcd[ic * Q::ND + id]);
             atomicAdd(Ta +c * N + d, j);
             if constexpr (UHF) atomicAdd(Tb +c * N + d, j);
         }
@@ -545,21 +610,17 @@ __device__ __forceinline__ void digest_jk(const FockArgs& A, const ShellPair& br
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic) {
             const int c = ket.a_off + ic;
-            atomicAdd(Ta +b * N + c, double(-deg * kbc[ib * Q::NC + ic]));
-            if constexpr (UHF) atomicAdd(Tb +b * N + c, double(-deg * kbcB[ib * Q::NC + ic]));
+            atomicAdd(Ta +b * N + c, to_f64(-deg * kbc[ib * Q::NC + ic]));
+            if constexpr (UHF) atomicAdd(Tb +b * N + c, to_f64(-deg * kbcB[ib * Q::NC + ic]));
         }
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id) {
             const int d = ket.b_off + id;
-            atomicAdd(Ta +b * N + d, double(-deg * kbd[ib * Q::ND + id]));
-            if constexpr (UHF) atomicAdd(Tb +b * N + d, double(-deg * kbdB[ib * Q::ND + id]));
+            atomicAdd(Ta +b * N + d, to_f64(-deg * kbd[ib * Q::ND + id]));
+            if constexpr (UHF) atomicAdd(Tb +b * N + d, to_f64(-deg * kbdB[ib * Q::ND + id]));
         }
     }
 }
-
-struct NormTable {
-    double v[LMAX + 1][15];
-};
 
 // Optional work counter: primitive quartets past the prefactor cut, summed over the converged lanes of
 // the warp and added to one of 32 slots of the launch (spread to avoid a hot address).
@@ -584,9 +645,9 @@ __device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt
         shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.rys_compat != 0, acc,
                                                        A.counters ? &npass : nullptr);
     else
-        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, R(A.prim_cut), false, acc,
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, A.prim_cut32, false, acc,
                                                          A.counters ? &npass : nullptr);
-    digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt.v);
+    digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt);
     if (A.counters) count_flush(A, npass);
 }
 

@@ -61,7 +61,10 @@ __global__ void k_build_pairs(const ShellsDev sh, int npairs, const int* __restr
     sp.b_off = sh.soff[b];
     const double* A = sh.centers + 3 * sh.scen[a];
     const double* B = sh.centers + 3 * sh.scen[b];
-    for (int k = 0; k < 3; ++k) sp.AB[k] = __dsub_rn(A[k], B[k]);
+    for (int k = 0; k < 3; ++k) {
+        sp.AB[k] = __dsub_rn(A[k], B[k]);
+        sp.ABf[k] = (float)sp.AB[k];
+    }
     const double ab2 = __dadd_rn(__dadd_rn(__dmul_rn(sp.AB[0], sp.AB[0]), __dmul_rn(sp.AB[1], sp.AB[1])),
                                  __dmul_rn(sp.AB[2], sp.AB[2]));
     const int p0 = poff[c];
@@ -101,6 +104,7 @@ __global__ void k_build_pairs(const ShellsDev sh, int npairs, const int* __restr
     }
     sp.nprim = m - p0;
     sp.q = 0.0;
+    sp.qf = 0.f;
     out[c] = sp;
 }
 
@@ -109,7 +113,10 @@ __global__ void k_gather_pairs(const ShellPair* __restrict__ src, const int* __r
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     ShellPair sp = src[perm[t]];
-    if (q) sp.q = q[t];
+    if (q) {
+        sp.q = q[t];
+        sp.qf = (float)sp.q;
+    }
     dst[t] = sp;
 }
 
