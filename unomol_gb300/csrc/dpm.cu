@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(128) gdpm_kernel(const ShellPair* __restrict__
     ket.nprim = GDPM_N;
     ket.prim_stride = 1;
     double acc[Q::NF];
-    shell_quartet_eri<LA, LB, 0, 0, double, PrimPair>(bra, ket, prims, rys, 0.0, compat != 0, acc);
+    shell_quartet_eri<LA, LB, 0, 0, double, PrimPair>(bra, ket, prims, rys, 0.0, 0.f, compat != 0, acc);
 #pragma unroll
     for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
@@ -83,6 +83,7 @@ extern "C" int unomol_gpu_gdpm(UnomolCtx* ctx, const double* q, double* H) {
         for (int x = 0; x < 3; ++x) g.P[x] = q[x], g.PA[x] = 0.0;
         g.E = 1.0 / GDPM_ALF[k];  // exp(0) / a_k: the Gaussian is its own product, K_cd = 1
         g.cc = GDPM_COF[k];
+        g.Ecc = SQRT_SRTERM * g.E * g.cc;
         g.pf = (float)g.p;
         g.Ef = (float)g.E;
         gp[k] = g;

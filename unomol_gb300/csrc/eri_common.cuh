@@ -38,13 +38,18 @@ struct __align__(16) PrimPair {
     double E;          // exp(-alpha_a alpha_b |AB|^2 / p) / p, coefficient free (prefactor screen)
     double cc;         // c_a c_b, times 2 for the i != j half of a same-shell pair
                        // (TwoElectronInts.cpp:444-449)
+    double Ecc;        // sqrt(2 pi^{5/2}) E cc: a primitive quartet's prefactor is Ecc_ab Ecc_cd / sqrt(p + q)
     float pf, Ef;      // p and E in FP32, for a cheap pre-screen (96 bytes: six 16-byte loads)
 };
 
 struct __align__(16) PrimPair32 {
     float p, rp, P[3], PA[3], E, cc;
-    float pad_[2];  // 48 bytes: three 16-byte loads
+    float Ecc;      // sqrt(2 pi^{5/2}) E cc, as PrimPair::Ecc
+    float pad_;     // 48 bytes: three 16-byte loads
 };
+
+constexpr double SQRT_SRTERM = 5.914967172795613;  // sqrt(2 pi^{5/2})
+static_assert(SQRT_SRTERM * SQRT_SRTERM - SRTERM < 1e-13 && SRTERM - SQRT_SRTERM * SQRT_SRTERM < 1e-13, "sqrt of SRTERM");
 
 // One shell pair, sorted into blocks of equal (class, primitive-pair count), within a block by
 // descending Schwarz bound.

@@ -250,7 +250,7 @@ struct QClass {
 template <int LA, int LB, int LC, int LD, typename R, typename PP>
 __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const ShellPair& ket,
                                                   const PP* __restrict__ prims,
-                                                  const R* __restrict__ rys, R prim_cut, bool compat,
+                                                  const R* __restrict__ rys, R prim_cut, float prim_cut32, bool compat,
                                                   R (&acc)[QClass<LA, LB, LC, LD>::NF], unsigned* npass = nullptr,
                                                   int part = 0, int nparts = 1) {
     using Q = QClass<LA, LB, LC, LD>;
@@ -268,20 +268,24 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
     const PP* pb = prims + bra.prim_begin;
     const PP* pk = prims + ket.prim_begin;
     const int nb = bra.nprim, nk = ket.nprim, sb = bra.prim_stride, sk = ket.prim_stride;
-    // one surviving primitive quartet: bra record bp, ket record kp, rs = 1/sqrt(p+q), sr its prefactor
+    // one surviving primitive quartet: bra record bp, ket record kp, rs = 1/sqrt(p+q), and its prefactor
+    // with the contraction coefficients, sr = Ecc_ab Ecc_cd rs (TwoElectronInts.cpp:472-480)
     auto primitive = [&](const PP& bp, const PP& kp, R rs, R sr) {
-        const R p = bp.p, rp = bp.rp, cab = bp.cc;
+        const R p = bp.p, rp = bp.rp;
         const R Px = bp.P[0], Py = bp.P[1], Pz = bp.P[2];
         const R PAx = bp.PA[0], PAy = bp.PA[1], PAz = bp.PA[2];
-        const R q = kp.p, rq = kp.rp, ccd = kp.cc;
+        const R q = kp.p, rq = kp.rp;
         const R rpq = rs * rs;
-        sr *= cab * ccd;
         if (npass) ++*npass;
         const R QCx = kp.PA[0], QCy = kp.PA[1], QCz = kp.PA[2];
         const R PQx = Px - R(kp.P[0]), PQy = Py - R(kp.P[1]), PQz = Pz - R(kp.P[2]);
         const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
         R x[NR], w[NR];
         rys_roots<NR, R>(T, rys, x, w, compat);
+        if constexpr (LA + LB + LC + LD == 0) {  // (ss|ss): the integral is the weight times the prefactor
+            acc[0] = fma(w[0], sr, acc[0]);
+            return;
+        }
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
             const R fff = x[r] * rpq;  // t^2 / (p + q)   (Rys.hpp:126-129)
@@ -317,18 +321,19 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
             const R rs = rsqrt(bp.p + kp.p);
             const R sr = R(SRTERM) * bp.E * kp.E * rs;
             if (!above_cut(sr, prim_cut)) continue;  // TwoElectronInts.cpp:478-479
-            primitive(bp, kp, rs, sr);
+            primitive(bp, kp, rs, R(bp.Ecc) * R(kp.Ecc) * rs);
         }
         return;
     }
     if constexpr (sizeof(R) == 8) {
         // FP64: each lane walks its primitive quartets (bra-major, as the reference) and first looks
-        // ahead for the next one past the prefactor screen (TwoElectronInts.cpp:478-479), with an FP32
-        // pre-screen on float copies of p and E (quartets clearly below the cut cost no FP64 work; the
-        // others take the exact FP64 test, so the surviving set and the order of the sums are
-        // unchanged).  The warp then evaluates one surviving quartet per lane and round, so lanes whose
+        // ahead for the next one past the prefactor screen (TwoElectronInts.cpp:478-479).  The screen
+        // runs on float copies of p and E (within ~1e-6 of the FP64 value): quartets more than 0.1 %
+        // below the cut are dropped and quartets more than 0.1 % above it kept without FP64 work; the
+        // few in between take the exact FP64 test, so the surviving set is the one the FP64 test
+        // gives.  The warp then evaluates one surviving quartet per lane and round, so lanes whose
         // quartets were screened out do not sit idle through another lane's FP64 work.
-        const float prescreen = (float)prim_cut * 0.999f;
+        const float lo32 = prim_cut32 * 0.999f, hi32 = prim_cut32 * 1.001f;
         int ib = 0, ik = 0, cb = -1;
         PP bp = pb[0];
         for (;;) {
@@ -345,18 +350,17 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
                     ik = 0;
                     ++ib;
                 }
-                if (float(SRTERM) * bp.Ef * kp.Ef * rsqrtf(bp.pf + kp.pf) < prescreen) continue;
+                const float v32 = float(SRTERM) * bp.Ef * kp.Ef * rsqrtf(bp.pf + kp.pf);
+                if (v32 < lo32) continue;
                 // one reciprocal square root gives both 1/sqrt(p+q) and 1/(p+q) (the FP64 pipe of this
                 // GPU is 1/64 of the FP32 one: a division and a square root cost twice as much)
                 rs = rsqrt(bp.p + kp.p);
-                sr = R(SRTERM) * bp.E * kp.E * rs;
-                if (above_cut(sr, prim_cut)) {
-                    found = true;
-                    break;
-                }
+                if (v32 <= hi32 && !above_cut(R(SRTERM) * bp.E * kp.E * rs, prim_cut)) continue;
+                found = true;
+                break;
             }
             if (!found) break;
-            primitive(bp, kp, rs, sr);
+            primitive(bp, kp, rs, bp.Ecc * kp.Ecc * rs);
         }
     } else {
         // FP32 (bound by its loads, not by divergence): the plain nested loops
@@ -367,7 +371,7 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
                 const R rs = rsqrt(bp.p + kp.p);
                 const R sr = R(SRTERM) * bp.E * kp.E * rs;
                 if (!above_cut(sr, prim_cut)) continue;  // TwoElectronInts.cpp:478-479
-                primitive(bp, kp, rs, sr);
+                primitive(bp, kp, rs, R(bp.Ecc) * R(kp.Ecc) * rs);
             }
         }
     }
@@ -642,10 +646,10 @@ __device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt
     if (A.mode != 0 && quartet_screened(A, bra, ket)) return;
     R acc[Q::NF];
     if constexpr (sizeof(R) == 8)
-        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.rys_compat != 0, acc,
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.prim_cut32, A.rys_compat != 0, acc,
                                                        A.counters ? &npass : nullptr);
     else
-        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, A.prim_cut32, false, acc,
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, A.prim_cut32, A.prim_cut32, false, acc,
                                                          A.counters ? &npass : nullptr);
     digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt);
     if (A.counters) count_flush(A, npass);
@@ -703,7 +707,7 @@ __global__ void __launch_bounds__(128) schwarz_kernel(const ShellPair* __restric
     if (w >= count) return;  // whole warps: count is per warp
     const ShellPair sp = pairs[begin + w];
     double acc[Q::NF];
-    shell_quartet_eri<LA, LB, LA, LB, double, PrimPair>(sp, sp, prims, rys, 0.0, false, acc, nullptr, lane, 32);
+    shell_quartet_eri<LA, LB, LA, LB, double, PrimPair>(sp, sp, prims, rys, 0.0, 0.f, false, acc, nullptr, lane, 32);
     double m = 0.0;
 #pragma unroll
     for (int ia = 0; ia < Q::NA; ++ia)

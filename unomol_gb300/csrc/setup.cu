@@ -86,6 +86,7 @@ __global__ void k_build_pairs(const ShellsDev sh, int npairs, const int* __restr
             }
             pp.E = __dmul_rn(exp(__dmul_rn(__dmul_rn(__dmul_rn(-ai, bj), ab2), pp.rp)), pp.rp);
             pp.cc = __dmul_rn(__dmul_rn(ci, cj), f);
+            pp.Ecc = SQRT_SRTERM * pp.E * pp.cc;
             pp.pf = (float)pp.p;
             pp.Ef = (float)pp.E;
             prims[m] = pp;
@@ -98,7 +99,8 @@ __global__ void k_build_pairs(const ShellsDev sh, int npairs, const int* __restr
             }
             q.E = (float)pp.E;
             q.cc = (float)pp.cc;
-            q.pad_[0] = q.pad_[1] = 0.f;
+            q.Ecc = (float)pp.Ecc;
+            q.pad_ = 0.f;
             prims32[m] = q;
         }
     }
