@@ -362,7 +362,7 @@ def counted_flops(ctx, inputs, dev, stream):
     import torch
     ctx.set_counting(True)
     dG = None
-    f64, f32, launches, q32, q, fq, pq = [], [], [], [], [], [], []
+    f64, f32, launches, q32, q, fq, pq, scr = [], [], [], [], [], [], [], []
     for full, x in inputs:
         dx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
         if full or dG is None:
@@ -377,8 +377,9 @@ def counted_flops(ctx, inputs, dev, stream):
         q32.append(st["shell_quartets_fp32"])
         fq.append(st["function_quartets_computed"])
         pq.append(st["primitive_quartets_computed"])
+        scr.append(st["shell_quartets_screened"])
     ctx.set_counting(False)
-    return f64, f32, launches, q, q32, fq, pq
+    return f64, f32, launches, q, q32, fq, pq, scr
 
 
 def run_ours(args):
@@ -434,7 +435,7 @@ def run_ours(args):
     clocks = Clocks(local)
     # warm-up, then the counted (untimed) pass for the algorithmic flops
     timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
-    f64, f32, launches, nq, nq32, nfq, npq = counted_flops(mixed, inputs, dev, stream)
+    f64, f32, launches, nq, nq32, nfq, npq, nscr = counted_flops(mixed, inputs, dev, stream)
     # timed region
     replicas.barrier(ws)
     torch.cuda.synchronize(dev)
@@ -510,7 +511,8 @@ def run_ours(args):
                        "rys_mode": "reference-compatible", "schwarz_cutoff": 1e-14,
                        "l2": "flushed: 256 MiB write before every timed build", "nbf": b.norb,
                        "builds_in_sequence": len(inputs), "parallelism": f"replicas x{ws}",
-                       "shell_quartets_per_build": [int(x) for x in nq], "fp32_shell_quartets_per_build": [int(x) for x in nq32]},
+                       "shell_quartets_per_build": [int(x) for x in nq], "fp32_shell_quartets_per_build": [int(x) for x in nq32],
+                       "screened_shell_quartets_per_build": [int(x) for x in nscr]},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * b.no2, "d2h_bytes_per_step": 8 * b.no2},
             "roofline": {"bound": "fp64+fp32 pipes", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": profile_traffic(args.form),

@@ -79,7 +79,11 @@ typedef struct UnomolStats {
                                       quartet its density contraction, counted from the kernels' steps */
     double eri_flops_fp32;         /* of which in the FP32 kernels (mixed mode) */
     int64_t function_quartets_computed; /* function quartets of the last build's work lists (in the
-                                           density-screened and mixed builds: its FP64 and FP32 parts) */
+                                           density-screened and mixed builds: its FP64 and FP32 parts,
+                                           without the quartets the per-quartet density screen drops) */
+    int64_t shell_quartets_screened;    /* density-screened and mixed builds: quartets of the work lists
+                                           dropped by the per-quartet density screen (max |P| of the six
+                                           blocks a quartet contracts with, times its bound) */
 } UnomolStats;
 
 /* TwoElectronInts(basis, start_shell, label) -- TwoElectronInts.hpp:83-88.
@@ -108,9 +112,10 @@ int unomol_gpu_fock_uhf_device(UnomolCtx* ctx, const double* dPa, const double* 
  * UNOMOL_PREC_FP64 (default): every quartet that passes the integral Schwarz cut, in FP64.
  * UNOMOL_PREC_MIXED: density-screened build made per call on the device.  With b = sqrt((ab|ab))
  *   sqrt((cd|cd)) and D = max |P| over the density passed in: quartets with b*D >= fp32_cutoff run in
- *   FP64, quartets with skip_cut <= b*D < fp32_cutoff in FP32 (Rys fits, recurrences and contraction in
- *   FP32; density contraction and the Fock accumulation in FP64), the rest (and quartets whose six
- *   density blocks are all small) are skipped.  Meant for incremental builds G(P) = G(P_old) + G(dP),
+ *   FP64, quartets with skip_cut <= b*D < fp32_cutoff in FP32 (Rys roots, recurrences, contraction and
+ *   the density contraction of each quartet in FP32; its J/K sums added into G in FP64), the rest (and
+ *   quartets whose six density blocks are all small) are skipped.  Meant for incremental builds
+ *   G(P) = G(P_old) + G(dP),
  *   where |dP| shrinks as the SCF converges.  fp32_cutoff <= skip_cut gives a density-screened FP64
  *   build. */
 int unomol_gpu_set_precision(UnomolCtx* ctx, int mode, double fp32_cutoff);

@@ -324,11 +324,17 @@ int build_worklists(UnomolCtx* ctx) {
         screened += tot[k];
         fq += tot[k] * nfq;
         prim_q += tot[k] * (int64_t)ctx->block_nprim[X] * ctx->block_nprim[Y];
+        bp.prim_quartets = ctx->block_nprim[X] * ctx->block_nprim[Y];
         per_class[bc * NPAIRCLASS + kc].push_back(bp);
     }
     for (int cls = 0; cls < NPAIRCLASS * NPAIRCLASS; ++cls) {
         auto& v = per_class[cls];
         if (v.empty()) continue;
+        // the costliest quartets first: a launch's CTAs start in grid order, so the block pairs whose
+        // quartets carry the most primitive quartets (up to 36 x 36) no longer end the launch on a few
+        // SMs while the rest are idle
+        std::stable_sort(v.begin(), v.end(),
+                         [](const BlockPair& x, const BlockPair& y) { return x.prim_quartets > y.prim_quartets; });
         ClassLaunch L{};
         L.bc = cls / NPAIRCLASS;
         L.kc = cls % NPAIRCLASS;
@@ -661,8 +667,9 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     const int ncls = NPAIRCLASS * NPAIRCLASS;
     A.counters = nullptr;
     if (ctx->counting) {
-        if (!ctx->d_counters) CU(cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 2 * ncls * 32));
-        CU(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 2 * ncls * 32, s));
+        // per class and part, 32 slots each: primitive quartets (FP64, FP32), screened quartets (FP64, FP32)
+        if (!ctx->d_counters) CU(cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 4 * ncls * 32));
+        CU(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4 * ncls * 32, s));
         A.counters = ctx->d_counters;
     }
     // one class: the reference's integral method (Rys for la+lb+lc+ld <= 8, MD above:
@@ -746,7 +753,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     CU(cudaGetLastError());
     ctx->stats.kernel_launches = launches;
     if (ctx->counting) {
-        std::vector<unsigned long long> c(2 * ncls * 32);
+        std::vector<unsigned long long> c(4 * ncls * 32);
         CU(cudaMemcpyAsync(c.data(), ctx->d_counters, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
         // shell quartets of this build per block pair: in the density-screened and mixed builds the
@@ -762,7 +769,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             if (has32)
                 CU(cudaMemcpy(q32.data(), ctx->d_cnt32, sizeof(long long) * q32.size(), cudaMemcpyDeviceToHost));
         }
-        int64_t prims = 0, s64 = 0, s32 = 0, fq_done = 0;
+        int64_t prims = 0, s64 = 0, s32 = 0, fq_done = 0, screened = 0;
         double fl = 0.0, fl32 = 0.0;
         for (const ClassLaunch& L : ctx->launches) {
             const int cls = L.bc * NPAIRCLASS + L.kc;
@@ -784,6 +791,15 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                     n64 += q64[k];
                     n32 += q32[k];
                 }
+                // quartets the per-quartet density screen dropped do no quartet-level work
+                long long d64 = 0, d32 = 0;
+                for (int k = 0; k < 32; ++k) {
+                    d64 += (long long)c[(2 * ncls + cls) * 32 + k];
+                    d32 += (long long)c[(3 * ncls + cls) * 32 + k];
+                }
+                n64 -= d64;
+                n32 -= d32;
+                screened += d64 + d32;
             }
             fl += (double)n64 * flops_per_quartet(la, lb, lc, ld);
             fl32 += (double)n32 * flops_per_quartet(la, lb, lc, ld);
@@ -799,6 +815,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             ctx->stats.shell_quartets = s64 + s32;
             ctx->stats.shell_quartets_fp32 = s32;
         }
+        ctx->stats.shell_quartets_screened = screened;
     }
     return UNOMOL_OK;
 }

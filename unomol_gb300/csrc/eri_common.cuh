@@ -76,6 +76,7 @@ struct BlockPair {
     int ket_begin, ket_count;   // pair index range of the ket block
     int triangle;               // bra block == ket block: ket index <= bra index
     int prefix_off;             // offset of this block pair's prefix array (bra_count + 1 entries)
+    int prim_quartets;          // primitive quartets of each of its shell quartets (nprim bra x nprim ket)
     long long work_begin;       // first work item (multiple of 32, so warps never straddle)
     long long work_count;       // quartets in this block pair
 };

@@ -434,6 +434,10 @@ int unomol_gpu_batch_create(const UnomolBasisDesc* bases, int nmol, UnomolBatch*
     for (int cls = 0; cls < NTMPLCLASS * NTMPLCLASS; ++cls) {
         auto& v = per_class[cls];
         if (v.empty()) continue;
+        // the costliest quartets of all molecules first (as for one context: no long tail of
+        // many-primitive quartets at the end of a launch)
+        std::stable_sort(v.begin(), v.end(),
+                         [](const BlockPair& x, const BlockPair& y) { return x.prim_quartets > y.prim_quartets; });
         BLaunch L;
         L.bc = cls / NTMPLCLASS;
         L.kc = cls % NTMPLCLASS;

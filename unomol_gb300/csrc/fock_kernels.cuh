@@ -635,6 +635,16 @@ __device__ __forceinline__ void count_flush(const FockArgs& A, unsigned v) {
         atomicAdd(A.counters + A.counter_base + (blockIdx.x & 31), (unsigned long long)s);
 }
 
+// Counting mode: quartets of this build's work lists dropped by the per-quartet density screen, per
+// warp into one of 32 slots of the launch's class (the third and fourth quarters of the counter array:
+// FP64 part, then FP32 part).
+__device__ __forceinline__ void count_screened(const FockArgs& A) {
+    const unsigned m = __activemask();
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1)
+        atomicAdd(A.counters + 2 * NPAIRCLASS * NPAIRCLASS * 32 + A.counter_base + (blockIdx.x & 31),
+                  (unsigned long long)__popc(m));
+}
+
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt, const R* __restrict__ rys, long long g) {
     using Q = QClass<LA, LB, LC, LD>;
@@ -643,7 +653,10 @@ __device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt
     if (!(A.mode == 0 ? decode_work_warp<false>(A, g, bi, ki) : decode_work_warp<true>(A, g, bi, ki))) return;
     const ShellPair bra = A.pairs[bi];
     const ShellPair ket = A.pairs[ki];
-    if (A.mode != 0 && quartet_screened(A, bra, ket)) return;
+    if (A.mode != 0 && quartet_screened(A, bra, ket)) {
+        if (A.counters) count_screened(A);
+        return;
+    }
     R acc[Q::NF];
     if constexpr (sizeof(R) == 8)
         shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.prim_cut32, A.rys_compat != 0, acc,
