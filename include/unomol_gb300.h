@@ -324,7 +324,7 @@ int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* input, const UnomolScfOptio
  * inputs: [nmol] (S, H packed, nelec even); options: maxits, eps, conv_type, accel (UNOMOL_SCF_DIIS:
  * the DIIS update and test of unomol_scf; otherwise the reference's damping and is_converged),
  * guess (core Hamiltonian, or UNOMOL_GUESS_GIVEN: the densities in P_io), loop (ground-state or DPM
- * loop order), diis_size, diis_tol.  P_io: the batch's packed densities (in: the guess when given;
+ * loop order), diis_size, diis_tol, incremental and rebuild_every.  P_io: the batch's packed densities (in: the guess when given;
  * out: the final densities; may be NULL with the core-Hamiltonian guess). */
 typedef struct UnomolBatchScfResult {
     double energy, e_electronic, diis_error;
@@ -335,6 +335,12 @@ typedef struct UnomolBatchScfResult {
 int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* inputs, int nmol, const UnomolScfOptions* options,
                          int graph, UnomolBatchScfResult* results, double* P_io, double* seconds, int* graph_used);
 const char* unomol_gpu_batch_scf_last_error(void);
+/* Fock builds of the last batched SCF on this thread: their device time (CUDA events around each
+ * iteration's build, also inside a replayed graph) and their number.  With options->incremental the
+ * batched SCF builds G(P - P_prev) added to the G it keeps, a full build every options->rebuild_every
+ * (the single-molecule scheme; the build count is kept on the device), so that in the precision form
+ * the density bound of each build shrinks as the molecules converge. */
+int unomol_gpu_batch_scf_last_builds(double* fock_ms, int* builds);
 
 /* ---- Learned initial density (no reference counterpart; the reference starts from the core
  * Hamiltonian, RHF.hpp:205-211, or reads PMATRIX.DAT, RHF.hpp:120-123) ----

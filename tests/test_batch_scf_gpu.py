@@ -42,3 +42,30 @@ def test_batched_scf_iteration_is_one_cuda_graph(gpu):
     r = bat.scf(graph=True)
     assert r["graph_used"], r["capture_note"]
     assert r["converged"].all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [True, False])
+def test_batched_scf_incremental_builds(gpu, graph):
+    """Incremental builds in the batched SCF (G(P_prev) + G(P - P_prev), a full build every 8): in FP64
+    the energies are those of full builds within 1e-9 Eh; in the precision form (FP32 cutoff 1e-3,
+    density skip 1e-13) within the form's 1e-6 Eh bar, at the same iteration counts to within one.  The
+    build timings come back (unomol_gpu_batch_scf_last_builds), also from a replayed graph."""
+    from unomol_gb300 import native
+    bases = _batch_molecules()
+    SH = [native.one_electron_gpu(b) for b in bases]
+    S, H = [x[0] for x in SH], [x[1] for x in SH]
+    bat = native.Batch(bases)
+    full = bat.scf(S=S, H=H, eps=1e-10, diis_tol=1e-7, graph=graph)
+    inc = bat.scf(S=S, H=H, eps=1e-10, diis_tol=1e-7, graph=graph, incremental=True)
+    assert full["converged"].all() and inc["converged"].all()
+    assert np.abs(inc["energy"] - full["energy"]).max() < 1e-9
+    assert abs(inc["builds"] - int(inc["iterations"].max())) <= 1 and inc["fock_ms"] > 0.0
+    if graph:
+        assert inc["graph_used"], inc["capture_note"]
+    bat.set_precision(native.PREC_MIXED, 1e-3, 1e-13)
+    mix = bat.scf(S=S, H=H, eps=1e-10, diis_tol=1e-7, graph=graph, incremental=True)
+    assert mix["converged"].all()
+    assert np.abs(mix["energy"] - full["energy"]).max() < 1e-6
+    assert np.abs(mix["iterations"] - full["iterations"]).max() <= 1
+    bat.close()

@@ -48,6 +48,13 @@ struct BState {
     double *B = nullptr, *coef = nullptr;  // [nmol][maxv][maxv], [nmol][maxv]
     double *Enew = nullptr, *Eold = nullptr, *err = nullptr, *dE = nullptr, *pdiff = nullptr, *Einit = nullptr;  // [nmol]
     double* Pold = nullptr;               // packed, batch order: the density before the last update's diagonalisation
+    // incremental builds: the density of the last build, the G kept, the build count (device)
+    double *Pprev = nullptr, *Gacc = nullptr;
+    int* step = nullptr;
+    long long ptot = 0;
+    cudaEvent_t eb[2] = {nullptr, nullptr};  // around every iteration's Fock build
+    double fock_ms = 0.0;
+    int builds = 0;
     int *nupd = nullptr, *conv = nullptr, *its = nullptr, *info = nullptr, *bad = nullptr;
     // grouped-GEMM pointer arrays (device) per product
     const double** pa[8] = {};
@@ -65,8 +72,11 @@ struct BState {
     std::string err_msg, capture_error;
     ~BState() {
         for (void* p : std::vector<void*>{d_mols, S, X, H, F, Fo, T1, T2, Pf, Ecur, W, Hpk, Fh, Eh, B, coef, Enew, Eold,
-                                          err, dE, pdiff, Einit, Pold, nupd, conv, its, info, bad, dwork, cublas_ws})
+                                          err, dE, pdiff, Einit, Pold, nupd, conv, its, info, bad, dwork, cublas_ws,
+                                          Pprev, Gacc, step})
             if (p) cudaFree(p);
+        for (cudaEvent_t e : eb)
+            if (e) cudaEventDestroy(e);
         for (int k = 0; k < 8; ++k) {
             if (pa[k]) cudaFree(pa[k]);
             if (pb[k]) cudaFree(pb[k]);
@@ -347,6 +357,32 @@ __global__ void k_converge(int nmol, const double* __restrict__ Enew, double* __
 
 unsigned blocks(long long n) { return (unsigned)((n + 255) / 256); }
 
+// Incremental builds (UnomolScfOptions.incremental), as the single-molecule SCF does them: G is linear in
+// P, so a build of P - P_prev added to the G kept gives G(P); every rebuild-th build is a full one.
+// The build count lives on the device, so that one captured iteration serves every build.
+// Before the build: the batch's density buffer takes the change (a full build keeps P); P_prev takes P.
+__global__ void k_inc_pre(long long n, double* __restrict__ P, double* __restrict__ Pprev, const int* __restrict__ step,
+                          int rebuild) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double p = P[i];
+    if (*step % rebuild != 0) P[i] = p - Pprev[i];
+    Pprev[i] = p;
+}
+
+// After the build: G kept plus this build's G (a full build replaces it), the density restored.
+__global__ void k_inc_post(long long n, double* __restrict__ P, const double* __restrict__ Pprev, double* __restrict__ G,
+                           double* __restrict__ Gacc, const int* __restrict__ step, int rebuild) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double g = *step % rebuild == 0 ? G[i] : Gacc[i] + G[i];
+    Gacc[i] = g;
+    G[i] = g;
+    P[i] = Pprev[i];
+}
+
+__global__ void k_inc_step(int* step) { ++*step; }
+
 // grouped GEMM C = op(A) op(B) for every molecule; pointer arrays were filled once for product `id`
 int gemm(BState& st, int id, cublasOperation_t ta, cublasOperation_t tb, bool k_occ) {
     const int ng = (int)st.gn.size();
@@ -431,15 +467,27 @@ int density_from_F(BState& st, double* dP, cudaStream_t s) {
 struct BOpts {
     int accel, cflag, first_check;
     double eps, tol;
+    int incremental, rebuild;
 };
 
 // one SCF update of every active molecule (the part that is captured as a graph)
 int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, const BOpts& o, cudaStream_t s) {
     if (o.accel != 2) k_damp<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.nupd, st.dE, o.first_check - 1, st.Pold, dP);
+    if (o.incremental) k_inc_pre<<<blocks(st.ptot), 256, 0, s>>>(st.ptot, dP, st.Pprev, st.step, o.rebuild);
+    // in a captured iteration the records are external event nodes, timed after every replay
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    BK(cudaStreamIsCapturing(s, &cap), UNOMOL_ECUDA);
+    const unsigned evf = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    BK(cudaEventRecordWithFlags(st.eb[0], s, evf), UNOMOL_ECUDA);
     int rc = unomol_gpu_batch_fock(batch, UNOMOL_BATCH_LAUNCHES, s);
     if (rc) {
         st.err_msg = unomol_gpu_batch_last_error(batch);
         return rc;
+    }
+    BK(cudaEventRecordWithFlags(st.eb[1], s, evf), UNOMOL_ECUDA);
+    if (o.incremental) {
+        k_inc_post<<<blocks(st.ptot), 256, 0, s>>>(st.ptot, dP, st.Pprev, dG, st.Gacc, st.step, o.rebuild);
+        k_inc_step<<<1, 1, 0, s>>>(st.step);
     }
     k_fock<<<st.nmol, 256, 0, s>>>(st.d_mols, st.Hpk, dG, dP, st.F, st.Enew);
     BK(cudaGetLastError(), UNOMOL_ECUDA);
@@ -531,6 +579,14 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     BK(cudaMalloc(&st.coef, sizeof(double) * nmol * st.maxv), UNOMOL_ENOMEM);
     for (double** p : {&st.Enew, &st.Eold, &st.err, &st.dE, &st.pdiff, &st.Einit}) BK(cudaMalloc(p, sizeof(double) * nmol), UNOMOL_ENOMEM);
     BK(cudaMalloc(&st.Pold, sizeof(double) * ptot), UNOMOL_ENOMEM);
+    st.ptot = ptot;
+    if (opt->incremental) {
+        BK(cudaMalloc(&st.Pprev, sizeof(double) * ptot), UNOMOL_ENOMEM);
+        BK(cudaMalloc(&st.Gacc, sizeof(double) * ptot), UNOMOL_ENOMEM);
+        BK(cudaMalloc(&st.step, sizeof(int)), UNOMOL_ENOMEM);
+        BK(cudaMemset(st.step, 0, sizeof(int)), UNOMOL_ECUDA);
+    }
+    for (cudaEvent_t& e : st.eb) BK(cudaEventCreate(&e), UNOMOL_ECUDA);
     BK(cudaMemset(st.dE, 0, sizeof(double) * nmol), UNOMOL_ECUDA);
     BK(cudaMemset(st.pdiff, 0, sizeof(double) * nmol), UNOMOL_ECUDA);
     for (int** p : {&st.nupd, &st.conv, &st.its, &st.info, &st.bad}) BK(cudaMalloc(p, sizeof(int) * nmol), UNOMOL_ENOMEM);
@@ -622,7 +678,7 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     }
     const int maxits = opt->maxits > 0 ? opt->maxits : 300;
     const BOpts o{opt->accel == UNOMOL_SCF_DIIS ? 2 : 0, opt->conv_type, opt->loop == UNOMOL_SCF_LOOP_DPM ? 2 : 3, opt->eps,
-                  opt->diis_tol};
+                  opt->diis_tol, opt->incremental ? 1 : 0, opt->rebuild_every > 0 ? opt->rebuild_every : 8};
     cudaGraphExec_t exec = nullptr;
     int used_graph = 0;
     if (graph) {
@@ -648,6 +704,9 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         else if ((rc = iteration(st, batch, dP, dG, o, s))) return fail(rc);
         BK(cudaMemcpyAsync(conv.data(), st.conv, sizeof(int) * nmol, cudaMemcpyDeviceToHost, s), UNOMOL_ECUDA);
         BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, st.eb[0], st.eb[1]) == cudaSuccess) st.fock_ms += ms;
+        ++st.builds;
         if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; })) break;
     }
     if (exec) cudaGraphExecDestroy(exec);
@@ -682,6 +741,9 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
 
 }  // namespace
 
+thread_local double g_bscf_fock_ms = 0.0;
+thread_local int g_bscf_builds = 0;
+
 extern "C" int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* in, int nmol, const UnomolScfOptions* opt,
                                     int graph, UnomolBatchScfResult* res, double* P_out, double* seconds, int* graph_used) {
     if (!batch || !in || !opt || !res || nmol <= 0) return UNOMOL_EINVAL;
@@ -692,9 +754,18 @@ extern "C" int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* in
         BState st;
         rc = batch_scf(st, batch, in, nmol, opt, graph, res, P_out, graph_used);
         g_bscf_err = rc ? st.err_msg : st.capture_error;
+        g_bscf_fock_ms = st.fock_ms;
+        g_bscf_builds = st.builds;
     }
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;
 }
 
 extern "C" const char* unomol_gpu_batch_scf_last_error(void) { return g_bscf_err.c_str(); }
+
+extern "C" int unomol_gpu_batch_scf_last_builds(double* fock_ms, int* builds) {
+    if (!fock_ms || !builds) return UNOMOL_EINVAL;
+    *fock_ms = g_bscf_fock_ms;
+    *builds = g_bscf_builds;
+    return UNOMOL_OK;
+}

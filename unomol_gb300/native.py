@@ -35,7 +35,7 @@ EXPORTS = [
     "unomol_gpu_one_electron", "unomol_gpu_one_electron_last_error", "unomol_gpu_l2_peak", "unomol_gpu_batch_scf",
     "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
     "unomol_gpu_moment_ints", "unomol_gpu_batch_set_precision", "unomol_gpu_batch_fock_device",
-    "unomol_tc_set_wait_polls", "unomol_gpu_set_launch_order",
+    "unomol_tc_set_wait_polls", "unomol_gpu_set_launch_order", "unomol_gpu_batch_scf_last_builds",
 ]
 RYS_REFERENCE = 0
 RYS_EXACT = 1
@@ -460,7 +460,7 @@ class Batch:
 
     def scf(self, S=None, H=None, eps: float = 1e-10, diis_tol: float = 1e-6, maxits: int = 200,
             diis_size: int = 8, graph: bool = True, accel: int = SCF_DIIS, conv_type: int = 0, guess_P=None,
-            loop: int = SCF_LOOP_GROUND):
+            loop: int = SCF_LOOP_GROUND, incremental: bool = False, rebuild_every: int = 8):
         """RHF SCF of every molecule at once (unomol_gpu_batch_scf).  S, H: lists of packed matrices
         (default: the GPU one-electron integrals of each basis); guess_P: list of packed starting
         densities (default: core Hamiltonian); accel / conv_type / loop as for scf().  Returns a dict
@@ -480,7 +480,7 @@ class Batch:
         inp = (ScfInput * n)(*[ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), s.ctypes.data_as(dp), h.ctypes.data_as(dp))
                                for b, s, h in zip(self.bases, S, H)])
         opt = ScfOptions(maxits, eps, conv_type, accel, GUESS_CORE if guess_P is None else GUESS_GIVEN, diis_size,
-                         diis_tol, 0.0, 0.0, 0.0, 0, 8, loop)
+                         diis_tol, 0.0, 0.0, 0.0, 1 if incremental else 0, rebuild_every, loop)
         res = (BatchScfResult * n)()
         P = np.zeros(self.total)
         if guess_P is not None:
@@ -490,7 +490,10 @@ class Batch:
         note = L.unomol_gpu_batch_scf_last_error().decode(errors="replace")
         if rc != 0:
             raise UnomolError(f"unomol_gpu_batch_scf error {rc}: {note}")
-        return {"energy": np.array([r.energy for r in res]), "iterations": np.array([r.iterations for r in res]),
+        L.unomol_gpu_batch_scf_last_builds.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        fms, nb = C.c_double(), C.c_int()
+        L.unomol_gpu_batch_scf_last_builds(C.byref(fms), C.byref(nb))
+        return {"fock_ms": fms.value, "builds": nb.value,"energy": np.array([r.energy for r in res]), "iterations": np.array([r.iterations for r in res]),
                 "init_energy": np.array([r.init_energy for r in res]), "ediff": np.array([r.ediff for r in res]),
                 "pdiff": np.array([r.pdiff for r in res]),
                 "converged": np.array([bool(r.converged) for r in res]),
