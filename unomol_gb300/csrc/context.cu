@@ -868,9 +868,9 @@ namespace {
 // The Rys tables of every context on one device: file-scope device arrays of the library's image,
 // filled once per device (rows re-laid with the padded strides of the kernels, zeros in the padding:
 // 16-byte loads), then the large-T limits.
-constexpr int RYS64_LEN = rys_table_len(RysStride<double>::value);
-constexpr int RYS32_LEN = rys_table_len(RysStride<float>::value);
-static __device__ __align__(16) double g_rys64[RYS64_LEN];
+constexpr int RYS64_LEN = rys_table_len(RysStride<double>::value, RYS_H);
+constexpr int RYS32_LEN = rys_table_len(RysStride<float>::value, RYS32_H);
+static __device__ __align__(32) double g_rys64[RYS64_LEN];  // 64-byte rows: two 256-bit loads each
 static __device__ __align__(32) float g_rys32[RYS32_LEN];  // 32-byte rows: one 256-bit load each
 constexpr int RYS_MAX_DEVICES = 64;
 double* g_rys64_ptr[RYS_MAX_DEVICES] = {nullptr};
@@ -878,8 +878,8 @@ float* g_rys32_ptr[RYS_MAX_DEVICES] = {nullptr};
 std::mutex g_rys_mu;
 
 int rys_tables(int dev, double*& d64, float*& d32, std::string& err) {
-    static_assert(rys_table_len(RYS_DEG + 1) == RYS_TABLE_SIZE + 50, "layout of rys_tables.inc");
-    static_assert(rys_table_len(RYS32_DEG + 1) == RYS32_TABLE_SIZE + 50, "layout of rys_tables.inc");
+    static_assert(rys_table_len(RYS_DEG + 1, RYS_H) == RYS_TABLE_SIZE + 50, "layout of rys_tables.inc");
+    static_assert(rys_table_len(RYS32_DEG + 1, RYS32_H) == RYS32_TABLE_SIZE + 50, "layout of rys_tables.inc");
     if (dev < 0 || dev >= RYS_MAX_DEVICES) {
         err = "device index out of range";
         return UNOMOL_EINVAL;
@@ -889,11 +889,11 @@ int rys_tables(int dev, double*& d64, float*& d32, std::string& err) {
         constexpr int S64 = RysStride<double>::value, S32 = RysStride<float>::value;
         std::vector<double> t64(RYS64_LEN, 0.0);
         std::vector<float> t32(RYS32_LEN, 0.f);
-        const int rows = RYS_TABLE_SIZE / (RYS_DEG + 1);
-        for (int r = 0; r < rows; ++r) {
+        const int rows64 = RYS_TABLE_SIZE / (RYS_DEG + 1), rows32 = RYS32_TABLE_SIZE / (RYS32_DEG + 1);
+        for (int r = 0; r < rows64; ++r)
             for (int d = 0; d <= RYS_DEG; ++d) t64[(size_t)r * S64 + d] = RYS_TABLE_H[(size_t)r * (RYS_DEG + 1) + d];
+        for (int r = 0; r < rows32; ++r)
             for (int d = 0; d <= RYS32_DEG; ++d) t32[(size_t)r * S32 + d] = RYS32_TABLE_H[(size_t)r * (RYS32_DEG + 1) + d];
-        }
         const size_t h64 = t64.size() - 50, h32 = t32.size() - 50;
         for (int n = 0; n < 5; ++n)
             for (int i = 0; i < 5; ++i) {

@@ -23,28 +23,30 @@ template <> struct RysDeg<float> { static constexpr int value = RYS32_DEG; };
 template <typename R> struct RysStride;
 template <> struct RysStride<double> { static constexpr int value = (RYS_DEG + 2) / 2 * 2; };
 template <> struct RysStride<float> { static constexpr int value = (RYS32_DEG + 4) / 4 * 4; };
+// Interval width in T of each precision's table (a power of two: T / H is exact).
+template <typename R> struct RysH;
+template <> struct RysH<double> { static constexpr double value = RYS_H; };
+template <> struct RysH<float> { static constexpr double value = RYS32_H; };
 
 __host__ __device__ constexpr double rys_tmax(int n) {
     return n == 1 ? RYS_TMAX_1 : n == 2 ? RYS_TMAX_2 : n == 3 ? RYS_TMAX_3 : n == 4 ? RYS_TMAX_4 : RYS_TMAX_5;
 }
-// Offset of the n-root block in a table whose polynomial rows hold `stride` coefficients (rys_tables.inc
-// with stride = degree + 1; the device tables with the padded strides of RysStride).
-__host__ __device__ constexpr int rys_off(int n, int stride) {
+// Offset of the n-root block in a table of interval width h whose polynomial rows hold `stride`
+// coefficients (rys_tables.inc with stride = degree + 1; the device tables with the padded strides of
+// RysStride).
+__host__ __device__ constexpr int rys_off(int n, int stride, double h) {
     int o = 0;
-    for (int m = 1; m < n; ++m) o += int(rys_tmax(m) / RYS_H) * 2 * m * stride;
+    for (int m = 1; m < n; ++m) o += int(rys_tmax(m) / h) * 2 * m * stride;
     return o;
 }
 // Size of a device table: polynomial blocks, then hermite x[5][5] and w[5][5].
-__host__ __device__ constexpr int rys_table_len(int stride) { return rys_off(RYS_NMAX + 1, stride) + 50; }
+__host__ __device__ constexpr int rys_table_len(int stride, double h) { return rys_off(RYS_NMAX + 1, stride, h) + 50; }
 
-// one polynomial row (16-byte aligned) into registers with 16-byte loads
+// one FP64 polynomial row (8 doubles, 64 bytes, 32-byte aligned) into registers with two 256-bit loads
+static_assert(RysStride<double>::value == 8, "two 256-bit loads per FP64 row");
 __device__ __forceinline__ void load_row(const double* __restrict__ c, double (&v)[RysStride<double>::value]) {
-#pragma unroll
-    for (int q = 0; q < RysStride<double>::value / 2; ++q) {
-        const double2 t = __ldg(reinterpret_cast<const double2*>(c) + q);
-        v[2 * q] = t.x;
-        v[2 * q + 1] = t.y;
-    }
+    asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(c));
+    asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(v[4]), "=d"(v[5]), "=d"(v[6]), "=d"(v[7]) : "l"(c + 4));
 }
 // FP32 rows are 8 floats (32 bytes, 32-byte aligned): one 256-bit load, half the load instructions of
 // two 16-byte loads (the FP32 kernels are bound by the L1 wavefronts of these per-lane rows)
@@ -146,11 +148,11 @@ __device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, 
         }
     }
     if (T < TMAX) {
-        const R Ts = T * R(1.0 / RYS_H);  // intervals of width RYS_H (a power of two: exact)
+        const R Ts = T * R(1.0 / RysH<R>::value);  // intervals of width H (a power of two: exact)
         const int k = (int)Ts;
         const R y = R(2) * (Ts - R(k)) - R(1);
         constexpr int ST = RysStride<R>::value;
-        const R* c = tab + rys_off(NR, ST) + k * (2 * NR * ST);
+        const R* c = tab + rys_off(NR, ST, RysH<R>::value) + k * (2 * NR * ST);
 #pragma unroll
         for (int i = 0; i < NR; ++i) {
             R cx[ST], cw[ST];
@@ -166,7 +168,7 @@ __device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, 
             w[i] = vw;
         }
     } else {  // large-T limit (also taken by a NaN T, which keeps the table index in range)
-        const R* herm = tab + rys_table_len(RysStride<R>::value) - 50;
+        const R* herm = tab + rys_table_len(RysStride<R>::value, RysH<R>::value) - 50;
         R rT = R(1) / T;
         R s = sqrt(rT);
 #pragma unroll

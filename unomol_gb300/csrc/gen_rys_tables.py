@@ -11,7 +11,8 @@ not matter):
      (W. Gautschi, "Orthogonal Polynomials: Computation and Approximation", 2004, sec. 2.1.7);
   3. nodes and weights from the eigen-decomposition of the Jacobi matrix (Golub & Welsch, 1969).
 
-On [0, TMAX) the nodes x_i(T) and weights w_i(T) are fitted interval by interval (width H) with
+On [0, TMAX) the nodes x_i(T) and weights w_i(T) are fitted interval by interval (width H for the
+FP64 table, H32 for the FP32 one) with
 Chebyshev interpolants, converted to monomials in y = 2 (T - T_k)/H - 1 in [-1, 1] and evaluated by
 Horner's rule.  For T >= TMAX the large-T limit is used: the weight function is then a half-line
 Gaussian, so x_i = r_i^2 / T and w_i = W_i / sqrt(T), with r_i > 0 the roots of the Hermite
@@ -23,10 +24,11 @@ The reference fits the same functions with its own tables (Rys.cpp:314-2197, reg
 the golden fixtures.
 
 Output arrays (C source included by the CUDA kernels):
-  RYS_NMAX, RYS_H (interval width), RYS_NINT[n] (intervals), RYS_DEG (polynomial degree),
-  RYS_TMAX[n], rys_coef[n][interval][2n][RYS_DEG+1]  (node i at 2i, weight i at 2i+1; highest power
-  first), rys_hermite_x[n][i], rys_hermite_w[n][i].
-A float copy with lower degree (RYS32_DEG) serves the FP32 kernels.
+  RYS_NMAX, RYS_H (interval width), RYS_DEG (polynomial degree), RYS_TMAX[n],
+  RYS_TABLE_H[n][interval][2n][RYS_DEG+1]  (node i at 2i, weight i at 2i+1; highest power first),
+  RYS_HERMITE_X_H[n][i], RYS_HERMITE_W_H[n][i].
+A float table with its own interval width and lower degree (RYS32_H, RYS32_DEG) serves the FP32
+kernels.
 
 Run: python gen_rys_tables.py  (a few minutes; writes rys_tables.inc next to this file)
 """
@@ -40,9 +42,11 @@ import numpy as np
 
 mp.mp.dps = 60
 NMAX = 5
-H = 0.5          # interval width in T
-DEG = 9          # FP64 Horner degree (10 coefficients; 3e-16 relative at H = 0.5, like 13 at H = 1)
-DEG32 = 5        # FP32 Horner degree (1.1e-7 relative at H = 0.5)
+H = 0.25         # FP64 interval width in T
+DEG = 7          # FP64 Horner degree (8 coefficients; 3e-15 relative at H = 0.25; degree 9 at H = 0.5
+                 # gives 2e-16 with 2 more FMAs per polynomial, degree 8 at H = 0.5 1e-14)
+H32 = 0.5        # FP32 interval width (the FP32 kernels read the table per lane: it stays small)
+DEG32 = 5        # FP32 Horner degree (1.1e-7 relative at H32 = 0.5)
 NCHEB = 24       # interpolation nodes per interval for the fit
 
 
@@ -139,33 +143,33 @@ def horner(coefs_high_first, y, dtype):
     return r
 
 
-def build(n: int, tmax: float):
-    nint = int(round(tmax / H))
-    tab64 = np.zeros((nint, 2 * n, DEG + 1))
-    tab32 = np.zeros((nint, 2 * n, DEG32 + 1))
-    worst64 = 0.0
-    worst32 = 0.0
+def fit_table(n: int, tmax: float, h: float, deg: int, dtype):
+    """Per interval of width h on [0, tmax): the degree-deg fits of the n nodes and weights, and the
+    worst relative error of their Horner evaluation in dtype at off-node points."""
+    nint = int(round(tmax / h))
+    tab = np.zeros((nint, 2 * n, deg + 1))
+    worst = 0.0
+    nodes = [mp.cos(mp.pi * (j + mp.mpf(1) / 2) / NCHEB) for j in range(NCHEB)]
     for k in range(nint):
-        a = k * H
-        nodes = [mp.cos(mp.pi * (j + mp.mpf(1) / 2) / NCHEB) for j in range(NCHEB)]
-        samples = [rys_exact(n, a + (y + 1) * H / 2) for y in nodes]
+        a = k * h
+        samples = [rys_exact(n, a + (y + 1) * h / 2) for y in nodes]
         for i in range(n):
             for which in (0, 1):
                 f = [s[which][i] for s in samples]
-                m64 = cheb_fit(f, DEG)
-                m32 = cheb_fit(f, DEG32)
-                tab64[k, 2 * i + which, :] = [float(v) for v in reversed(m64)]
-                tab32[k, 2 * i + which, :] = [float(v) for v in reversed(m32)]
-        # check in double / float at off-node points
+                tab[k, 2 * i + which, :] = [float(v) for v in reversed(cheb_fit(f, deg))]
         for y in np.linspace(-1, 1, 9):
-            ex = rys_exact(n, a + (mp.mpf(y) + 1) * H / 2)
+            ex = rys_exact(n, a + (mp.mpf(y) + 1) * h / 2)
             for i in range(n):
                 for which in (0, 1):
                     tv = ex[which][i]
-                    v64 = horner(tab64[k, 2 * i + which], y, np.float64)
-                    v32 = horner(tab32[k, 2 * i + which], np.float32(y), np.float32)
-                    worst64 = max(worst64, float(abs(v64 - tv) / abs(tv)))
-                    worst32 = max(worst32, float(abs(mp.mpf(float(v32)) - tv) / abs(tv)))
+                    v = horner(tab[k, 2 * i + which], dtype(y), dtype)
+                    worst = max(worst, float(abs(mp.mpf(float(v)) - tv) / abs(tv)))
+    return tab, worst
+
+
+def build(n: int, tmax: float):
+    tab64, worst64 = fit_table(n, tmax, H, DEG, np.float64)
+    tab32, worst32 = fit_table(n, tmax, H32, DEG32, np.float32)
     return tab64, tab32, worst64, worst32
 
 
@@ -178,7 +182,7 @@ def main():
     lines = ["// Generated by gen_rys_tables.py -- do not edit. Rys nodes x=t^2 and weights, piecewise",
              "// polynomials in y = 2 (T - k H)/H - 1 on [k H, (k+1) H), highest power first.",
              f"#define RYS_NMAX {NMAX}", f"#define RYS_H {H!r}", f"#define RYS_DEG {DEG}",
-             f"#define RYS32_DEG {DEG32}"]
+             f"#define RYS32_H {H32!r}", f"#define RYS32_DEG {DEG32}"]
     tmaxes, offs, offs32 = [], [], []
     body64, body32 = [], []
     hx_all, hw_all = [], []
@@ -187,8 +191,8 @@ def main():
     for n in range(1, NMAX + 1):
         tmax = asym_tmax(n)
         t64, t32, e64, e32 = build(n, tmax)
-        print(f"n={n}: TMAX={tmax} intervals={t64.shape[0]} worst rel err fp64={e64:.2e} fp32={e32:.2e}",
-              file=sys.stderr)
+        print(f"n={n}: TMAX={tmax} intervals={t64.shape[0]}/{t32.shape[0]} worst rel err fp64={e64:.2e} "
+              f"fp32={e32:.2e}", file=sys.stderr, flush=True)
         tmaxes.append(tmax)
         offs.append(o)
         offs32.append(o32)
