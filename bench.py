@@ -369,7 +369,7 @@ def counted_flops(ctx, inputs, dev, stream):
     import torch
     ctx.set_counting(True)
     dG = None
-    f64, f32, launches, q32, q, fq, pq, scr = [], [], [], [], [], [], [], []
+    f64, f32, launches, q32, q, fq, pq, scr, dem = [], [], [], [], [], [], [], [], []
     for full, x in inputs:
         dx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
         if full or dG is None:
@@ -385,8 +385,9 @@ def counted_flops(ctx, inputs, dev, stream):
         fq.append(st["function_quartets_computed"])
         pq.append(st["primitive_quartets_computed"])
         scr.append(st["shell_quartets_screened"])
+        dem.append(st["shell_quartets_demoted"])
     ctx.set_counting(False)
-    return f64, f32, launches, q, q32, fq, pq, scr
+    return f64, f32, launches, q, q32, fq, pq, scr, dem
 
 
 def run_ours(args):
@@ -442,7 +443,7 @@ def run_ours(args):
     clocks = Clocks(local)
     # warm-up, then the counted (untimed) pass for the algorithmic flops
     timed_builds(mixed, inputs, max(args.warmup, 3), dev, stream, flush)
-    f64, f32, launches, nq, nq32, nfq, npq, nscr = counted_flops(mixed, inputs, dev, stream)
+    f64, f32, launches, nq, nq32, nfq, npq, nscr, ndem = counted_flops(mixed, inputs, dev, stream)
     # timed region
     replicas.barrier(ws)
     torch.cuda.synchronize(dev)
@@ -519,7 +520,8 @@ def run_ours(args):
                        "l2": "flushed: 256 MiB write before every timed build", "nbf": b.norb,
                        "builds_in_sequence": len(inputs), "parallelism": f"replicas x{ws}",
                        "shell_quartets_per_build": [int(x) for x in nq], "fp32_shell_quartets_per_build": [int(x) for x in nq32],
-                       "screened_shell_quartets_per_build": [int(x) for x in nscr]},
+                       "screened_shell_quartets_per_build": [int(x) for x in nscr],
+                       "fp32_shell_quartets_of_fp64_lists_per_build": [int(x) for x in ndem]},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * b.no2, "d2h_bytes_per_step": 8 * b.no2},
             "roofline": {"bound": "fp64+fp32 pipes", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": profile_traffic(args.form),

@@ -84,6 +84,9 @@ typedef struct UnomolStats {
     int64_t shell_quartets_screened;    /* density-screened and mixed builds: quartets of the work lists
                                            dropped by the per-quartet density screen (max |P| of the six
                                            blocks a quartet contracts with, times its bound) */
+    int64_t shell_quartets_demoted;     /* mixed builds: quartets of the FP64 part's work lists run in FP32
+                                           because their own density bound (as above) is below the FP32
+                                           cutoff (included in shell_quartets_fp32) */
 } UnomolStats;
 
 /* TwoElectronInts(basis, start_shell, label) -- TwoElectronInts.hpp:83-88.

@@ -113,3 +113,31 @@ def test_incremental_mixed_scf_converges_across_fp32_cutoffs(gpu, cut):
     assert r64["converged"] and rm["converged"], (r64["iterations"], rm["iterations"])
     assert rm["iterations"] <= r64["iterations"] + 4
     assert abs(rm["energy"] - r64["energy"]) <= 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["water3_631g", "ethane_631g"])
+def test_fp64_part_runs_low_density_quartets_in_fp32(gpu, name):
+    """The work lists put a quartet in the FP64 part when its Schwarz bound times the largest |P| of the
+    whole density reaches the FP32 cutoff; the fused mixed kernel runs it in FP32 when its bound times
+    the largest |P| of its own six blocks is below the cutoff.  Over a range of cutoffs some quartets
+    move, the counts add up (moved quartets are FP32 quartets and stay in the build), and G stays within
+    FP32 accuracy of the plain FP64 build."""
+    from unomol_gb300 import native
+    g = load_golden(name)
+    t = native.TwoElectronInts(basis_of(g))
+    G0 = t.form_g(g["P_rand"])
+    t.set_counting(True)
+    t.form_g(g["P_rand"])
+    nq = t.stats()["shell_quartets"]
+    moved = []
+    for cut in (1e-1, 1e-2, 1e-3, 1e-4, 1e-5):
+        t.set_precision(native.PREC_MIXED, cut)
+        t.set_density_screening(1e-20)
+        G1 = t.form_g(g["P_rand"])
+        st = t.stats()
+        assert st["shell_quartets"] == nq
+        assert 0 <= st["shell_quartets_demoted"] <= st["shell_quartets_fp32"] <= st["shell_quartets"]
+        assert np.abs(G1 - G0).max() <= 1e-5 * np.abs(G0).max()
+        moved.append(st["shell_quartets_demoted"])
+    assert max(moved) > 0, moved

@@ -656,6 +656,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
         A.dmax = ctx->d_dmax;
         A.skip_cut = ctx->skip_cut;
         A.skip_cut32 = (float)ctx->skip_cut;
+        A.fp32_cut32 = ctx->fp32_cut > ctx->skip_cut ? (float)ctx->fp32_cut : 0.f;  // per-quartet FP32 choice (fused kernel)
         A.dyn_mseg = ctx->d_mseg;
         CU(wl_to_float(ctx->d_Pa, ctx->d_Pa32, n2, s));
         A.Pa32 = ctx->d_Pa32;
@@ -667,9 +668,10 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     const int ncls = NPAIRCLASS * NPAIRCLASS;
     A.counters = nullptr;
     if (ctx->counting) {
-        // per class and part, 32 slots each: primitive quartets (FP64, FP32), screened quartets (FP64, FP32)
-        if (!ctx->d_counters) CU(cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 4 * ncls * 32));
-        CU(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4 * ncls * 32, s));
+        // per class and part, 32 slots each: primitive quartets (FP64, FP32), screened quartets (FP64, FP32),
+        // quartets of the FP64 part's lists run in FP32
+        if (!ctx->d_counters) CU(cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 5 * ncls * 32));
+        CU(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 5 * ncls * 32, s));
         A.counters = ctx->d_counters;
     }
     // one class: the reference's integral method (Rys for la+lb+lc+ld <= 8, MD above:
@@ -753,7 +755,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
     CU(cudaGetLastError());
     ctx->stats.kernel_launches = launches;
     if (ctx->counting) {
-        std::vector<unsigned long long> c(4 * ncls * 32);
+        std::vector<unsigned long long> c(5 * ncls * 32);
         CU(cudaMemcpyAsync(c.data(), ctx->d_counters, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
         // shell quartets of this build per block pair: in the density-screened and mixed builds the
@@ -769,7 +771,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             if (has32)
                 CU(cudaMemcpy(q32.data(), ctx->d_cnt32, sizeof(long long) * q32.size(), cudaMemcpyDeviceToHost));
         }
-        int64_t prims = 0, s64 = 0, s32 = 0, fq_done = 0, screened = 0;
+        int64_t prims = 0, s64 = 0, s32 = 0, fq_done = 0, screened = 0, demoted = 0;
         double fl = 0.0, fl32 = 0.0;
         for (const ClassLaunch& L : ctx->launches) {
             const int cls = L.bc * NPAIRCLASS + L.kc;
@@ -791,15 +793,18 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                     n64 += q64[k];
                     n32 += q32[k];
                 }
-                // quartets the per-quartet density screen dropped do no quartet-level work
-                long long d64 = 0, d32 = 0;
+                // quartets the per-quartet density screen dropped do no quartet-level work; quartets of
+                // the FP64 part's lists that the fused kernel ran in FP32 count as FP32
+                long long d64 = 0, d32 = 0, dem = 0;
                 for (int k = 0; k < 32; ++k) {
                     d64 += (long long)c[(2 * ncls + cls) * 32 + k];
                     d32 += (long long)c[(3 * ncls + cls) * 32 + k];
+                    dem += (long long)c[(4 * ncls + cls) * 32 + k];
                 }
-                n64 -= d64;
-                n32 -= d32;
+                n64 -= d64 + dem;
+                n32 += dem - d32;
                 screened += d64 + d32;
+                demoted += dem;
             }
             fl += (double)n64 * flops_per_quartet(la, lb, lc, ld);
             fl32 += (double)n32 * flops_per_quartet(la, lb, lc, ld);
@@ -816,6 +821,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             ctx->stats.shell_quartets_fp32 = s32;
         }
         ctx->stats.shell_quartets_screened = screened;
+        ctx->stats.shell_quartets_demoted = demoted;
     }
     return UNOMOL_OK;
 }

@@ -101,7 +101,8 @@ struct FockArgs {
     double thr_int;             // per-integral cut (1e-14)
     double prim_cut;            // primitive prefactor cut (1e-12)
     float thr_int32, prim_cut32, skip_cut32;  // the same cuts in FP32, for the FP32 kernels
-    double fp32_cut;            // mixed mode: bound*pmax below this -> FP32 kernel, else FP64
+    float fp32_cut32;           // mixed mode: a quartet with bound * max|P| of its blocks below this runs in FP32
+    double fp32_cut;            // mixed mode: bound * max|P| below this -> FP32 part, else FP64 part
     int mode;                   // 0 all quartets; 1 only "large" (FP64 part); 2 only "small" (FP32 part)
     int nshell;
     int rys_compat;             // reference-compatible two-root Rys regime (FP64 only)

@@ -187,6 +187,7 @@ FockArgs batch_args(UnomolBatch* b, const BLaunch& L, int k) {
     A.skip_cut = b->skip_cut;
     A.skip_cut32 = (float)b->skip_cut;
     A.fp32_cut = b->fp32_cut;
+    A.fp32_cut32 = b->fp32_cut > b->skip_cut ? (float)b->fp32_cut : 0.f;  // per-quartet FP32 choice of the fused kernel
     A.dyn_mseg = b->d_mseg;
     A.mol_nshell = b->d_nshell;
     A.mol_pmax = b->d_pmax_off;

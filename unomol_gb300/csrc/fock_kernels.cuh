@@ -286,33 +286,33 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
         rys_roots<NR, R>(T, rys, x, w, compat);
         if constexpr (LA + LB + LC + LD == 0) {  // (ss|ss): the integral is the weight times the prefactor
             acc[0] = fma(w[0], sr, acc[0]);
-            return;
-        }
+        } else {
 #pragma unroll
-        for (int r = 0; r < NR; ++r) {
-            const R fff = x[r] * rpq;  // t^2 / (p + q)   (Rys.hpp:126-129)
-            const R B00 = R(0.5) * fff;
-            const R B1 = (R(0.5) - B00 * q) * rp;
-            const R B1p = (R(0.5) - B00 * p) * rq;
-            const R qf = q * fff, pf = p * fff;
-            R Ix[Q::NI], Iy[Q::NI], Iz[Q::NI];
-            rys_axis<LA, LB, LC, LD, R>(R(1), PAx - qf * PQx, QCx + pf * PQx, B00, B1, B1p, ABx, CDx, Ix);
-            rys_axis<LA, LB, LC, LD, R>(R(1), PAy - qf * PQy, QCy + pf * PQy, B00, B1, B1p, ABy, CDy, Iy);
-            rys_axis<LA, LB, LC, LD, R>(w[r] * sr, PAz - qf * PQz, QCz + pf * PQz, B00, B1, B1p, ABz, CDz, Iz);
+            for (int r = 0; r < NR; ++r) {
+                const R fff = x[r] * rpq;  // t^2 / (p + q)   (Rys.hpp:126-129)
+                const R B00 = R(0.5) * fff;
+                const R B1 = (R(0.5) - B00 * q) * rp;
+                const R B1p = (R(0.5) - B00 * p) * rq;
+                const R qf = q * fff, pf = p * fff;
+                R Ix[Q::NI], Iy[Q::NI], Iz[Q::NI];
+                rys_axis<LA, LB, LC, LD, R>(R(1), PAx - qf * PQx, QCx + pf * PQx, B00, B1, B1p, ABx, CDx, Ix);
+                rys_axis<LA, LB, LC, LD, R>(R(1), PAy - qf * PQy, QCy + pf * PQy, B00, B1, B1p, ABy, CDy, Iy);
+                rys_axis<LA, LB, LC, LD, R>(w[r] * sr, PAz - qf * PQz, QCz + pf * PQz, B00, B1, B1p, ABz, CDz, Iz);
 #pragma unroll
-            for (int ia = 0; ia < Q::NA; ++ia)
+                for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
-                for (int ibb = 0; ibb < Q::NB; ++ibb)
+                    for (int ibb = 0; ibb < Q::NB; ++ibb)
 #pragma unroll
-                    for (int ic = 0; ic < Q::NC; ++ic)
+                        for (int ic = 0; ic < Q::NC; ++ic)
 #pragma unroll
-                        for (int id = 0; id < Q::ND; ++id) {
-                            const int f = ((ia * Q::NB + ibb) * Q::NC + ic) * Q::ND + id;
-                            const int jx = Q::iidx(cart_lx(LA, ia), cart_lx(LB, ibb), cart_lx(LC, ic), cart_lx(LD, id));
-                            const int jy = Q::iidx(cart_ly(LA, ia), cart_ly(LB, ibb), cart_ly(LC, ic), cart_ly(LD, id));
-                            const int jz = Q::iidx(cart_lz(LA, ia), cart_lz(LB, ibb), cart_lz(LC, ic), cart_lz(LD, id));
-                            acc[f] = fma(Ix[jx] * Iy[jy], Iz[jz], acc[f]);
-                        }
+                            for (int id = 0; id < Q::ND; ++id) {
+                                const int f = ((ia * Q::NB + ibb) * Q::NC + ic) * Q::ND + id;
+                                const int jx = Q::iidx(cart_lx(LA, ia), cart_lx(LB, ibb), cart_lx(LC, ic), cart_lx(LD, id));
+                                const int jy = Q::iidx(cart_ly(LA, ia), cart_ly(LB, ibb), cart_ly(LC, ic), cart_ly(LD, id));
+                                const int jz = Q::iidx(cart_lz(LA, ia), cart_lz(LB, ibb), cart_lz(LC, ic), cart_lz(LD, id));
+                                acc[f] = fma(Ix[jx] * Iy[jy], Iz[jz], acc[f]);
+                            }
+            }
         }
     };
     if (nparts > 1) {
@@ -471,9 +471,9 @@ __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g,
     return true;
 }
 
-// Density screening of one quartet: Schwarz bound times the largest |P| of the six shell-pair blocks
-// the quartet contracts with (J: ab, cd; K: ac, ad, bc, bd).
-__device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellPair& bra, const ShellPair& ket) {
+// Density-weighted bound of one quartet: its Schwarz bound times the largest |P| of the six shell-pair
+// blocks it contracts with (J: ab, cd; K: ac, ad, bc, bd).
+__device__ __forceinline__ float quartet_bound(const FockArgs& A, const ShellPair& bra, const ShellPair& ket) {
     const int a = bra.ish, b = bra.jsh, c = ket.ish, d = ket.jsh;
     int n = A.nshell;
     const float* pm = A.pmax;
@@ -483,7 +483,7 @@ __device__ __forceinline__ bool quartet_screened(const FockArgs& A, const ShellP
     }
     float m = fmaxf(fmaxf(pm[a * n + b], pm[c * n + d]), fmaxf(pm[a * n + c], pm[a * n + d]));
     m = fmaxf(m, fmaxf(pm[b * n + c], pm[b * n + d]));
-    return bra.qf * ket.qf * m < A.skip_cut32;
+    return bra.qf * ket.qf * m;
 }
 
 // Density contraction of one shell quartet and scatter into T (G = T + T^T):
@@ -647,18 +647,21 @@ __device__ __forceinline__ void count_screened(const FockArgs& A) {
                   (unsigned long long)__popc(m));
 }
 
+// Counting mode: quartets of the FP64 part's work lists that the mixed kernel ran in FP32 (fifth quarter
+// of the counter array), per warp into one of 32 slots of the launch's class.
+__device__ __forceinline__ void count_demoted(const FockArgs& A) {
+    const unsigned m = __activemask();
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1)
+        atomicAdd(A.counters + 4 * NPAIRCLASS * NPAIRCLASS * 32 + A.counter_base + (blockIdx.x & 31),
+                  (unsigned long long)__popc(m));
+}
+
+// Integrals, density contraction and scatter of one shell quartet in the arithmetic type R.
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
-__device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt, const R* __restrict__ rys, long long g) {
+__device__ __forceinline__ void quartet_item(const FockArgs& A, const NormTable& nt, const R* __restrict__ rys,
+                                             const ShellPair& bra, const ShellPair& ket, bool same_pair) {
     using Q = QClass<LA, LB, LC, LD>;
-    int bi, ki;
     unsigned npass = 0;
-    if (!(A.mode == 0 ? decode_work_warp<false>(A, g, bi, ki) : decode_work_warp<true>(A, g, bi, ki))) return;
-    const ShellPair bra = A.pairs[bi];
-    const ShellPair ket = A.pairs[ki];
-    if (A.mode != 0 && quartet_screened(A, bra, ket)) {
-        if (A.counters) count_screened(A);
-        return;
-    }
     R acc[Q::NF];
     if constexpr (sizeof(R) == 8)
         shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.prim_cut32, A.rys_compat != 0, acc,
@@ -666,8 +669,47 @@ __device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt
     else
         shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, A.prim_cut32, A.prim_cut32, false, acc,
                                                          A.counters ? &npass : nullptr);
-    digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, bi == ki, acc, nt);
+    digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, same_pair, acc, nt);
     if (A.counters) count_flush(A, npass);
+}
+
+template <int LA, int LB, int LC, int LD, bool UHF, typename R>
+__device__ __forceinline__ void fock_item(const FockArgs& A, const NormTable& nt, const R* __restrict__ rys, long long g) {
+    int bi, ki;
+    if (!(A.mode == 0 ? decode_work_warp<false>(A, g, bi, ki) : decode_work_warp<true>(A, g, bi, ki))) return;
+    const ShellPair bra = A.pairs[bi];
+    const ShellPair ket = A.pairs[ki];
+    if (A.mode != 0 && quartet_bound(A, bra, ket) < A.skip_cut32) {
+        if (A.counters) count_screened(A);
+        return;
+    }
+    quartet_item<LA, LB, LC, LD, UHF, R>(A, nt, rys, bra, ket, bi == ki);
+}
+
+// FP64 part of a mixed build, with the precision chosen per quartet.  The work lists put a quartet in
+// the FP64 part when its Schwarz bound times the largest |P| of the whole density reaches the FP32 cut;
+// here a quartet whose bound times the largest |P| of its own six blocks (the density elements it is
+// contracted with) is below that cut runs in FP32 (with the FP32 part's arguments A32), under the same
+// per-quartet error bound as the FP32 part's own quartets.
+template <int LA, int LB, int LC, int LD, bool UHF>
+__device__ __forceinline__ void fock_item_fp64_part(const FockArgs& A64, const FockArgs& A32, const NormTable& nt,
+                                                    const double* __restrict__ rys64, const float* __restrict__ rys32,
+                                                    long long g) {
+    int bi, ki;
+    if (!decode_work_warp<true>(A64, g, bi, ki)) return;
+    const ShellPair bra = A64.pairs[bi];
+    const ShellPair ket = A64.pairs[ki];
+    const float bound = quartet_bound(A64, bra, ket);
+    if (bound < A64.skip_cut32) {
+        if (A64.counters) count_screened(A64);
+        return;
+    }
+    if (bound < A64.fp32_cut32) {
+        if (A64.counters) count_demoted(A64);
+        quartet_item<LA, LB, LC, LD, UHF, float>(A32, nt, rys32, bra, ket, bi == ki);
+    } else {
+        quartet_item<LA, LB, LC, LD, UHF, double>(A64, nt, rys64, bra, ket, bi == ki);
+    }
 }
 
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
@@ -679,7 +721,8 @@ __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const No
 // of 2 x nblk CTAs, alternating (even CTAs FP64, odd CTAs FP32).  Both parts number their quartets
 // compactly from 0, so their working CTAs come first in the grid and an SM holds both kinds at once:
 // warps on the FP64 pipe beside warps on the FP32 pipe and the loads.  CTAs past a part's total end at
-// their first load.
+// their first load.  The FP64 part's quartets whose own density bound is below the FP32 cut run in FP32
+// (fock_item_fp64_part).
 template <int LA, int LB, int LC, int LD, bool UHF>
 __global__ void __launch_bounds__(128) fock_jk_mixed(const FockArgs A64, const FockArgs A32, const NormTable nt,
                                                       const double* __restrict__ rys64,
@@ -688,7 +731,7 @@ __global__ void __launch_bounds__(128) fock_jk_mixed(const FockArgs A64, const F
     if (blockIdx.x & 1)
         fock_item<LA, LB, LC, LD, UHF, float>(A32, nt, rys32, g);
     else
-        fock_item<LA, LB, LC, LD, UHF, double>(A64, nt, rys64, g);
+        fock_item_fp64_part<LA, LB, LC, LD, UHF>(A64, A32, nt, rys64, rys32, g);
 }
 
 // Persistent form for batches of molecules: a fixed grid of CTAs (a few per SM) pulls tiles of
@@ -804,7 +847,7 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
     if (!(A.mode == 0 ? decode_work_warp<false>(A, g, bi, ki) : decode_work_warp<true>(A, g, bi, ki))) return;
     const ShellPair bra = A.pairs[bi];
     const ShellPair ket = A.pairs[ki];
-    if (A.mode != 0 && quartet_screened(A, bra, ket)) return;
+    if (A.mode != 0 && quartet_bound(A, bra, ket) < A.skip_cut32) return;
     const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
     const int NF = NA * NB * NC * ND;
     const int nr = (la + lb + lc + ld) / 2 + 1;

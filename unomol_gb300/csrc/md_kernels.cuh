@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(128) fock_jk_md(const FockArgs A, const NormTa
         if (!(A.mode == 0 ? decode_work(A, w, bi, ki) : decode_work_dyn(A, w, bi, ki))) continue;
         const ShellPair bra = A.pairs[bi];
         const ShellPair ket = A.pairs[ki];
-        if (A.mode != 0 && quartet_screened(A, bra, ket)) continue;
+        if (A.mode != 0 && quartet_bound(A, bra, ket) < A.skip_cut32) continue;
         const int id = f % ND, ic = (f / ND) % NC, ib = (f / (ND * NC)) % NB, ia = f / (ND * NC * NB);
         double v = md_function_quartet(bra, ket, A.prims, la, lb, lc, ld, ia, ib, ic, id);
         v *= nt.v[la][ia] * nt.v[lb][ib] * nt.v[lc][ic] * nt.v[ld][id];

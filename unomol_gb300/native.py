@@ -58,7 +58,7 @@ class Stats(C.Structure):
                 ("nbf", C.c_int), ("npairs", C.c_int), ("kernel_launches", C.c_int), ("pad_", C.c_int),
                 ("primitive_quartets_computed", C.c_int64), ("eri_flops", C.c_double),
                 ("eri_flops_fp32", C.c_double), ("function_quartets_computed", C.c_int64),
-                ("shell_quartets_screened", C.c_int64)]
+                ("shell_quartets_screened", C.c_int64), ("shell_quartets_demoted", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
