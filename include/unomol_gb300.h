@@ -193,6 +193,58 @@ int unomol_gpu_l2_peak(double* read_gbs, double* atomic_gops);
  * so calls that overlap on the GPU (other streams, other host threads) race; serialise them. */
 int unomol_gpu_fock_rhf_noalloc(UnomolCtx* ctx, const double* dP, double* dG, void* stream);
 
+/* ---- Conventional build from stored integrals ----
+ * The reference computes every unique integral once (TwoElectronInts.cpp:511-697), keeps each one with
+ * |v| > 1e-14 as a 24-byte record {double val; int i, j, k, l} (TwoInts, TwoElectronInts.hpp:20-23) in
+ * an 8 GiB memory cache that spills to its integral file (cache.hpp:18-386), and streams the records
+ * through its scatter on every formGmatrix call (TwoElectronInts.cpp:699-869).  These calls give the
+ * same two things on the GPU:
+ *   - the records: unomol_gpu_write_records computes the canonical integrals (i >= j, k >= l,
+ *     (i,j) >= (k,l) in that order, the reference's labels and storage cut; the same set the reference
+ *     stores, in another order) and writes them as raw 24-byte records, the layout of the reference's
+ *     integral file;
+ *   - a stored build: unomol_gpu_store_integrals computes the records on the GPU (or
+ *     unomol_gpu_store_records reads them from such a file) and turns them into the sparse matrix of
+ *     the linear map P -> G over packed indices, kept in device memory.  While a context holds a
+ *     store, unomol_gpu_fock_rhf/uhf and their _device variants stream that matrix (FP64, no
+ *     integrals recomputed); the precision, density-screening and integral-method settings then play
+ *     no part.  unomol_gpu_recalculate rebuilds the store for the new centres; unomol_gpu_drop_store
+ *     returns to the direct build.  The allocation-free build always runs the direct build.
+ * The store holds one matrix element per distinct (row, column) pair: for RHF (UNOMOL_STORE_RHF) the
+ * matrix of G = 2J - K; for UHF (UNOMOL_STORE_UHF) the J and the K matrices, which serve RHF builds
+ * as well.  Its size grows with the square of the surviving shell quartets: for the 32-water 6-31G
+ * cluster (416 functions) about 10^9 elements, 12 bytes each.  max_gib bounds the device memory that
+ * building the store may hold at once (0: 64 GiB); a store that does not fit returns UNOMOL_ENOMEM. */
+typedef struct UnomolRecord {
+    double val;
+    int32_t i, j, k, l;
+} UnomolRecord; /* TwoInts (TwoElectronInts.hpp:20-23): 24 bytes */
+
+#define UNOMOL_STORE_RHF 1
+#define UNOMOL_STORE_UHF 2
+
+typedef struct UnomolStoreInfo {
+    int kind;            /* 0 (no store), UNOMOL_STORE_RHF or UNOMOL_STORE_UHF */
+    int slabs;           /* row ranges the matrix is kept in */
+    int64_t records;     /* integral records the store was made from */
+    int64_t nonzeros;    /* stored matrix elements */
+    int64_t bytes;       /* device bytes of the store (values, columns, row offsets) */
+    double ms_records;   /* device time of the integral pass (or of reading and checking the records) */
+    double ms_assemble;  /* device time of turning the records into the matrix (sorts and merges) */
+} UnomolStoreInfo;
+
+/* TwoElectronInts::calculate (TwoElectronInts.cpp:511-697) into a store on the device; see above. */
+int unomol_gpu_store_integrals(UnomolCtx* ctx, int kind, double max_gib);
+/* The same from a file of 24-byte records (the reference's integral file layout, or the output of
+ * unomol_gpu_write_records); the records must be canonical and index the context's basis. */
+int unomol_gpu_store_records(UnomolCtx* ctx, const char* path, int kind, double max_gib);
+/* Back to the direct build; frees the store. */
+int unomol_gpu_drop_store(UnomolCtx* ctx);
+int unomol_gpu_store_info(const UnomolCtx* ctx, UnomolStoreInfo* out);
+/* Computes the canonical records of the context's basis on the GPU and writes them to `path` as raw
+ * 24-byte records (cache.hpp:298-327 writes the same layout); *count = records written. */
+int unomol_gpu_write_records(UnomolCtx* ctx, const char* path, int64_t* count);
+
 void unomol_gpu_destroy(UnomolCtx* ctx);
 
 /* ---- Batches of molecules (no reference counterpart: the reference handles one molecule) ----

@@ -1,0 +1,258 @@
+"""Conventional build from stored integrals (unomol_gpu_store_integrals / _store_records /
+_write_records) against the reference's own integral records and G(P).
+
+The reference keeps every canonical integral with |v| > 1e-14 as a 24-byte TwoInts record
+(TwoElectronInts.hpp:20-23, TwoElectronInts.cpp:622-671) and builds G by streaming those records through
+its scatter (TwoElectronInts.cpp:699-869).  Checked here:
+  * the records the GPU writes are the reference's records: the same labels (i >= j, k >= l,
+    (i,j) >= (k,l)) with values within 1e-12, for the fixtures that hold the reference's record dump; the
+    same count as the reference stored for every fixture (labels within 1 % of the storage cut may fall on
+    either side of it);
+  * G(P) of the stored build within 1e-10 of the reference's, RHF and UHF stores, every fixture, both
+    integral methods;
+  * a store made from the reference's own records (written to a file in the reference's layout) gives
+    the reference's G: the record format and the scatter semantics are the reference's;
+  * write -> read round trip, recalculate, the SCF through the store, and the error paths.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import basis_of, golden_cases, load_golden, rand_density
+
+TOL_G = 1e-10
+TOL_VAL = 1e-12
+CUT = 1e-14
+CASES = golden_cases()
+
+
+def _ctx(g, method=None):
+    from unomol_gb300.native import TwoElectronInts
+    t = TwoElectronInts(basis_of(g))
+    if method is not None:
+        t.set_eri_method(method)
+    return t
+
+
+def _records(path):
+    from unomol_gb300.native import RECORD_DTYPE
+    return np.fromfile(path, dtype=RECORD_DTYPE)
+
+
+def _key(i, j, k, l, n):
+    return ((i.astype(np.int64) * n + j) * n + k) * n + l
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_631g", "h2o_sto3g_c0"])
+def test_records_are_the_reference_records(gpu, name, tmp_path):
+    g = load_golden(name)
+    t = _ctx(g)
+    path = str(tmp_path / "ints.dat")
+    n = t.write_records(path)
+    rec = _records(path)
+    assert len(rec) == n == os.path.getsize(path) // 24
+    # canonical labels
+    assert np.all(rec["j"] <= rec["i"]) and np.all(rec["l"] <= rec["k"])
+    assert np.all((rec["k"] < rec["i"]) | ((rec["k"] == rec["i"]) & (rec["l"] <= rec["j"])))
+    nbf = basis_of(g).norb
+    kg = _key(rec["i"], rec["j"], rec["k"], rec["l"], nbf)
+    ijkl = g["ints_ijkl"].astype(np.int64)
+    kr = _key(ijkl[:, 0], ijkl[:, 1], ijkl[:, 2], ijkl[:, 3], nbf)
+    assert len(np.unique(kg)) == len(kg), "a label appears twice"
+    common, ig, ir = np.intersect1d(kg, kr, return_indices=True)
+    err = np.abs(rec["val"][ig] - g["ints_val"][ir]).max()
+    assert err <= TOL_VAL, f"{name}: max|dv| = {err:.3e}"
+    # labels on one side only: within 1 % of the storage cut
+    only_g = np.setdiff1d(np.arange(len(kg)), ig)
+    only_r = np.setdiff1d(np.arange(len(kr)), ir)
+    assert np.all(np.abs(rec["val"][only_g]) < 1.01 * CUT), f"{len(only_g)} GPU records the reference does not store"
+    assert np.all(np.abs(g["ints_val"][only_r]) < 1.01 * CUT), f"{len(only_r)} reference records missing"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_record_count_matches_reference(gpu, name, tmp_path):
+    g = load_golden(name)
+    t = _ctx(g)
+    t.set_screening(0.0)  # every quartet, as the reference's pass
+    n = t.write_records(str(tmp_path / "ints.dat"))
+    want = int(g["n_stored"])
+    assert abs(n - want) <= max(2, want // 100000), f"{name}: {n} records, the reference stored {want}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_stored_rhf_store_parity(gpu, name):
+    from unomol_gb300.native import STORE_RHF
+    g = load_golden(name)
+    t = _ctx(g)
+    t.store_integrals(STORE_RHF)
+    err = np.abs(t.form_g(g["P_rand"]) - g["G_rand"]).max()
+    assert err <= TOL_G, f"{name}: max|dG| = {err:.3e}"
+    info = t.store_info()
+    assert info["kind"] == STORE_RHF and info["nonzeros"] > 0 and info["records"] > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_stored_uhf_store_parity(gpu, name):
+    from unomol_gb300.native import STORE_UHF
+    g = load_golden(name)
+    t = _ctx(g)
+    t.store_integrals(STORE_UHF)
+    Ga, Gb = t.form_g_uhf(g["Pa"], g["Pb"])
+    err = max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max())
+    assert err <= TOL_G, f"{name}: UHF max|dG| = {err:.3e}"
+    err = np.abs(t.form_g(g["P_rand"]) - g["G_rand"]).max()  # an RHF build from the J and K matrices
+    assert err <= TOL_G, f"{name}: RHF from the UHF store, max|dG| = {err:.3e}"
+
+
+MD_CASES = golden_cases("*_md.npz", exclude_md=False)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", MD_CASES)
+def test_stored_md_mode(gpu, name):
+    """Records by McMurchie-Davidson (the reference built with -DUNOMOL_MD_INTS)."""
+    from unomol_gb300.native import ERI_MD, STORE_UHF
+    g = load_golden(name)
+    t = _ctx(g, ERI_MD)
+    t.store_integrals(STORE_UHF)
+    assert np.abs(t.form_g(g["P_rand"]) - g["G_rand"]).max() <= TOL_G
+    Ga, Gb = t.form_g_uhf(g["Pa"], g["Pb"])
+    assert max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max()) <= TOL_G
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_631g", "h2o_sto3g_c0"])
+def test_store_from_the_reference_records(gpu, name, tmp_path):
+    """The reference's own records, written in its 24-byte layout, read into a store."""
+    from unomol_gb300.native import RECORD_DTYPE, STORE_RHF, STORE_UHF
+    g = load_golden(name)
+    rec = np.zeros(len(g["ints_val"]), dtype=RECORD_DTYPE)
+    rec["val"] = g["ints_val"]
+    for c, k in enumerate("ijkl"):
+        rec[k] = g["ints_ijkl"][:, c]
+    path = str(tmp_path / "MINTS.DAT")
+    rec.tofile(path)
+    t = _ctx(g)
+    t.store_records(path, STORE_RHF)
+    assert t.store_info()["records"] == len(rec)
+    assert np.abs(t.form_g(g["P_rand"]) - g["G_rand"]).max() <= TOL_G
+    t.store_records(path, STORE_UHF)
+    Ga, Gb = t.form_g_uhf(g["Pa"], g["Pb"])
+    assert max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max()) <= TOL_G
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ref_dh95_co2", "he_ccpvqz", "ref_tzp_ch4"])
+def test_write_read_round_trip(gpu, name, tmp_path):
+    """d, f and g shells: records written by one context, read by another, G as the direct build."""
+    from unomol_gb300.native import STORE_UHF
+    g = load_golden(name)
+    path = str(tmp_path / "ints.dat")
+    n = _ctx(g).write_records(path)
+    t = _ctx(g)
+    direct = t.form_g(g["P_rand"])
+    t.store_records(path, STORE_UHF)
+    assert t.store_info()["records"] == n
+    assert np.abs(t.form_g(g["P_rand"]) - direct).max() <= 1e-12 * max(1.0, np.abs(direct).max())
+    assert np.abs(t.form_g(g["P_rand"]) - g["G_rand"]).max() <= TOL_G
+
+
+@pytest.mark.gpu
+def test_store_follows_recalculate_and_drop(gpu):
+    """recalculate (TwoElectronInts.hpp:94-96) rebuilds the store for the moved centres."""
+    from unomol_gb300 import molecules
+    from unomol_gb300.basis import Basis
+    from unomol_gb300.native import STORE_RHF, TwoElectronInts
+    atoms = molecules.water_cluster(3, 5)
+    rng = np.random.default_rng(11)
+    moved_atoms = [(e, tuple(np.asarray(x) + rng.normal(scale=0.1, size=3))) for e, x in atoms]
+    b = Basis(text=molecules.patin_text(atoms, "6-31G"))
+    moved = Basis(text=molecules.patin_text(moved_atoms, "6-31G"))
+    t = TwoElectronInts(b)
+    t.store_integrals(STORE_RHF)
+    P = rand_density(b.norb, 7)
+    G0 = t.form_g(P)
+    t.recalculate(moved)
+    assert t.store_info()["kind"] == STORE_RHF
+    want = TwoElectronInts(moved).form_g(P)
+    assert np.abs(G0 - want).max() > 1e-6  # the geometry really moved
+    assert np.abs(t.form_g(P) - want).max() <= 1e-12 * max(1.0, np.abs(want).max())
+    t.drop_store()
+    assert t.store_info()["kind"] == 0
+    assert np.abs(t.form_g(P) - want).max() <= 1e-12 * max(1.0, np.abs(want).max())
+
+
+@pytest.mark.gpu
+def test_scf_through_the_store(gpu):
+    """The SCF driver's builds go through the store: same energy as the direct SCF."""
+    from unomol_gb300 import native
+    g = load_golden("water3_631g")
+    b = basis_of(g)
+    S, T, H = native.one_electron(b)
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, maxits=100, eps=1e-10, diis_tol=1e-7)
+    direct = native.scf(native.TwoElectronInts(b), b, **kw)
+    t = native.TwoElectronInts(b)
+    t.store_integrals(native.STORE_RHF)
+    stored = native.scf(t, b, **kw)
+    assert abs(stored["energy"] - direct["energy"]) <= 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("screening,tol", [(None, 1e-8), (0.0, 1e-10)], ids=["schwarz", "full"])
+def test_stored_decane(gpu, screening, tol):
+    """n-decane 6-31G (134 functions): the reference's G for a random and for the converged density,
+    and the UHF cation's Ga, Gb."""
+    from unomol_gb300.basis import Basis
+    from unomol_gb300.native import STORE_UHF, TwoElectronInts
+    g = load_golden("decane_631g")
+    b = Basis(text=str(g["patin"]))
+    t = TwoElectronInts(b)
+    if screening is not None:
+        t.set_screening(screening)
+    t.store_integrals(STORE_UHF)
+    P = rand_density(b.norb, int(g["seed"]))
+    assert np.abs(t.form_g(P) - g["G_rand"]).max() <= tol
+    assert np.abs(t.form_g(g["P_conv"]) - g["G_conv"]).max() <= tol
+    bc = Basis(text=str(g["patin_cation"]))
+    tc = TwoElectronInts(bc)
+    if screening is not None:
+        tc.set_screening(screening)
+    tc.store_integrals(STORE_UHF)
+    Pa, Pb = rand_density(bc.norb, int(g["seed"]) + 1), rand_density(bc.norb, int(g["seed"]) + 2)
+    Ga, Gb = tc.form_g_uhf(Pa, Pb)
+    assert max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max()) <= tol
+
+
+@pytest.mark.gpu
+def test_store_error_paths(gpu, tmp_path):
+    from unomol_gb300.native import RECORD_DTYPE, STORE_RHF, STORE_UHF, UnomolError
+    g = load_golden("h2o_631g")
+    t = _ctx(g)
+    t.store_integrals(STORE_RHF)
+    with pytest.raises(UnomolError, match="UHF build on an RHF store"):
+        t.form_g_uhf(g["Pa"], g["Pb"])
+    with pytest.raises(UnomolError, match="unknown store kind"):
+        t.store_integrals(7)
+    with pytest.raises(UnomolError, match="memory budget"):
+        t.store_integrals(STORE_UHF, max_gib=1e-6)
+    # the earlier store is kept after a failed one
+    assert t.store_info()["kind"] == STORE_RHF
+    assert np.abs(t.form_g(g["P_rand"]) - g["G_rand"]).max() <= TOL_G
+    bad = np.zeros(3, dtype=RECORD_DTYPE)
+    bad["val"] = 1.0
+    bad["i"], bad["j"], bad["k"], bad["l"] = [3, 1, 2], [2, 0, 1], [1, 0, 3], [0, 0, 0]  # record 2: (2,1) < (3,0)
+    path = str(tmp_path / "bad.dat")
+    bad.tofile(path)
+    with pytest.raises(UnomolError, match="not a canonical record"):
+        t.store_records(path, STORE_RHF)
+    with open(path, "ab") as f:
+        f.write(b"\0" * 5)
+    with pytest.raises(UnomolError, match="multiple of 24"):
+        t.store_records(path, STORE_RHF)
+    with pytest.raises(UnomolError, match="cannot open"):
+        t.store_records(str(tmp_path / "missing.dat"), STORE_RHF)

@@ -22,7 +22,7 @@ OBJDIR = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-DUGB_MAX_PAIRCLASS=6",
                   "-I" + os.path.join(ROOT, "include")]
-UNITS = ["fock_fp64.cu", "fock_fp32.cu", "fock_mixed.cu", "fock_md.cu", "fock_batch.cu", "mlp.cu", "guess.cu", "context.cu", "setup.cu", "worklists.cu", "peak.cu", "scf.cu", "scf_batch.cu", "one_electron.cpp", "one_electron_gpu.cu", "dpm.cu"]
+UNITS = ["fock_fp64.cu", "fock_fp32.cu", "fock_mixed.cu", "fock_md.cu", "fock_batch.cu", "mlp.cu", "guess.cu", "context.cu", "setup.cu", "worklists.cu", "peak.cu", "scf.cu", "scf_batch.cu", "one_electron.cpp", "one_electron_gpu.cu", "dpm.cu", "store.cu"]
 
 
 def nvcc() -> str:

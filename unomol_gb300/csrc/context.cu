@@ -25,6 +25,7 @@
 #include "fock_dispatch.cuh"
 #include "fock_kernels.cuh"
 #include "setup.h"
+#include "store.h"
 #include "worklists.h"
 
 using namespace ugb;
@@ -107,6 +108,8 @@ struct UnomolCtx {
     int counting = 0;
     int reverse_launches = 0;  // class launches in reverse order (unomol_gpu_set_launch_order)
     double fp32_cut = 1e-10;
+    // conventional build: the stored integral matrix (store.cu); while set, Fock builds stream it
+    ugb::IntStore* store = nullptr;
     UnomolStats stats{};
     std::string err;
 };
@@ -600,8 +603,23 @@ static cudaError_t launch_class_kernel(const UnomolCtx* ctx, const ClassLaunch& 
     return launch_fock_generic(la, lb, lc, ld, uhf, fp32, A, ctx->nt, ctx->d_rys, ctx->d_rys32, s);
 }
 
+// Fock build from the stored integral matrix (unomol_gpu_store_integrals / _store_records).
+int store_build(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa, double* dGb, cudaStream_t s) {
+    if (dPb && store_kind(ctx->store) != UNOMOL_STORE_UHF)
+        return fail(ctx, UNOMOL_EINVAL, "UHF build on an RHF store: store the integrals with UNOMOL_STORE_UHF");
+    int launches = 0;
+    CU(cudaEventRecord(ctx->ev[0], s));
+    CU(cudaEventRecord(ctx->ev[1], s));
+    CU(store_fock(ctx->store, dPa, dPb, dGa, dGb, s, &launches));
+    CU(cudaEventRecord(ctx->ev[2], s));
+    CU(cudaEventRecord(ctx->ev[3], s));
+    ctx->stats.kernel_launches = launches;
+    return UNOMOL_OK;
+}
+
 // The Fock build proper: packed device P in, packed device G added into.
 int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dGa, double* dGb, cudaStream_t s) {
+    if (ctx->store) return store_build(ctx, dPa, dPb, dGa, dGb, s);
     const bool uhf = dPb != nullptr;
     int rc = ensure_density_buffers(ctx, uhf);
     if (rc) return rc;
@@ -852,6 +870,7 @@ CtxView ctx_view(const UnomolCtx* c) {
     v.d_prims32 = c->d_prims32;
     v.nprims = c->nprims;
     v.d_prefix = c->d_prefix;
+    v.d_bps = c->d_bps;
     v.nrows = c->nrows;
     v.bps = &c->bps;
     v.block_begin = &c->block_begin;
@@ -1046,7 +1065,65 @@ int unomol_gpu_create(const UnomolBasisDesc* b, int start_shell, UnomolCtx** out
 int unomol_gpu_recalculate(UnomolCtx* ctx, const double* centers) {
     if (!ctx || !centers) return fail(ctx, UNOMOL_EINVAL, "null argument");
     ctx->centers.assign(centers, centers + 3 * ctx->ncen);
-    return build_setup(ctx);
+    const int rc = build_setup(ctx);
+    if (rc || !ctx->store) return rc;
+    // the reference's recalculate recomputes its stored integrals (TwoElectronInts.hpp:94-96)
+    const int kind = store_kind(ctx->store);
+    const double max_gib = store_max_gib(ctx->store);
+    store_free(ctx->store);
+    ctx->store = nullptr;
+    return unomol_gpu_store_integrals(ctx, kind, max_gib);
+}
+
+int unomol_gpu_store_integrals(UnomolCtx* ctx, int kind, double max_gib) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    CU(cudaSetDevice(ctx->dev));
+    IntStore* st = nullptr;
+    std::string err;
+    const int rc = store_from_integrals(ctx_view(ctx), kind, max_gib, &st, err);
+    if (rc) return fail(ctx, rc, err);
+    store_free(ctx->store);
+    ctx->store = st;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_store_records(UnomolCtx* ctx, const char* path, int kind, double max_gib) {
+    if (!ctx || !path) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    CU(cudaSetDevice(ctx->dev));
+    IntStore* st = nullptr;
+    std::string err;
+    const int rc = store_from_file(ctx_view(ctx), path, kind, max_gib, &st, err);
+    if (rc) return fail(ctx, rc, err);
+    store_free(ctx->store);
+    ctx->store = st;
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_drop_store(UnomolCtx* ctx) {
+    if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
+    if (ctx->store) {
+        CU(cudaStreamSynchronize(ctx->stream));
+        store_free(ctx->store);
+        ctx->store = nullptr;
+    }
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_store_info(const UnomolCtx* ctx, UnomolStoreInfo* out) {
+    if (!ctx || !out) return UNOMOL_EINVAL;
+    store_info(ctx->store, out);
+    return UNOMOL_OK;
+}
+
+int unomol_gpu_write_records(UnomolCtx* ctx, const char* path, int64_t* count) {
+    if (!ctx || !path || !count) return fail(ctx, UNOMOL_EINVAL, "null argument");
+    CU(cudaSetDevice(ctx->dev));
+    long long n = 0;
+    std::string err;
+    const int rc = write_records(ctx_view(ctx), path, &n, err);
+    if (rc) return fail(ctx, rc, err);
+    *count = n;
+    return UNOMOL_OK;
 }
 
 int unomol_gpu_set_screening(UnomolCtx* ctx, double cut) {
@@ -1158,6 +1235,8 @@ int unomol_gpu_fock_uhf(UnomolCtx* ctx, const double* Pa, const double* Pb, doub
 void unomol_gpu_destroy(UnomolCtx* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    store_free(ctx->store);
+    ctx->store = nullptr;
     dfree(ctx->d_basis);
     dfree(ctx->d_setup);
     dfree(ctx->d_lists);

@@ -25,6 +25,7 @@ struct CtxView {
     const PrimPair32* d_prims32 = nullptr;
     long long nprims = 0;
     const long long* d_prefix = nullptr;
+    const BlockPair* d_bps = nullptr;  // device block pairs (the class launches' ranges index them)
     long long nrows = 0;
     const std::vector<BlockPair>* bps = nullptr;  // host: block pairs, blocks of equal (class, primitive pairs)
     const std::vector<int>* block_begin = nullptr;

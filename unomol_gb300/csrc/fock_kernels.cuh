@@ -838,20 +838,15 @@ __device__ __forceinline__ void rys_roots_rt(int nr, R T, const R* __restrict__ 
     }
 }
 
-template <bool UHF, typename R, typename PP>
-__global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const NormTable nt, const R* __restrict__ rys,
-                                                      const PP* __restrict__ prims, int la, int lb, int lc, int ld) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int bi, ki;
-    unsigned npass = 0;
-    if (!(A.mode == 0 ? decode_work_warp<false>(A, g, bi, ki) : decode_work_warp<true>(A, g, bi, ki))) return;
-    const ShellPair bra = A.pairs[bi];
-    const ShellPair ket = A.pairs[ki];
-    if (A.mode != 0 && quartet_bound(A, bra, ket) < A.skip_cut32) return;
+// Contracted integrals of one shell quartet with runtime angular momenta (classes with f or g shells
+// and the large d classes) into acc[NF] (f = ((ia*NB + ib)*NC + ic)*ND + id), without the component
+// normalisation factors; npass counts the primitive quartets past the prefactor cut.
+template <typename R, typename PP>
+__device__ void generic_quartet_eri(const FockArgs& A, const ShellPair& bra, const ShellPair& ket, const R* __restrict__ rys,
+                                    const PP* __restrict__ prims, int la, int lb, int lc, int ld, R* acc, unsigned& npass) {
     const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
     const int NF = NA * NB * NC * ND;
     const int nr = (la + lb + lc + ld) / 2 + 1;
-    R acc[GEN_NF];
     for (int f = 0; f < NF; ++f) acc[f] = R(0);
     const R prim_cut = R(A.prim_cut);
     const PP* pb = prims + bra.prim_begin;
@@ -895,6 +890,21 @@ __global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const No
             }
         }
     }
+}
+
+template <bool UHF, typename R, typename PP>
+__global__ void __launch_bounds__(64) fock_jk_generic(const FockArgs A, const NormTable nt, const R* __restrict__ rys,
+                                                      const PP* __restrict__ prims, int la, int lb, int lc, int ld) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int bi, ki;
+    unsigned npass = 0;
+    if (!(A.mode == 0 ? decode_work_warp<false>(A, g, bi, ki) : decode_work_warp<true>(A, g, bi, ki))) return;
+    const ShellPair bra = A.pairs[bi];
+    const ShellPair ket = A.pairs[ki];
+    if (A.mode != 0 && quartet_bound(A, bra, ket) < A.skip_cut32) return;
+    const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
+    R acc[GEN_NF];
+    generic_quartet_eri<R, PP>(A, bra, ket, rys, prims, la, lb, lc, ld, acc, npass);
     // density contraction and scatter, as digest_jk with runtime sizes
     int N = A.nbf;
     long long base = 0;

@@ -36,7 +36,13 @@ EXPORTS = [
     "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
     "unomol_gpu_moment_ints", "unomol_gpu_batch_set_precision", "unomol_gpu_batch_fock_device",
     "unomol_tc_set_wait_polls", "unomol_gpu_set_launch_order", "unomol_gpu_batch_scf_last_builds",
+    "unomol_gpu_store_integrals", "unomol_gpu_store_records", "unomol_gpu_drop_store", "unomol_gpu_store_info",
+    "unomol_gpu_write_records",
 ]
+STORE_RHF = 1
+STORE_UHF = 2
+# TwoInts (TwoElectronInts.hpp:20-23): the 24-byte records of the reference's integral file
+RECORD_DTYPE = np.dtype([("val", "<f8"), ("i", "<i4"), ("j", "<i4"), ("k", "<i4"), ("l", "<i4")])
 RYS_REFERENCE = 0
 RYS_EXACT = 1
 ERI_REFERENCE = 0
@@ -59,6 +65,14 @@ class Stats(C.Structure):
                 ("primitive_quartets_computed", C.c_int64), ("eri_flops", C.c_double),
                 ("eri_flops_fp32", C.c_double), ("function_quartets_computed", C.c_int64),
                 ("shell_quartets_screened", C.c_int64), ("shell_quartets_demoted", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class StoreInfo(C.Structure):
+    _fields_ = [("kind", C.c_int), ("slabs", C.c_int), ("records", C.c_int64), ("nonzeros", C.c_int64),
+                ("bytes", C.c_int64), ("ms_records", C.c_double), ("ms_assemble", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -221,6 +235,35 @@ class TwoElectronInts:
 
     def set_screening(self, cutoff: float):
         _check(lib().unomol_gpu_set_screening(self._h, float(cutoff)), self._h)
+
+    def store_integrals(self, kind: int = STORE_RHF, max_gib: float = 0.0):
+        """Conventional build: compute every canonical integral once on the GPU and keep the matrix of
+        P -> G in device memory; later builds stream it (unomol_gpu_store_integrals)."""
+        lib().unomol_gpu_store_integrals.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        _check(lib().unomol_gpu_store_integrals(self._h, int(kind), float(max_gib)), self._h)
+
+    def store_records(self, path: str, kind: int = STORE_RHF, max_gib: float = 0.0):
+        """The same store from a file of 24-byte TwoInts records (unomol_gpu_store_records)."""
+        lib().unomol_gpu_store_records.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_double]
+        _check(lib().unomol_gpu_store_records(self._h, os.fsencode(path), int(kind), float(max_gib)), self._h)
+
+    def drop_store(self):
+        lib().unomol_gpu_drop_store.argtypes = [C.c_void_p]
+        _check(lib().unomol_gpu_drop_store(self._h), self._h)
+
+    def store_info(self) -> dict:
+        s = StoreInfo()
+        lib().unomol_gpu_store_info.argtypes = [C.c_void_p, C.POINTER(StoreInfo)]
+        _check(lib().unomol_gpu_store_info(self._h, C.byref(s)), self._h)
+        return s.as_dict()
+
+    def write_records(self, path: str) -> int:
+        """Write the canonical integral records (|v| > 1e-14) to `path` as raw TwoInts records; returns
+        their count.  np.fromfile(path, RECORD_DTYPE) reads them back."""
+        n = C.c_int64()
+        lib().unomol_gpu_write_records.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]
+        _check(lib().unomol_gpu_write_records(self._h, os.fsencode(path), C.byref(n)), self._h)
+        return int(n.value)
 
     def stats(self) -> dict:
         s = Stats()
