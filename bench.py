@@ -25,6 +25,9 @@ k = 0, 8, ..., else the density change), cycled for K steps.
   fp64_incremental  the same incremental sequence with the FP32 part off (density-screened FP64
            builds): value / fp64_incremental is the gain of FP32, fp64_incremental / plain_fp64 that of
            the incremental build;
+  stored_form  the conventional build (the reference's own scheme: every integral computed once, then
+           streamed per build): the stored matrix of P -> G in HBM, FP64, builds of the plain SCF's
+           densities, its SCF, and the streaming kernel against the measured HBM bandwidth;
   batched_form the batching workload (256 molecules, alkanes C1-C8 and 1-6 water clusters, STO-3G or
            6-31G): batched FP64 and precision-form builds of the converged densities, and the batched
            SCF of both forms (|dE| per molecule);
@@ -364,6 +367,42 @@ def batch_form(args, dev, stream, flush):
     return out
 
 
+def stored_form(b, kw, r64, plain, dens, dev, stream, flush, steps):
+    """The conventional build (unomol_gpu_store_integrals): every canonical integral computed once into
+    the sparse matrix of P -> G kept in HBM, each build one stream of that matrix (FP64).  Timed on the
+    same full densities as plain_fp64; the SCF through the store against the plain SCF; the roofline of
+    the streaming kernel against the measured HBM copy bandwidth (algorithmic bytes per build = the
+    store's values, columns and row offsets, each read once)."""
+    import torch
+    from unomol_gb300 import native
+    st = native.TwoElectronInts(b)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    st.store_integrals(native.STORE_RHF)
+    torch.cuda.synchronize(dev)
+    t_store = time.perf_counter() - t0
+    info = st.store_info()
+    full = [(True, D) for D in dens]
+    timed_builds(st, full, 3, dev, stream, flush)
+    s_ms, _ = timed_builds(st, full, steps, dev, stream, flush)
+    rate = len(s_ms) / (sum(s_ms) / 1e3)
+    max_dF = float(np.max(np.abs(st.form_g(r64["P"]) - plain.form_g(r64["P"]))))
+    rs = native.scf(st, b, **kw)
+    hbm = measured_hbm()
+    gbs = info["bytes"] / (statistics.mean(s_ms) * 1e-3) / 1e9
+    st.close()
+    return {"value": rate, "unit": UNIT, "ms_per_build": statistics.mean(s_ms),
+            "store_build_s": t_store, "store_ms_records": info["ms_records"], "store_ms_assemble": info["ms_assemble"],
+            "records": info["records"], "nonzeros": info["nonzeros"], "bytes": info["bytes"], "slabs": info["slabs"],
+            "abs_dE": abs(rs["energy"] - r64["energy"]), "max_abs_dF": max_dF, "iterations": rs["iterations"],
+            "scf_wall_s": rs["seconds"], "scf_wall_s_with_store_build": rs["seconds"] + t_store,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": gbs / hbm if hbm else None, "kernel": "store_spmv",
+                         "algorithmic_bytes_per_build": info["bytes"]},
+            "note": "dtype f64; builds of the plain SCF's densities (full builds), L2 flushed per build; "
+                    "store_build_s = integral pass + assembly, once per geometry"}
+
+
 def counted_flops(ctx, inputs, dev, stream):
     """Algorithmic flops (FP64, FP32) and launches of every build of the sequence (untimed)."""
     import torch
@@ -474,6 +513,9 @@ def run_ours(args):
                         "note": "the value's build sequence, density skip cutoff as the value's, FP32 off: "
                                 "fp32_gain = value / this, incremental_gain = this / plain_fp64"}
     inc64.close()
+    stored = None
+    if args.form == "mixed" and not args.no_store:
+        stored = stored_form(b, kw, r64, plain, rm["densities"], dev, stream, flush, args.steps)
     batched = batch_form(args, dev, stream, flush) if args.form == "mixed" and not args.no_batch else None
     # end to end through the host entry point, pinned host buffers
     pin_in = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for _, x in inputs]
@@ -535,6 +577,7 @@ def run_ours(args):
                                        "per shell quartet (density contraction) at the FP64 and FP32 parts of "
                                        "each build's own work lists"},
             "batched_form": batched,
+            "stored_form": stored,
             "plain_fp64": {"value": plain_rate, "unit": UNIT, "ms_per_build": statistics.mean(p_ms),
                            "kernel_ms": statistics.mean(p_eri), "speedup_of_value": value / plain_rate},
             "fp64_incremental": fp64_incremental,
@@ -583,6 +626,7 @@ def main():
     ap.add_argument("--fp32-cutoff", type=float, default=FP32_CUTOFF)
     ap.add_argument("--profile", action="store_true", help="device builds only (for ncu captures)")
     ap.add_argument("--no-batch", action="store_true", help="leave out the 256-molecule batched form")
+    ap.add_argument("--no-store", action="store_true", help="leave out the stored-integral (conventional) form")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

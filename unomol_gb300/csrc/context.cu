@@ -159,8 +159,8 @@ void build_norms(NormTable& nt) {
 // NR * (2 polynomials * deg Horner steps * 2) + 3, deg = the table degree of the precision (RYS_DEG
 // for FP64, RYS32_DEG for FP32); per root 10 for B00, B1, B1', then per axis 4 for C, C', the 2D
 // recurrence, the two horizontal transfers (2 per step), and 3 per function quartet for the product
-// and accumulation.  Per shell quartet: 17 per function quartet for normalisation and the six density
-// contractions.
+// and accumulation; (ss|ss) evaluates only the weight and one FMA.  Per shell quartet: 17 per function
+// quartet for normalisation and the six density contractions.
 double flops_per_prim(int la, int lb, int lc, int ld, bool fp32 = false) {
     const int L12 = la + lb, L34 = lc + ld, NR = (L12 + L34) / 2 + 1;
     const int NF = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
@@ -172,6 +172,9 @@ double flops_per_prim(int la, int lb, int lc, int ld, bool fp32 = false) {
     double hrr = 0;
     for (int b = 1; b <= lb; ++b) hrr += 2.0 * (L12 - b + 1) * (L34 + 1);
     for (int d = 1; d <= ld; ++d) hrr += 2.0 * (la + 1) * (lb + 1) * (L34 - d + 1);
+    if (L12 + L34 == 0)  // (ss|ss): the weight F0(T) alone (FP64: one table polynomial; FP32: the closed
+                         // form, rsqrt, erf and two products) and one FMA into the integral
+        return 20 + (fp32 ? 5.0 : 2.0 * RYS_DEG + 3) + 2;
     const double roots = 2.0 * (fp32 ? RYS32_DEG : RYS_DEG) * 2.0;
     return 20 + NR * roots + 3 + NR * (10 + 3 * (4 + vrr + hrr) + 3.0 * NF);
 }

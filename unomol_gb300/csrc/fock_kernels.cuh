@@ -283,6 +283,14 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
         const R PQx = Px - R(kp.P[0]), PQy = Py - R(kp.P[1]), PQz = Pz - R(kp.P[2]);
         const R T = p * q * rpq * (PQx * PQx + PQy * PQy + PQz * PQz);
         R x[NR], w[NR];
+        if constexpr (LA + LB + LC + LD == 0 && sizeof(R) == 4) {
+            // (ss|ss) in FP32 needs only F0(T) = sqrt(pi / T) erf(sqrt T) / 2: one branch-free form for every
+            // T (T kept away from 0, where erf(x) / x is still accurate to a few ulps)
+            const float Tc = fmaxf(T, 1e-30f);
+            const float r = rsqrtf(Tc);
+            acc[0] = fmaf(0.886226925452758f * r * erff(Tc * r), sr, acc[0]);
+            return;
+        }
         rys_roots<NR, R>(T, rys, x, w, compat);
         if constexpr (LA + LB + LC + LD == 0) {  // (ss|ss): the integral is the weight times the prefactor
             acc[0] = fma(w[0], sr, acc[0]);
@@ -365,11 +373,13 @@ __device__ __forceinline__ void shell_quartet_eri(const ShellPair& bra, const Sh
             primitive(bp, kp, rs, bp.Ecc * kp.Ecc * rs);
         }
     } else {
-        // FP32 (bound by its loads, not by divergence): the plain nested loops
-        for (int ib = 0; ib < nb; ++ib) {
-            const PP bp = pb[ib * sb];
-            for (int ik = 0; ik < nk; ++ik) {
-                const PP kp = pk[ik * sk];
+        // FP32 (bound by its loads, not by divergence): the plain nested loops, ket records outer (the
+        // lanes of a warp hold different ket pairs but mostly one bra pair, whose records are then
+        // broadcast loads in the inner loop)
+        for (int ik = 0; ik < nk; ++ik) {
+            const PP kp = pk[ik * sk];
+            for (int ib = 0; ib < nb; ++ib) {
+                const PP bp = pb[ib * sb];
                 const R rs = rsqrt(bp.p + kp.p);
                 const R sr = R(SRTERM) * bp.E * kp.E * rs;
                 if (!above_cut(sr, prim_cut)) continue;  // TwoElectronInts.cpp:478-479
@@ -433,10 +443,11 @@ __device__ __forceinline__ bool decode_work_dyn(const FockArgs& A, long long g, 
 // the bra row of its first item with 32-way ballot searches (each round narrows the range 32-fold, one
 // load per lane), and every lane then steps forward to its own row.  The result is that of
 // decode_work / decode_work_dyn (DYN) with ~3 rounds of loads instead of two serial binary searches.
+// decode_warp_items: the same for warps whose lanes hold fewer items: the warp's items start at g0 (all
+// of them inside one 32-aligned range) and the lane decodes item g0 + item.
 template <bool DYN>
-__device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g, int& bra_idx, int& ket_idx) {
+__device__ __forceinline__ bool decode_warp_items(const FockArgs& A, long long g0, int item, int& bra_idx, int& ket_idx) {
     const int lane = threadIdx.x & 31;
-    const long long g0 = g - lane;
     if (g0 >= (DYN ? *A.dyn_total : A.nwork)) return false;  // uniform over the warp
     int lo = 0, hi = A.nbp - 1;  // largest block pair whose first item is <= g0 (block pair 0 starts at 0)
     while (lo < hi) {
@@ -461,7 +472,7 @@ __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g,
         a += (31 - __clz(m)) * step;
         b = min(b, a + step - 1);
     }
-    const long long w = w0 + lane;
+    const long long w = w0 + item;
     if (w >= count) return false;
     while (a + 1 < bp.bra_count && pre[a + 1] <= w) ++a;
     bra_idx = bp.bra_begin + a;
@@ -469,6 +480,12 @@ __device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g,
     if (DYN && A.mode == 2) j += A.dyn_mseg[bp.prefix_off + a];
     ket_idx = bp.ket_begin + j;
     return true;
+}
+
+template <bool DYN>
+__device__ __forceinline__ bool decode_work_warp(const FockArgs& A, long long g, int& bra_idx, int& ket_idx) {
+    const int lane = threadIdx.x & 31;
+    return decode_warp_items<DYN>(A, g - lane, lane, bra_idx, ket_idx);
 }
 
 // Density-weighted bound of one quartet: its Schwarz bound times the largest |P| of the six shell-pair
@@ -712,6 +729,65 @@ __device__ __forceinline__ void fock_item_fp64_part(const FockArgs& A64, const F
     }
 }
 
+// One shell quartet on a group of NP lanes (mask gmask): lane `part` of the group sums the primitive
+// quartets part, part + NP, ...; the group adds its partial integrals with warp shuffles and its first
+// lane contracts them with the density.
+template <int LA, int LB, int LC, int LD, bool UHF, typename R, int NP>
+__device__ __forceinline__ void quartet_item_group(const FockArgs& A, const NormTable& nt, const R* __restrict__ rys,
+                                                   const ShellPair& bra, const ShellPair& ket, bool same_pair, int part,
+                                                   unsigned gmask) {
+    using Q = QClass<LA, LB, LC, LD>;
+    unsigned npass = 0;
+    R acc[Q::NF];
+    if constexpr (sizeof(R) == 8)
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair>(bra, ket, A.prims, rys, R(A.prim_cut), A.prim_cut32, A.rys_compat != 0, acc,
+                                                       A.counters ? &npass : nullptr, part, NP);
+    else
+        shell_quartet_eri<LA, LB, LC, LD, R, PrimPair32>(bra, ket, A.prims32, rys, A.prim_cut32, A.prim_cut32, false, acc,
+                                                         A.counters ? &npass : nullptr, part, NP);
+#pragma unroll
+    for (int o = 1; o < NP; o <<= 1)
+#pragma unroll
+        for (int f = 0; f < Q::NF; ++f) acc[f] += __shfl_xor_sync(gmask, acc[f], o);
+    if (part == 0) digest_jk<LA, LB, LC, LD, UHF, R>(A, bra, ket, same_pair, acc, nt);
+    if (A.counters) count_flush(A, npass);
+}
+
+// FP64 part of a mixed build with NP lanes per quartet: the warp holds the 32 / NP items from g0 (the FP64
+// part's quartets are few and the costliest of the build, so one lane per quartet leaves most of the
+// FP64 pipe's issue slots idle); precision chosen per quartet as in fock_item_fp64_part.
+template <int LA, int LB, int LC, int LD, bool UHF, int NP>
+__device__ __forceinline__ void fock_group_fp64_part(const FockArgs& A64, const FockArgs& A32, const NormTable& nt,
+                                                     const double* __restrict__ rys64, const float* __restrict__ rys32,
+                                                     long long g0) {
+    const int lane = threadIdx.x & 31, sub = lane / NP, part = lane % NP;
+    const unsigned gmask = ((1u << NP) - 1u) << (sub * NP);
+    int bi, ki;
+    if (!decode_warp_items<true>(A64, g0, sub, bi, ki)) return;  // warp-collective; uniform over a group
+    const ShellPair bra = A64.pairs[bi];
+    const ShellPair ket = A64.pairs[ki];
+    const float bound = quartet_bound(A64, bra, ket);
+    if (bound < A64.skip_cut32) {
+        if (A64.counters && part == 0) count_screened(A64);
+        return;
+    }
+    if (bound < A64.fp32_cut32) {
+        if (A64.counters && part == 0) count_demoted(A64);
+        quartet_item_group<LA, LB, LC, LD, UHF, float, NP>(A32, nt, rys32, bra, ket, bi == ki, part, gmask);
+    } else {
+        quartet_item_group<LA, LB, LC, LD, UHF, double, NP>(A64, nt, rys64, bra, ket, bi == ki, part, gmask);
+    }
+}
+
+#ifndef UGB_FP64_PARTS
+#define UGB_FP64_PARTS 4
+#endif
+// Lanes per quartet of the FP64 part of a mixed build
+template <int LA, int LB, int LC, int LD>
+struct Fp64Parts {
+    static constexpr int value = UGB_FP64_PARTS;
+};
+
 template <int LA, int LB, int LC, int LD, bool UHF, typename R>
 __global__ void __launch_bounds__(128) fock_jk_kernel(const FockArgs A, const NormTable nt, const R* __restrict__ rys) {
     fock_item<LA, LB, LC, LD, UHF, R>(A, nt, rys, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -728,10 +804,22 @@ __global__ void __launch_bounds__(128) fock_jk_mixed(const FockArgs A64, const F
                                                       const double* __restrict__ rys64,
                                                       const float* __restrict__ rys32) {
     const long long g = (long long)(blockIdx.x >> 1) * blockDim.x + threadIdx.x;
-    if (blockIdx.x & 1)
+    if (blockIdx.x & 1) {
         fock_item<LA, LB, LC, LD, UHF, float>(A32, nt, rys32, g);
-    else
+        return;
+    }
+    constexpr int NP = Fp64Parts<LA, LB, LC, LD>::value;
+    if constexpr (NP == 1) {
         fock_item_fp64_part<LA, LB, LC, LD, UHF>(A64, A32, nt, rys64, rys32, g);
+    } else {
+        // the FP64 CTAs cover 32 / NP items per warp and step over the part's total in whole warps
+        const long long per_warp = 32 / NP;
+        const long long nwarps = (long long)((gridDim.x + 1) >> 1) * (blockDim.x >> 5);
+        const long long total = *A64.dyn_total;
+        for (long long wi = (long long)(blockIdx.x >> 1) * (blockDim.x >> 5) + (threadIdx.x >> 5); wi * per_warp < total;
+             wi += nwarps)
+            fock_group_fp64_part<LA, LB, LC, LD, UHF, NP>(A64, A32, nt, rys64, rys32, wi * per_warp);
+    }
 }
 
 // Persistent form for batches of molecules: a fixed grid of CTAs (a few per SM) pulls tiles of
