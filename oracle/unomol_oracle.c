@@ -293,8 +293,15 @@ static unsigned long long mix64(unsigned long long z) {
  * Pb == NULL: RHF (G += 2J - K); else UHF (Ga, Gb).  rys_mode 0 = reference-compatible, 1 = exact.
  * counts (optional): [0] shell quartets done, [1] function quartets, [2] primitive quartets,
  * [3] stored integrals.  Returns 0, or -1 for an unsupported basis (L > 2). */
-int orc_fock(const orc_basis* B, int start, const double* Pa, const double* Pb, double* Ga, double* Gb, int rys_mode,
-             long long stride, long long offset, int nthreads, long long* counts) {
+/* Record sink of orc_records: the stored integrals (TwoInts val, i, j, k, l) instead of the scatter. */
+typedef struct {
+    double* val;
+    int* ijkl;
+    long long cap, n;
+} rec_sink;
+
+static int fock_pass(const orc_basis* B, int start, const double* Pa, const double* Pb, double* Ga, double* Gb, int rys_mode,
+                     long long stride, long long offset, int nthreads, long long* counts, rec_sink* sink) {
     init_tables();
     for (int s = 0; s < B->nshell; ++s)
         if (B->shell_l[s] > MAXL) return -1;
@@ -381,7 +388,18 @@ int orc_fock(const orc_basis* B, int start, const double* Pa, const double* Pb, 
                         for (int kc = 0; kc < knt; ++kc) {
                             if (fabs(sq->val[kc]) > 1.e-14) {
                                 ++cnt[3];
-                                scatter(sq->val[kc], idx[kc][0], idx[kc][1], idx[kc][2], idx[kc][3], Pa, Pb, ga, gb);
+                                if (sink) {
+#pragma omp critical
+                                    {
+                                        if (sink->n < sink->cap) {
+                                            sink->val[sink->n] = sq->val[kc];
+                                            for (int t = 0; t < 4; ++t) sink->ijkl[4 * sink->n + t] = idx[kc][t];
+                                        }
+                                        ++sink->n;
+                                    }
+                                } else {
+                                    scatter(sq->val[kc], idx[kc][0], idx[kc][1], idx[kc][2], idx[kc][3], Pa, Pb, ga, gb);
+                                }
                             }
                         }
                     }
@@ -404,4 +422,23 @@ int orc_fock(const orc_basis* B, int start, const double* Pa, const double* Pb, 
         for (int t = 0; t < 4; ++t) counts[t] = tot[t];
     free(sp0);
     return 0;
+}
+
+int orc_fock(const orc_basis* B, int start, const double* Pa, const double* Pb, double* Ga, double* Gb, int rys_mode,
+             long long stride, long long offset, int nthreads, long long* counts) {
+    return fock_pass(B, start, Pa, Pb, Ga, Gb, rys_mode, stride, offset, nthreads, counts, NULL);
+}
+
+/* The stored integrals of TwoElectronInts::calculate (TwoElectronInts.cpp:622-671): the canonical
+ * function quartets with |v| > 1e-14 as (val, i, j, k, l), at most cap of them written into val[] and
+ * ijkl[4 * cap]; returns the count (which may exceed cap), or -1 for an unsupported basis. */
+long long orc_records(const orc_basis* B, int start, int rys_mode, double* val, int* ijkl, long long cap) {
+    const int no2 = B->norb * (B->norb + 1) / 2;
+    double* P = (double*)calloc(no2, sizeof(double));
+    double* G = (double*)calloc(no2, sizeof(double));
+    rec_sink sink = {val, ijkl, cap, 0};
+    const int rc = fock_pass(B, start, P, NULL, G, NULL, rys_mode, 1, 0, 0, NULL, &sink);
+    free(P);
+    free(G);
+    return rc ? -1 : sink.n;
 }

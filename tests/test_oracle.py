@@ -88,3 +88,46 @@ def test_reference_damped_trajectory_amplifies_input_differences():
     assert np.abs(e0 - g["trace"]).max() == 0.0  # the fixture is this trajectory
     d = np.abs(e1 - e0)
     assert d[:3].max() < 1e-9 and d[3] > 1e-9 and d[4] > 1e-7, d
+
+
+@pytest.mark.parametrize("name", ["h2o_631g", "h2o_sto3g_c0"])
+def test_oracle_records_are_the_reference_records(name):
+    """orc_records (the stored integrals of the integral pass, TwoElectronInts.cpp:622-671) against the
+    records the reference itself stored: the same labels (the oracle's threads split the outer shell
+    loop, so the order differs), values within 1e-12."""
+    import orc
+    g = load_golden(name)
+    val, ijkl = orc.records(basis_of(g))
+
+    def by_label(v, q):
+        q = q.astype(np.int64)
+        o = np.lexsort((q[:, 3], q[:, 2], q[:, 1], q[:, 0]))
+        return v[o], q[o]
+    v1, q1 = by_label(val, ijkl)
+    v2, q2 = by_label(g["ints_val"], g["ints_ijkl"])
+    assert np.array_equal(q1, q2)
+    assert np.abs(v1 - v2).max() <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["h2o_631g", "h2o_sto3g_c0"])
+def test_six_term_scatter_of_the_reference_records(name):
+    """The record -> G map of the conventional build (six terms per record with the coincidence factors,
+    G = T + T^T) applied to the reference's own records gives the reference's G, RHF and UHF."""
+    import orc
+    g = load_golden(name)
+    n = basis_of(g).norb
+    G = orc.scatter_records(g["ints_val"], g["ints_ijkl"], n, g["P_rand"])
+    assert np.abs(G - g["G_rand"]).max() <= 1e-12
+    Ga, Gb = orc.scatter_records(g["ints_val"], g["ints_ijkl"], n, g["Pa"], g["Pb"])
+    assert max(np.abs(Ga - g["Ga"]).max(), np.abs(Gb - g["Gb"]).max()) <= 1e-12
+
+
+@pytest.mark.parametrize("name", [c for c in FAST if not c.startswith("he")][:12])
+def test_six_term_scatter_of_oracle_records(name):
+    """The same map on the C restatement's records, for fixtures without a record dump."""
+    import orc
+    g = load_golden(name)
+    b = basis_of(g)
+    val, ijkl = orc.records(b)
+    assert abs(len(val) - int(g["n_stored"])) <= 2
+    assert np.abs(orc.scatter_records(val, ijkl, b.norb, g["P_rand"]) - g["G_rand"]).max() <= TOL_G

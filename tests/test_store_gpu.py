@@ -72,6 +72,31 @@ def test_records_are_the_reference_records(gpu, name, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ref_dh95_co2", "ref_b_dhdz", "ref_631_co", "water3_631g"])
+def test_records_match_the_oracle_records(gpu, name, tmp_path):
+    """Fixtures without a record dump (d shells included): the GPU's records against the C restatement's
+    (oracle/unomol_oracle.c: orc_records), labels equal, values within 1e-12."""
+    import sys
+    from conftest import ROOT
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import orc
+    g = load_golden(name)
+    b = basis_of(g)
+    t = _ctx(g)
+    t.set_screening(0.0)
+    path = str(tmp_path / "ints.dat")
+    t.write_records(path)
+    rec = _records(path)
+    val, ijkl = orc.records(b)
+    kg = _key(rec["i"], rec["j"], rec["k"], rec["l"], b.norb)
+    ko = _key(ijkl[:, 0], ijkl[:, 1], ijkl[:, 2], ijkl[:, 3], b.norb)
+    _, ig, io = np.intersect1d(kg, ko, return_indices=True)
+    assert np.abs(rec["val"][ig] - val[io]).max() <= TOL_VAL
+    assert np.all(np.abs(np.delete(rec["val"], ig)) < 1.01 * CUT)
+    assert np.all(np.abs(np.delete(val, io)) < 1.01 * CUT)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", CASES)
 def test_record_count_matches_reference(gpu, name, tmp_path):
     g = load_golden(name)

@@ -26,6 +26,10 @@
         work lists): create and the best of `reps` recalculates of one context for n-decane, 32 and 64
         waters (6-31G), and the creation of the 256-molecule batch.
 
+    python -m unomol_gb300.measure store [--system water32|decane] [--reps 5] [--out store.json]
+        The conventional build from stored integrals (RHF and UHF stores): construction time, matrix size,
+        device time per build against the direct FP64 build, and the agreement of G.
+
     python -m unomol_gb300.measure sweep [--out sweep.json]
         FP32 cutoff sweep of the precision form on the 32-water 6-31G cluster (molecules.water_cluster(32, 0),
         superposition-of-fragments guess, DIIS, 1e-10 Eh): the incremental mixed-precision SCF against the
@@ -280,15 +284,69 @@ def _setup(reps: int) -> dict:
     return out
 
 
+def _store(reps: int, system: str) -> dict:
+    """The conventional build (unomol_gpu_store_integrals, RHF and UHF stores) of n-decane or the 32-water
+    cluster (6-31G): construction time (integral pass, assembly), matrix size, device time per build
+    (events on one stream, L2 flushed by a 256 MiB write before each build, mean of `reps` after three
+    warm-ups) against the direct FP64 build of the same density, and max |G(store) - G(direct)|."""
+    import time
+
+    import torch
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    atoms = molecules.alkane(10) if system == "decane" else molecules.water_cluster(32, 0)
+    b = Basis(text=molecules.patin_text(atoms, "6-31G"))
+    rng = np.random.default_rng(0)
+    q, _ = np.linalg.qr(rng.normal(size=(b.norb, b.nelec // 2)))
+    P = np.ascontiguousarray((q @ q.T)[np.tril_indices(b.norb)])
+    dP = torch.from_numpy(P).to(dev)
+    dG = torch.zeros_like(dP)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timeit(ctx, n):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for k in range(n + 3):
+            flush.fill_(k & 0xFF)
+            if k >= 3:
+                ev[k - 3][0].record(stream)
+            ctx.fock_device(dP.data_ptr(), dG.data_ptr(), stream.cuda_stream)
+            if k >= 3:
+                ev[k - 3][1].record(stream)
+        torch.cuda.synchronize(dev)
+        return sum(a.elapsed_time(c) for a, c in ev) / n
+
+    direct = native.TwoElectronInts(b)
+    out = {"system": system + "/6-31G", "nbf": b.norb, "direct_fp64_ms": timeit(direct, max(2, reps // 4))}
+    G_direct = direct.form_g(P)
+    for kind, name in ((native.STORE_RHF, "rhf"), (native.STORE_UHF, "uhf")):
+        t = native.TwoElectronInts(b)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        t.store_integrals(kind)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        info = t.store_info()
+        ms = timeit(t, reps)
+        out[name + "_store"] = dict(info, construction_wall_s=wall, ms_per_build=ms,
+                                    stream_gbs=info["bytes"] / (ms * 1e-3) / 1e9,
+                                    max_abs_dG_vs_direct=float(np.abs(t.form_g(P) - G_direct).max()))
+        t.close()
+    return out
+
+
 def main():
-    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM / DPM / set-up measurements")
-    ap.add_argument("what", choices=["batch", "sweep", "gemm", "dpm", "setup"])
+    ap = argparse.ArgumentParser(description="batching / precision-form / tensor-core GEMM / DPM / set-up / "
+                                             "stored-integral measurements")
+    ap.add_argument("what", choices=["batch", "sweep", "gemm", "dpm", "setup", "store"])
     ap.add_argument("--points", type=int, default=64)
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--system", default="water32", choices=["water32", "decane"])
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
     rep = (_batch(a.reps) if a.what == "batch" else _sweep() if a.what == "sweep" else
-           _gemm(max(a.reps, 10)) if a.what == "gemm" else _setup(a.reps) if a.what == "setup" else _dpm(a.points))
+           _gemm(max(a.reps, 10)) if a.what == "gemm" else _setup(a.reps) if a.what == "setup" else
+           _store(a.reps, a.system) if a.what == "store" else _dpm(a.points))
     print(json.dumps(rep, indent=1))
     if a.out:
         with open(a.out, "w") as f:
