@@ -45,6 +45,7 @@ struct ClassLaunch {
 
 struct UnomolCtx {
     int dev = 0;
+    int nsm = 1;  // SMs of the device
     cudaStream_t stream = nullptr;
     int nshell = 0, nbf = 0, ncen = 0, start_shell = 0, maxl = 0;
     std::vector<int> sl, snp, scen, soff, sprim;
@@ -700,6 +701,9 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
 #ifndef UGB_FUSED_MIXED
 #define UGB_FUSED_MIXED 1
 #endif
+#ifndef UGB_FUSE_MAXL
+#define UGB_FUSE_MAXL 1  // classes with la+lb+lc+ld above this run their two parts as separate kernels
+#endif
     // mixed builds with both parts: the FP64 and FP32 parts of a templated class in one launch
     // (fock_jk_mixed), classes alternating over two equal-priority streams; otherwise the FP64 part on a
     // high-priority stream and the FP32 part on a second one
@@ -733,7 +737,8 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
             A.dyn_count = ctx->d_cnt64 + L.bp_begin;
             A.dyn_begin = ctx->d_begin64 + L.bp_begin;
             A.dyn_total = ctx->d_total64 + li;
-            if (fused && fock_mixed_fused(L.bc, L.kc) && pc_la(L.bc) + pc_lb(L.bc) + pc_la(L.kc) + pc_lb(L.kc) <= 8) {
+            const int lsum = pc_la(L.bc) + pc_lb(L.bc) + pc_la(L.kc) + pc_lb(L.kc);
+            if (fused && fock_mixed_fused(L.bc, L.kc) && lsum <= 8) {
                 FockArgs A32 = A;
                 A32.mode = 2;
                 A32.dyn_prefix = ctx->d_pre32;
@@ -741,8 +746,18 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                 A32.dyn_begin = ctx->d_begin32 + L.bp_begin;
                 A32.dyn_total = ctx->d_total32 + li;
                 A32.counter_base += ncls * 32;
-                CU(launch_fock_mixed(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ls[li & 1]));
-                ++launches;
+                if (lsum <= UGB_FUSE_MAXL) {
+                    CU(launch_fock_mixed(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ls[li & 1]));
+                    ++launches;
+                } else {
+                    // classes whose FP32 code needs far fewer registers than their FP64 code: the FP64 part
+                    // (four lanes per quartet) and the FP32 part as two kernels on the two streams, each
+                    // at its own register count
+                    CU(launch_fock_fp64_part(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ctx->nsm * 8,
+                                             ls[li & 1]));
+                    CU(launch_class_kernel(ctx, L, uhf, true, A32, ls[(li + 1) & 1]));
+                    launches += 2;
+                }
                 continue;
             }
             CU(launch_class(L, false));
@@ -950,6 +965,7 @@ int rys_tables(int dev, double*& d64, float*& d32, std::string& err) {
 // Stream, events, Rys tables, the basis on the device and the first set-up of a new context.
 int init_device(UnomolCtx* ctx, int np) {
     CU(cudaGetDevice(&ctx->dev));
+    CU(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
     CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     for (auto& e : ctx->ev) CU(cudaEventCreate(&e));
     {

@@ -22,6 +22,10 @@ cudaError_t launch_fock_fp32(int bc, int kc, bool uhf, const FockArgs& A, const 
 bool fock_mixed_fused(int bc, int kc);
 cudaError_t launch_fock_mixed(int bc, int kc, bool uhf, const FockArgs& A64, const FockArgs& A32, const NormTable& nt,
                               const double* rys64, const float* rys32, cudaStream_t stream);
+// The FP64 part of a mixed build of one class alone (classes that fock_mixed_fused accepts), on a grid of
+// at most `grid` CTAs whose warps step over the part's quartets (NP lanes per quartet).
+cudaError_t launch_fock_fp64_part(int bc, int kc, bool uhf, const FockArgs& A64, const FockArgs& A32, const NormTable& nt,
+                                  const double* rys64, const float* rys32, int grid, cudaStream_t stream);
 cudaError_t launch_schwarz(int pc, const ShellPair* pairs, const PrimPair* prims, int begin, int count,
                            const NormTable& nt, const double* rys, double* q_out, cudaStream_t stream);
 

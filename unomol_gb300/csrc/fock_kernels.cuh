@@ -822,6 +822,20 @@ __global__ void __launch_bounds__(128) fock_jk_mixed(const FockArgs A64, const F
     }
 }
 
+// The FP64 part of a mixed build alone (NP lanes per quartet, per-quartet precision as in fock_jk_mixed),
+// for the classes whose FP32 part runs as its own kernel at the FP32 code's register count: a fixed grid
+// whose warps step over the part's quartets.
+template <int LA, int LB, int LC, int LD, bool UHF>
+__global__ void __launch_bounds__(128) fock_jk_fp64_part(const FockArgs A64, const FockArgs A32, const NormTable nt,
+                                                         const double* __restrict__ rys64, const float* __restrict__ rys32) {
+    constexpr int NP = Fp64Parts<LA, LB, LC, LD>::value;
+    const long long per_warp = 32 / NP;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long total = *A64.dyn_total;
+    for (long long wi = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wi * per_warp < total; wi += nwarps)
+        fock_group_fp64_part<LA, LB, LC, LD, UHF, NP>(A64, A32, nt, rys64, rys32, wi * per_warp);
+}
+
 // Persistent form for batches of molecules: a fixed grid of CTAs (a few per SM) pulls tiles of
 // blockDim consecutive work items from an atomic counter until the launch's work is done, so that
 // molecules of uneven size balance across the GPU in one launch per class.  Tiles follow the work

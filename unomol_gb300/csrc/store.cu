@@ -19,9 +19,11 @@
 // and summed per key (CUB), which leaves one CSR matrix per slab with sorted columns and one element per
 // distinct (row, column).
 //
-// Build.  One warp per row streams the row's values and columns from HBM (cache-streaming loads, read
-// once per build) and gathers P, which stays in L2.  No integral is recomputed; the RHF store needs no
-// atomics (every row is one G element).
+// Build.  One warp per row piece (rows longer than PIECE_MAX elements are split into near-equal pieces,
+// so that no warp of the last wave streams a much longer row than the others) streams the values and
+// columns from HBM (cache-streaming loads, read once per build) and gathers P, which stays in L2.  No
+// integral is recomputed; in the RHF store a whole row's sum is its G element (a plain add), the pieces
+// of split rows add theirs atomically.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -39,6 +41,15 @@
 
 namespace ugb {
 
+// A piece of one row for one warp of the build: rows longer than a piece's limit are split, so that the
+// warps of a build get similar element counts (the last wave does not wait on a few long rows).
+struct RowPiece {
+    int row;    // row within the slab
+    int begin;  // element range [begin, end) of the slab
+    int end;
+    int whole;  // 1: the piece is the whole row (its sum is the row's G element)
+};
+
 struct StoreSlab {
     long long r0 = 0, r1 = 0;  // rows [r0, r1) of the matrix
     long long nnz = 0;
@@ -46,6 +57,8 @@ struct StoreSlab {
     int* rowptr = nullptr;
     int* col = nullptr;
     double* val = nullptr;
+    RowPiece* pieces = nullptr;  // separate allocation
+    int npieces = 0;
 };
 
 struct IntStore {
@@ -59,6 +72,10 @@ struct IntStore {
 namespace {
 
 constexpr int NBUCKET = 1024;  // row buckets of the term histogram (slabs are runs of buckets)
+#ifndef UGB_PIECE_MAX
+#define UGB_PIECE_MAX 4096
+#endif
+constexpr int PIECE_MAX = UGB_PIECE_MAX;  // elements per warp piece of a build
 
 __device__ __forceinline__ long long packed(int x, int y) {
     return x >= y ? (long long)x * (x + 1) / 2 + y : (long long)y * (y + 1) / 2 + x;
@@ -245,18 +262,18 @@ struct AddOp {
     __device__ __forceinline__ double operator()(double a, double b) const { return a + b; }
 };
 
-// Build: one warp per row of a slab.  MODE 0: RHF store, RHF build; 1: UHF store, RHF build;
-// 2: UHF store, UHF build.
+// Build: one warp per row piece of a slab (whole rows, and the pieces of long rows).  MODE 0: RHF
+// store, RHF build; 1: UHF store, RHF build; 2: UHF store, UHF build.
 template <int MODE>
-__global__ void __launch_bounds__(256) store_spmv(const int* __restrict__ rowptr, const int* __restrict__ col,
-                                                  const double* __restrict__ val, long long r0, int nrows, long long np,
+__global__ void __launch_bounds__(256) store_spmv(const RowPiece* __restrict__ pieces, int npieces, const int* __restrict__ col,
+                                                  const double* __restrict__ val, long long r0, long long np,
                                                   const double* __restrict__ Pa, const double* __restrict__ Pb,
                                                   double* __restrict__ Ga, double* __restrict__ Gb) {
     const int lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * (blockDim.x >> 5);
-    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nrows; w += nwarps) {
-        const int beg = rowptr[w], end = rowptr[w + 1];
-        const long long r = r0 + w;
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < npieces; w += nwarps) {
+        const RowPiece pc = pieces[w];
+        const long long r = r0 + pc.row;
         const bool krow = MODE != 0 && r >= np;
         double sa = 0.0, sb = 0.0;
         auto add = [&](double v, int c) {
@@ -271,7 +288,8 @@ __global__ void __launch_bounds__(256) store_spmv(const int* __restrict__ rowptr
                 sa = fma(v, __ldg(Pa + c), sa);
             }
         };
-        int k = beg + lane;
+        const int end = pc.end;
+        int k = pc.begin + lane;
         for (; k + 96 < end; k += 128) {  // four independent loads per lane in flight
             double v[4];
             int c[4];
@@ -291,7 +309,8 @@ __global__ void __launch_bounds__(256) store_spmv(const int* __restrict__ rowptr
         }
         if (lane != 0) continue;
         if constexpr (MODE == 0) {
-            Ga[r] += sa;
+            if (pc.whole) Ga[r] += sa;  // the row's one warp
+            else atomicAdd(Ga + r, sa);
         } else if constexpr (MODE == 1) {
             if (krow) atomicAdd(Ga + (r - np), sa);
             else atomicAdd(Ga + r, 2.0 * sa);
@@ -478,6 +497,26 @@ int assemble(IntStore* st, const UnomolRecord* d_rec, long long nrec, double bud
         st->bytes += (long long)bytes;
     }
     SCU(cudaStreamSynchronize(s));
+    // the warps' pieces of every slab, from its row offsets
+    for (StoreSlab& S : st->slabs) {
+        const int rows = (int)(S.r1 - S.r0);
+        std::vector<int> rp(rows + 1);
+        SCU(cudaMemcpy(rp.data(), S.rowptr, sizeof(int) * (rows + 1), cudaMemcpyDeviceToHost));
+        std::vector<RowPiece> pc;
+        for (int r = 0; r < rows; ++r) {
+            const int b = rp[r], e = rp[r + 1];
+            if (e <= b) continue;
+            const int n = (e - b + PIECE_MAX - 1) / PIECE_MAX;
+            for (int t = 0; t < n; ++t)
+                pc.push_back({r, b + (int)((long long)(e - b) * t / n), b + (int)((long long)(e - b) * (t + 1) / n), n == 1 ? 1 : 0});
+        }
+        S.npieces = (int)pc.size();
+        if (S.npieces) {
+            SCU(cudaMalloc(&S.pieces, sizeof(RowPiece) * pc.size()));
+            SCU(cudaMemcpy(S.pieces, pc.data(), sizeof(RowPiece) * pc.size(), cudaMemcpyHostToDevice));
+        }
+        st->bytes += (long long)(sizeof(RowPiece) * pc.size());
+    }
     return UNOMOL_OK;
 }
 
@@ -713,15 +752,14 @@ cudaError_t store_fock(const IntStore* st, const double* dPa, const double* dPb,
     if (uhf && st->kind != UNOMOL_STORE_UHF) return cudaErrorInvalidValue;
     const int mode = st->kind == UNOMOL_STORE_RHF ? 0 : (uhf ? 2 : 1);
     for (const StoreSlab& S : st->slabs) {
-        const int rows = (int)(S.r1 - S.r0);
-        if (rows <= 0) continue;
-        const unsigned blocks = (unsigned)((rows + 7) / 8);  // eight warps (rows) per CTA
+        if (S.npieces <= 0) continue;
+        const unsigned blocks = (unsigned)((S.npieces + 7) / 8);  // eight warps (pieces) per CTA
         if (mode == 0)
-            store_spmv<0><<<blocks, 256, 0, s>>>(S.rowptr, S.col, S.val, S.r0, rows, st->np, dPa, dPb, dGa, dGb);
+            store_spmv<0><<<blocks, 256, 0, s>>>(S.pieces, S.npieces, S.col, S.val, S.r0, st->np, dPa, dPb, dGa, dGb);
         else if (mode == 1)
-            store_spmv<1><<<blocks, 256, 0, s>>>(S.rowptr, S.col, S.val, S.r0, rows, st->np, dPa, dPb, dGa, dGb);
+            store_spmv<1><<<blocks, 256, 0, s>>>(S.pieces, S.npieces, S.col, S.val, S.r0, st->np, dPa, dPb, dGa, dGb);
         else
-            store_spmv<2><<<blocks, 256, 0, s>>>(S.rowptr, S.col, S.val, S.r0, rows, st->np, dPa, dPb, dGa, dGb);
+            store_spmv<2><<<blocks, 256, 0, s>>>(S.pieces, S.npieces, S.col, S.val, S.r0, st->np, dPa, dPb, dGa, dGb);
         ++*launches;
     }
     return cudaGetLastError();
@@ -745,8 +783,10 @@ void store_info(const IntStore* st, UnomolStoreInfo* out) {
 
 void store_free(IntStore* st) {
     if (!st) return;
-    for (StoreSlab& S : st->slabs)
+    for (StoreSlab& S : st->slabs) {
         if (S.mem) cudaFree(S.mem);
+        if (S.pieces) cudaFree(S.pieces);
+    }
     delete st;
 }
 
