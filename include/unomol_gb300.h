@@ -5,7 +5,8 @@
  * The reference computes every unique integral once in its constructor, stores them in a cache and
  * streams the cache on every formGmatrix call.  Here the constructor uploads the basis and builds
  * shell pairs and Schwarz bounds on the GPU; every formGmatrix call recomputes the integrals on the
- * GPU and contracts them directly into G (direct SCF: no integral store).
+ * GPU and contracts them directly into G (direct SCF), unless the context holds a store of the
+ * integrals (unomol_gpu_store_integrals below: the reference's conventional scheme, in device memory).
  *
  * Conventions (identical to the reference):
  *   - packed lower triangle, row major: element (i, j), j <= i, at i*(i+1)/2 + j, N*(N+1)/2 doubles;
@@ -327,7 +328,15 @@ typedef struct UnomolScfOptions {
     int loop;            /* UNOMOL_SCF_LOOP_GROUND: the loop of findEnergy (two updates, then the
                             convergence test; RHF.hpp:138-162); UNOMOL_SCF_LOOP_DPM: the loop of
                             findPolarizationPotential (one update, then the test; RHF.hpp:323-329) */
+    int density;         /* new density from F: UNOMOL_DENSITY_DIAG (default: eigen-solve, C_occ C_occ^T,
+                            RHF.hpp:178-203) or UNOMOL_DENSITY_SP2 (no reference counterpart: second-order
+                            spectral projection of X^T F X by matrix products, the same projector when a
+                            gap separates the occupied states; an iteration without that gap, and the
+                            final orbital energies, use the eigen-solve) */
 } UnomolScfOptions;
+
+#define UNOMOL_DENSITY_DIAG 0
+#define UNOMOL_DENSITY_SP2 1
 
 #define UNOMOL_SCF_LOOP_GROUND 0
 #define UNOMOL_SCF_LOOP_DPM 1
@@ -354,6 +363,8 @@ typedef struct UnomolScfResult {
     double seconds_fock;  /* Fock builds (host call to result on the host), */
     double seconds_diis;  /* DIIS error and extrapolation (+ level shift), */
     double seconds_diag;  /* diagonalisation and new density */
+    int sp2_steps;        /* UNOMOL_DENSITY_SP2: projection steps over the whole SCF */
+    int sp2_fallbacks;    /* UNOMOL_DENSITY_SP2: densities that needed the eigen-solve (no gap) */
 } UnomolScfResult;
 
 #define UNOMOL_GUESS_CORE 0

@@ -63,3 +63,39 @@ def test_diis_reaches_same_energy(gpu, name):
     r = native.scf(t, b, S=g["S"], H=g["H"], accel=native.SCF_DIIS, eps=1e-12, diis_tol=1e-8)
     assert r["converged"]
     assert abs(r["energy"] - float(g["scf_energy"])) <= 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_631g", "ethane_631g", "ref_b_dhdz", "propane_cation_sto3g", "water3_631g"])
+def test_sp2_density_reaches_the_same_energy(gpu, name):
+    """The density by second-order spectral projection (UNOMOL_DENSITY_SP2) in place of the eigen-solve:
+    the same converged energy as the eigen-solve path (1e-10 Eh), RHF and UHF, with the projection used
+    in (nearly) every iteration and orbital energies still returned."""
+    from unomol_gb300 import native
+    g = load_golden(name)
+    b = basis_of(g)
+    S, H = (g["S"], g["H"]) if "S" in g else native.one_electron(b)[0::2]
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, eps=1e-12, diis_tol=1e-8)
+    ref = native.scf(native.TwoElectronInts(b), b, **kw)
+    r = native.scf(native.TwoElectronInts(b), b, density=native.DENSITY_SP2, **kw)
+    assert r["converged"] and ref["converged"]
+    assert abs(r["energy"] - ref["energy"]) <= TOL_E, (r["energy"], ref["energy"])
+    assert r["sp2_steps"] > 0
+    assert r["sp2_fallbacks"] <= 2, r["sp2_fallbacks"]
+    assert np.abs(r["P"] - ref["P"]).max() <= 1e-6
+
+
+@pytest.mark.gpu
+def test_sp2_density_on_the_32_water_cluster(gpu):
+    """The bench workload: SP2 SCF of the 32-water cluster against the eigen-solve SCF."""
+    from unomol_gb300 import guess, molecules, native
+    from unomol_gb300.basis import Basis
+    b = Basis(text=molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10))
+    S, T, H = native.one_electron(b)
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, maxits=100, eps=1e-10, diis_tol=1e-7,
+              guess_P=guess.fragment_density(b))
+    t = native.TwoElectronInts(b)
+    ref = native.scf(t, b, **kw)
+    r = native.scf(t, b, density=native.DENSITY_SP2, **kw)
+    assert abs(r["energy"] - ref["energy"]) <= TOL_E
+    assert r["sp2_fallbacks"] == 0

@@ -18,6 +18,10 @@
 
 using namespace ugb;
 
+#ifndef UGB_BATCH_FUSE_MAXL
+#define UGB_BATCH_FUSE_MAXL 1  // classes with la+lb+lc+ld above this launch their two parts separately
+#endif
+
 namespace {
 
 template <int BC, int KC, typename R>
@@ -249,7 +253,15 @@ int batch_build(UnomolBatch* b, cudaStream_t s) {
             A32.dyn_count = b->d_cnt32 + L.bp_begin;
             A32.dyn_begin = b->d_begin32 + L.bp_begin;
             A32.dyn_total = b->d_total32 + k;
-            BCU(launch_fock_mixed(L.bc, L.kc, false, A, A32, b->nt, b->rys, b->rys32, ls[k & 1]));
+            if (pc_la(L.bc) + pc_lb(L.bc) + pc_la(L.kc) + pc_lb(L.kc) <= UGB_BATCH_FUSE_MAXL) {
+                BCU(launch_fock_mixed(L.bc, L.kc, false, A, A32, b->nt, b->rys, b->rys32, ls[k & 1]));
+            } else {
+                // as for one molecule: the heavier classes' FP64 part (four lanes per quartet) and FP32 part
+                // (persistent) as two kernels on the two streams, each at its own register count
+                BCU(launch_fock_fp64_part(L.bc, L.kc, false, A, A32, b->nt, b->rys, b->rys32, b->nsm * 8, ls[k & 1]));
+                A32.tile_counter = b->d_tiles + 2 * k + 1;
+                BCU(launch_persistent(L.bc, L.kc, A32, b->nt, b->rys32, b->nsm * L.ctas_per_sm, L.block, ls[(k + 1) & 1]));
+            }
             continue;
         }
         BCU(launch_persistent(L.bc, L.kc, A, b->nt, b->rys, b->nsm * L.ctas_per_sm, L.block, ls[0]));

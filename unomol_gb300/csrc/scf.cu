@@ -184,6 +184,161 @@ int diag_density(Dev& d, const std::vector<double>& Fpk, double* d_pk, int nocc,
     return UNOMOL_OK;
 }
 
+// ---- Density by second-order spectral projection (SP2; A. M. N. Niklasson, Phys. Rev. B 66, 155115
+// (2002)), in place of the eigen-solve ----
+// With F' = X^T F X scaled so that its spectrum lies in [0, 1] with the occupied (lowest) states near 1,
+// X_{k+1} = X_k^2 or 2 X_k - X_k^2, whichever brings tr X_{k+1} closer to nocc, converges to the
+// projector onto the nocc lowest eigenvectors of F' when a gap separates them from the rest; then
+// P = X P' X^T, the same density as C_occ C_occ^T.  Each step is one symmetric rank-n update (DSYRK, half
+// a DGEMM) at N = 416 instead of a cuSOLVER syevd.
+
+// Gershgorin bounds of a symmetric matrix (one block): out[0] = min_i (A_ii - r_i), out[1] = max_i (A_ii + r_i)
+__global__ void k_gershgorin(const double* __restrict__ A, int n, double* __restrict__ out) {
+    __shared__ double lo_s[256], hi_s[256];
+    double lo = 1e300, hi = -1e300;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double r = 0.0;
+        for (int j = 0; j < n; ++j)
+            if (j != i) r += fabs(A[(size_t)j * n + i]);
+        const double c = A[(size_t)i * n + i];
+        lo = fmin(lo, c - r);
+        hi = fmax(hi, c + r);
+    }
+    lo_s[threadIdx.x] = lo;
+    hi_s[threadIdx.x] = hi;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            lo_s[threadIdx.x] = fmin(lo_s[threadIdx.x], lo_s[threadIdx.x + o]);
+            hi_s[threadIdx.x] = fmax(hi_s[threadIdx.x], hi_s[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = lo_s[0];
+        out[1] = hi_s[0];
+    }
+}
+
+// X = (hi I - A) / (hi - lo), in place
+__global__ void k_sp2_start(double* __restrict__ A, int n, const double* __restrict__ bounds) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    const int i = (int)(t % n), j = (int)(t / n);
+    const double lo = bounds[0], hi = bounds[1];
+    A[t] = ((i == j ? hi : 0.0) - A[t]) / (hi - lo);
+}
+
+// One SP2 step's decision on the device (one block), so that steps follow each other without a host
+// round trip.  X2 = lower triangle of X^2 (DSYRK output).  st: [0] tr X, [1] square? (1/0), [2] and [3]
+// the idempotency errors tr X - tr X^2 of the last two steps, [4] converged (1/0), [5] steps taken,
+// [6] nocc.  Converged: the error is at rounding level (< 1e-9 n) and no longer falls (Niklasson's
+// stopping rule); from then on the steps change nothing.
+__global__ void k_sp2_decide(const double* __restrict__ X2, int n, double* __restrict__ st) {
+    __shared__ double s_[256];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += X2[(size_t)i * n + i];
+    s_[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s_[threadIdx.x] += s_[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0 || st[4] != 0.0) return;
+    const double tr = st[0], tr2 = s_[0], nocc = st[6];
+    const double e = tr - tr2;
+    if (st[5] >= 2.0 && e < 1e-9 * n && e >= st[3]) {
+        st[4] = 1.0;
+        st[1] = -1.0;  // no update
+        return;
+    }
+    const bool square = fabs(tr2 - nocc) < fabs(2.0 * tr - tr2 - nocc);
+    st[1] = square ? 1.0 : 0.0;
+    st[0] = square ? tr2 : 2.0 * tr - tr2;
+    st[3] = st[2];
+    st[2] = e;
+    st[5] += 1.0;
+}
+
+// X = X2 (square) or 2 X - X2 as st[1] says (nothing once converged), X2 the lower triangle of X^2
+__global__ void k_sp2_step(double* __restrict__ X, const double* __restrict__ X2, int n, const double* __restrict__ st) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    const double mode = st[1];
+    if (mode < 0.0) return;
+    const int r = (int)(t % n), c = (int)(t / n);
+    const double x2 = r >= c ? X2[(size_t)c * n + r] : X2[(size_t)r * n + c];
+    X[t] = mode > 0.5 ? x2 : 2.0 * X[t] - x2;
+}
+
+// tr X into st[0] (one block)
+__global__ void k_sp2_trace0(const double* __restrict__ X, int n, double* __restrict__ st, double nocc) {
+    __shared__ double s_[256];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += X[(size_t)i * n + i];
+    s_[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s_[threadIdx.x] += s_[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st[0] = s_[0];
+        st[1] = 0.0;
+        st[2] = st[3] = 1e300;
+        st[4] = 0.0;
+        st[5] = 0.0;
+        st[6] = nocc;
+    }
+}
+
+// F (packed, host) -> P packed (host) by SP2; ok = false (and P untouched) when it does not reach an
+// idempotent projector of trace nocc (no gap at the Fermi level): the caller then diagonalises.  The
+// steps run in chunks of SP2_CHUNK on the device; the host reads the state once per chunk.
+constexpr int SP2_CHUNK = 8;
+constexpr int SP2_MAX_STEPS = 120;
+
+int sp2_density(Dev& d, const std::vector<double>& Fpk, double* d_pk, int nocc, std::vector<double>& P, bool& ok,
+                int& steps) {
+    const int n = d.n;
+    const double one = 1.0, zero = 0.0;
+    ok = false;
+    steps = 0;
+    if (nocc <= 0 || nocc >= n) return UNOMOL_OK;
+    double* h = d.work;  // [0..1] spectral bounds, [8..14] the SP2 state (the eigen-solver workspace is free here)
+    if (d.lwork < 16) return UNOMOL_OK;
+    double* stt = h + 8;
+    CK(cudaMemcpyAsync(d_pk, Fpk.data(), Fpk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<blocks((long long)n * n), 256, 0, d.s>>>(d_pk, d.F, n);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.F, n, d.X, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, d.X, n, d.T1, n, &zero, d.W, n), UNOMOL_ECUDA);
+    k_gershgorin<<<1, 256, 0, d.s>>>(d.W, n, h);
+    k_sp2_start<<<blocks((long long)n * n), 256, 0, d.s>>>(d.W, n, h);
+    k_sp2_trace0<<<1, 256, 0, d.s>>>(d.W, n, stt, (double)nocc);
+    double state[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int done = 0; done < SP2_MAX_STEPS; done += SP2_CHUNK) {
+        for (int k = 0; k < SP2_CHUNK; ++k) {
+            CK(cublasDsyrk(d.cb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, n, &one, d.W, n, &zero, d.T1, n), UNOMOL_ECUDA);
+            k_sp2_decide<<<1, 256, 0, d.s>>>(d.T1, n, stt);
+            k_sp2_step<<<blocks((long long)n * n), 256, 0, d.s>>>(d.W, d.T1, n, stt);
+        }
+        CK(cudaMemcpyAsync(state, stt, sizeof(state), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+        CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+        if (state[4] != 0.0) break;
+    }
+    steps = (int)state[5];
+    if (!(state[4] != 0.0 && std::fabs(state[0] - nocc) < 1e-8)) return UNOMOL_OK;  // no projector: diagonalise
+    // P = X P' X^T
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.X, n, d.W, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, d.T1, n, d.X, n, &zero, d.C, n), UNOMOL_ECUDA);
+    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(d.C, d_pk, n);
+    P.resize((size_t)n * (n + 1) / 2);
+    CK(cudaMemcpyAsync(P.data(), d_pk, P.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    ok = true;
+    return UNOMOL_OK;
+}
+
 // ---- DIIS (Pulay) on the packed Fock matrices ----
 struct Diis {
     int maxv = 8;
@@ -421,6 +576,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     using clk = std::chrono::steady_clock;
     auto since = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
     double t_fock = 0.0, t_diis = 0.0, t_diag = 0.0;
+    int sp2_steps = 0, sp2_fallbacks = 0;
     const double t_setup = since(t0);
     const int maxits = opt->maxits > 0 ? opt->maxits : 300;
     const double eps = opt->eps;
@@ -534,13 +690,26 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
         const auto tg = clk::now();
         PoldA2 = PoldA;
         PoldA = Pa;
-        r = diag_density(d, Fa, d_pk, noccA, Pa, evA, nullptr);
+        // the density of F: SP2 when asked for (falls back to the eigen-solve without a gap), else syevd
+        auto density_of = [&](const std::vector<double>& F, int nocc, std::vector<double>& P, std::vector<double>& ev) -> int {
+            if (opt->density == UNOMOL_DENSITY_SP2) {
+                bool ok = false;
+                int st = 0;
+                const int rr = sp2_density(d, F, d_pk, nocc, P, ok, st);
+                if (rr) return rr;
+                sp2_steps += st;
+                if (ok) return UNOMOL_OK;
+                ++sp2_fallbacks;
+            }
+            return diag_density(d, F, d_pk, nocc, P, ev, nullptr);
+        };
+        r = density_of(Fa, noccA, Pa, evA);
         if (r) return r;
         pdiff = diffnorm_packed(Pa, PoldA, n);
         if (uhf) {
             PoldB2 = PoldB;
             PoldB = Pb;
-            r = diag_density(d, Fb, d_pk, noccB, Pb, evB, nullptr);
+            r = density_of(Fb, noccB, Pb, evB);
             if (r) return r;
             pdiff += diffnorm_packed(Pb, PoldB, n);
         }
@@ -587,6 +756,12 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     std::memcpy(P_io, Pa.data(), no2 * sizeof(double));
     if (uhf) std::memcpy(P_io + no2, Pb.data(), no2 * sizeof(double));
     if (orbital_energies) {
+        if (opt->density == UNOMOL_DENSITY_SP2) {  // the projection gives no eigenvalues: one eigen-solve
+            const auto tg = std::chrono::steady_clock::now();
+            if ((rc = diag_density(d, Fa, d_pk, noccA, tmp, evA, nullptr))) return fail(rc);
+            if (uhf && (rc = diag_density(d, Fb, d_pk, noccB, tmp, evB, nullptr))) return fail(rc);
+            t_diag += std::chrono::duration<double>(std::chrono::steady_clock::now() - tg).count();
+        }
         std::memcpy(orbital_energies, evA.data(), n * sizeof(double));
         if (uhf) std::memcpy(orbital_energies + n, evB.data(), n * sizeof(double));
     }
@@ -610,6 +785,8 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     res->seconds_fock = t_fock;
     res->seconds_diis = t_diis;
     res->seconds_diag = t_diag;
+    res->sp2_steps = sp2_steps;
+    res->sp2_fallbacks = sp2_fallbacks;
     res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return UNOMOL_OK;
 }

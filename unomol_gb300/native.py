@@ -291,7 +291,7 @@ class ScfOptions(C.Structure):
     _fields_ = [("maxits", C.c_int), ("eps", C.c_double), ("conv_type", C.c_int), ("accel", C.c_int),
                 ("guess", C.c_int), ("diis_size", C.c_int), ("diis_tol", C.c_double),
                 ("diis_start", C.c_double), ("level_shift", C.c_double), ("level_shift_until", C.c_double),
-                ("incremental", C.c_int), ("rebuild_every", C.c_int), ("loop", C.c_int)]
+                ("incremental", C.c_int), ("rebuild_every", C.c_int), ("loop", C.c_int), ("density", C.c_int)]
 
 
 class ScfResult(C.Structure):
@@ -303,7 +303,7 @@ class ScfResult(C.Structure):
                 ("densities", C.POINTER(C.c_double)), ("densities_cap", C.c_int), ("guess_used", C.c_int),
                 ("purify_iterations", C.c_int), ("purify_error", C.c_double), ("guess_trace", C.c_double),
                 ("seconds_setup", C.c_double), ("seconds_fock", C.c_double), ("seconds_diis", C.c_double),
-                ("seconds_diag", C.c_double)]
+                ("seconds_diag", C.c_double), ("sp2_steps", C.c_int), ("sp2_fallbacks", C.c_int)]
 
 
 class BatchScfResult(C.Structure):
@@ -312,6 +312,8 @@ class BatchScfResult(C.Structure):
                 ("ediff", C.c_double), ("pdiff", C.c_double)]
 
 
+DENSITY_DIAG = 0
+DENSITY_SP2 = 1
 SCF_DAMPED = 0
 SCF_DIIS = 2
 SCF_LOOP_GROUND, SCF_LOOP_DPM = 0, 1
@@ -380,10 +382,11 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
         maxits: int | None = None, eps: float | None = None, conv_type: int | None = None,
         diis_size: int = 8, diis_tol: float = 1e-6, record: int = 0, diis_start: float = 0.0,
         level_shift: float = 0.0, level_shift_until: float = 0.05, incremental: bool = False,
-        rebuild_every: int = 8, keep_densities: int = 0, purify: bool = False, loop: int = 0):
+        rebuild_every: int = 8, keep_densities: int = 0, purify: bool = False, loop: int = 0, density: int = 0):
     """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ...
     purify: start from guess_P after McWeeny purification and a trace check, or from the core
-    Hamiltonian when it fails them (out["guess_used"] says which)."""
+    Hamiltonian when it fails them (out["guess_used"] says which).  density: DENSITY_DIAG (eigen-solve)
+    or DENSITY_SP2 (second-order spectral projection, eigen-solve where it finds no gap)."""
     L = lib()
     L.unomol_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.POINTER(ScfOptions), C.POINTER(ScfResult),
                              _dp, C.c_void_p]
@@ -397,7 +400,7 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
                      conv_type if conv_type is not None else b.scf_flag[0], accel,
                      GUESS_CORE if guess_P is None else (GUESS_PURIFY if purify else GUESS_GIVEN),
                      diis_size, diis_tol, diis_start, level_shift, level_shift_until, 1 if incremental else 0,
-                     rebuild_every, loop)
+                     rebuild_every, loop, int(density))
     uhf = b.nelec % 2 == 1
     P = np.zeros(b.no2 * (2 if uhf else 1))
     if guess_P is not None:
@@ -418,7 +421,8 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
     out = {k: getattr(res, k) for k in ("energy", "e_electronic", "init_energy", "ediff", "pdiff", "diis_error",
                                         "seconds", "iterations", "converged", "fock_builds", "fock_ms",
                                         "purify_iterations", "purify_error", "guess_trace", "seconds_setup",
-                                        "seconds_fock", "seconds_diis", "seconds_diag")}
+                                        "seconds_fock", "seconds_diis", "seconds_diag", "sp2_steps",
+                                        "sp2_fallbacks")}
     out["guess_used"] = GUESS_USED.get(res.guess_used, str(res.guess_used))
     out["P"] = P
     out["orbital_energies"] = eps_orb
