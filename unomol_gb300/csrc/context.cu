@@ -702,7 +702,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
 #define UGB_FUSED_MIXED 1
 #endif
 #ifndef UGB_FUSE_MAXL
-#define UGB_FUSE_MAXL 1  // classes with la+lb+lc+ld above this run their two parts as separate kernels
+#define UGB_FUSE_MAXL 0  // classes with la+lb+lc+ld above this run their two parts as separate kernels
 #endif
     // mixed builds with both parts: the FP64 and FP32 parts of a templated class in one launch
     // (fock_jk_mixed), classes alternating over two equal-priority streams; otherwise the FP64 part on a

@@ -131,6 +131,36 @@ __device__ __forceinline__ void rys2_reference_regime(double T, double* x, doubl
     w[1] = w1;
 }
 
+// log2(1 / H) of the FP64 table's interval width H (a power of two)
+__host__ __device__ constexpr int rys_h_shift64() {
+    int sft = 0;
+    for (double h = RYS_H; h < 1.0; h *= 2.0) ++sft;
+    return sft;
+}
+static_assert(RYS_H * (1 << rys_h_shift64()) == 1.0, "the FP64 table interval is 2^-s");
+
+// Interval index k = floor(T / H) and local coordinate y = 2 (T / H - k) - 1 in [-1, 1) of the FP64
+// table, from the IEEE bits of T >= 0 with integer operations and one DFMA: T / H = 1.m x 2^E, k is the
+// integer part of the shifted mantissa, 1 + frac is the double whose mantissa field is the remaining bits,
+// and y = 2 (1 + frac) - 3 (exact).  Below one interval (E < 0) k = 0 and y = 2 T / H - 1.  Returns
+// T < tmax (compared as bit patterns; a NaN T compares above, as before).
+__device__ __forceinline__ bool rys_index64(double T, double tmax, int& k, double& y) {
+    constexpr int S = rys_h_shift64();
+    const long long u = __double_as_longlong(T);
+    const int E = (int)((u >> 52) & 0x7ff) - 1023 + S;  // exponent of T * 2^S
+    if (E < 0) {
+        k = 0;
+        y = fma(T, double(1 << (S + 1)), -1.0);
+    } else {
+        const long long M = (u & 0xfffffffffffffLL) | 0x10000000000000LL;
+        const int sh = 52 - min(E, 52);
+        k = (int)(M >> sh);
+        const long long fb = M & ((1LL << sh) - 1);
+        y = fma(2.0, __longlong_as_double(0x3ff0000000000000LL | (fb << (52 - sh))), -3.0);
+    }
+    return u < __double_as_longlong(tmax);
+}
+
 // Rys nodes x_r = t_r^2 and weights w_r at T (NR roots).  compat: reference-compatible two-root
 // regime (FP64 only; see rys2_reference_regime).
 template <int NR, typename R>
@@ -147,10 +177,20 @@ __device__ __forceinline__ void rys_roots(R T, const R* __restrict__ tab, R* x, 
             return;
         }
     }
-    if (T < TMAX) {
+    int k;
+    R y;
+    bool in_table;
+    if constexpr (sizeof(R) == 8) {
+        // FP64: the interval and the local coordinate from the bits of T on the integer pipe (the FP64
+        // pipe, 1/64 of the FP32 rate on this GPU, also runs compares and int/double conversions)
+        in_table = rys_index64(T, TMAX, k, y);
+    } else {
+        in_table = T < TMAX;
         const R Ts = T * R(1.0 / RysH<R>::value);  // intervals of width H (a power of two: exact)
-        const int k = (int)Ts;
-        const R y = R(2) * (Ts - R(k)) - R(1);
+        k = (int)Ts;
+        y = R(2) * (Ts - R(k)) - R(1);
+    }
+    if (in_table) {
         constexpr int ST = RysStride<R>::value;
         const R* c = tab + rys_off(NR, ST, RysH<R>::value) + k * (2 * NR * ST);
 #pragma unroll
