@@ -141,3 +141,27 @@ def test_fp64_part_runs_low_density_quartets_in_fp32(gpu, name):
         assert np.abs(G1 - G0).max() <= 1e-5 * np.abs(G0).max()
         moved.append(st["shell_quartets_demoted"])
     assert max(moved) > 0, moved
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["water3_631g", "h2o_cation_631g", "ref_631_co"])
+@pytest.mark.parametrize("cut", [1e-2, 1e-4])
+def test_mixed_uhf_both_parts(gpu, name, cut):
+    """UHF through both parts of the mixed build (the fused (ss|ss) launch, and the other classes' FP64
+    part on four lanes per quartet beside their FP32 kernel): Ga and Gb within FP32 accuracy of the
+    plain FP64 build, with the FP32 and FP64 parts both non-empty."""
+    from unomol_gb300 import native
+    g = load_golden(name)
+    t = native.TwoElectronInts(basis_of(g))
+    Ga0, Gb0 = t.form_g_uhf(g["Pa"], g["Pb"])
+    t.set_precision(native.PREC_MIXED, cut)
+    t.set_density_screening(1e-20)
+    t.set_counting(True)
+    Ga1, Gb1 = t.form_g_uhf(g["Pa"], g["Pb"])
+    st = t.stats()
+    assert st["shell_quartets_fp32"] < st["shell_quartets"]
+    if cut >= 1e-2:
+        assert st["shell_quartets_fp32"] > 0
+    scale = max(np.abs(Ga0).max(), np.abs(Gb0).max())
+    err = max(np.abs(Ga1 - Ga0).max(), np.abs(Gb1 - Gb0).max())
+    assert err <= 1e-5 * scale, err
