@@ -92,8 +92,12 @@ def test_records_match_the_oracle_records(gpu, name, tmp_path):
     ko = _key(ijkl[:, 0], ijkl[:, 1], ijkl[:, 2], ijkl[:, 3], b.norb)
     _, ig, io = np.intersect1d(kg, ko, return_indices=True)
     assert np.abs(rec["val"][ig] - val[io]).max() <= TOL_VAL
-    assert np.all(np.abs(np.delete(rec["val"], ig)) < 1.01 * CUT)
-    assert np.all(np.abs(np.delete(val, io)) < 1.01 * CUT)
+    # labels on one side only lie at the storage cut: the restatement, compiled here with the host's own
+    # contraction of products into FMAs, rounds integrals of 1e-14 differently (up to 25 % of the cut
+    # on one machine seen), and those fall on either side of it
+    assert np.all(np.abs(np.delete(rec["val"], ig)) < 1.5 * CUT)
+    assert np.all(np.abs(np.delete(val, io)) < 1.5 * CUT)
+    assert len(rec) + len(val) - 2 * len(ig) <= max(10, len(val) // 10000)
 
 
 @pytest.mark.gpu
