@@ -704,16 +704,17 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
 #ifndef UGB_FUSE_MAXL
 #define UGB_FUSE_MAXL 0  // classes with la+lb+lc+ld above this run their two parts as separate kernels
 #endif
-    // mixed builds with both parts: the FP64 and FP32 parts of a templated class in one launch
-    // (fock_jk_mixed), classes alternating over two equal-priority streams; otherwise the FP64 part on a
-    // high-priority stream and the FP32 part on a second one
+    // mixed builds: the FP64 work (the FP64-part kernels, and (ss|ss) with both parts in one launch,
+    // fock_jk_mixed) on a high-priority stream, the FP32 kernels on a second one, so that the FP64 CTAs
+    // take the SMs first and the FP32 CTAs fill the rest (213 vs 206 builds/s with the classes alternating
+    // over two equal-priority streams); plain builds alternate their classes over two streams
     const bool split = mixed && ctx->fp32_cut > ctx->skip_cut;
     const bool fused = split && UGB_FUSED_MIXED && ctx->eri_method != UNOMOL_ERI_MD;
     cudaStream_t ls[2] = {s, s};  // streams of the FP64 and FP32 launches (plain builds: alternate classes)
     if (!ctx->counting) {
         CU(cudaEventRecord(ctx->fork, s));
-        ls[0] = ctx->part_stream[mixed && !fused ? 0 : 1];
-        ls[1] = ctx->part_stream[mixed && !fused ? 1 : 2];
+        ls[0] = ctx->part_stream[mixed ? 0 : 1];
+        ls[1] = ctx->part_stream[mixed ? 1 : 2];
         for (int k = 0; k < 2; ++k) CU(cudaStreamWaitEvent(ls[k], ctx->fork, 0));
     }
     auto launch_class = [&](const ClassLaunch& L, bool fp32, bool side = false) -> cudaError_t {
@@ -747,15 +748,15 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                 A32.dyn_total = ctx->d_total32 + li;
                 A32.counter_base += ncls * 32;
                 if (lsum <= UGB_FUSE_MAXL) {
-                    CU(launch_fock_mixed(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ls[li & 1]));
+                    CU(launch_fock_mixed(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ls[0]));
                     ++launches;
                 } else {
                     // classes whose FP32 code needs far fewer registers than their FP64 code: the FP64 part
                     // (four lanes per quartet) and the FP32 part as two kernels on the two streams, each
                     // at its own register count
                     CU(launch_fock_fp64_part(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ctx->nsm * 8,
-                                             ls[li & 1]));
-                    CU(launch_class_kernel(ctx, L, uhf, true, A32, ls[(li + 1) & 1]));
+                                             ls[0]));
+                    CU(launch_class_kernel(ctx, L, uhf, true, A32, ls[1]));
                     launches += 2;
                 }
                 continue;
