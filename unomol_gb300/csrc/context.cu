@@ -702,12 +702,12 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
 #define UGB_FUSED_MIXED 1
 #endif
 #ifndef UGB_FUSE_MAXL
-#define UGB_FUSE_MAXL 0  // classes with la+lb+lc+ld above this run their two parts as separate kernels
-#endif
-    // mixed builds: the FP64 work (the FP64-part kernels, and (ss|ss) with both parts in one launch,
-    // fock_jk_mixed) on a high-priority stream, the FP32 kernels on a second one, so that the FP64 CTAs
-    // take the SMs first and the FP32 CTAs fill the rest (213 vs 206 builds/s with the classes alternating
-    // over two equal-priority streams); plain builds alternate their classes over two streams
+#define UGB_FUSE_MAXL -1  // classes with la+lb+lc+ld above this run their two parts as separate kernels
+#endif                    // (-1: every class; the batched build keeps fused launches for (ss|ss), (ps|ss))
+    // mixed builds: the FP64-part kernels on a high-priority stream, the FP32 kernels on a second one, so
+    // that the FP64 CTAs take the SMs first and the FP32 CTAs fill the rest (213 vs 206 builds/s with the
+    // classes alternating over two equal-priority streams); plain builds alternate their classes over two
+    // streams
     const bool split = mixed && ctx->fp32_cut > ctx->skip_cut;
     const bool fused = split && UGB_FUSED_MIXED && ctx->eri_method != UNOMOL_ERI_MD;
     cudaStream_t ls[2] = {s, s};  // streams of the FP64 and FP32 launches (plain builds: alternate classes)
