@@ -8,8 +8,12 @@
 // DPM / finite-field paths stay as they are.
 //
 // Differences a caller can observe:
-//   * no integral store: the constructor builds shell pairs and Schwarz bounds on the GPU, and every
-//     formGmatrix recomputes the integrals (direct SCF); `label` (the cache file name) is unused;
+//   * no integral store by default: the constructor builds shell pairs and Schwarz bounds on the GPU,
+//     and every formGmatrix recomputes the integrals (direct SCF); `label` (the cache file name) is
+//     unused.  The reference's conventional scheme is one call away:
+//     unomol_gpu_store_integrals(context(), UNOMOL_STORE_UHF, 0.0) keeps every integral in device
+//     memory and later formGmatrix calls stream it; unomol_gpu_write_records writes the records in
+//     the layout of the reference's integral file;
 //   * directFormGMatrix is exact (the reference's variant drops pairs with |AB|^2 > 20 bohr^2,
 //     TwoElectronInts.cpp:920,961);
 //   * errors end the program through the reference's convention (message on stderr, exit(EXIT_FAILURE),
