@@ -754,7 +754,7 @@ int fock_device(UnomolCtx* ctx, const double* dPa, const double* dPb, double* dG
                     // classes whose FP32 code needs far fewer registers than their FP64 code: the FP64 part
                     // (four lanes per quartet) and the FP32 part as two kernels on the two streams, each
                     // at its own register count
-                    CU(launch_fock_fp64_part(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ctx->nsm * 8,
+                    CU(launch_fock_fp64_part(L.bc, L.kc, uhf, A, A32, ctx->nt, ctx->d_rys, ctx->d_rys32, ctx->nsm * 4,
                                              ls[0]));
                     CU(launch_class_kernel(ctx, L, uhf, true, A32, ls[1]));
                     launches += 2;
@@ -1095,9 +1095,22 @@ int unomol_gpu_recalculate(UnomolCtx* ctx, const double* centers) {
     return unomol_gpu_store_integrals(ctx, kind, max_gib);
 }
 
+// The context's device current for the length of a call, the caller's restored after it.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 int unomol_gpu_store_integrals(UnomolCtx* ctx, int kind, double max_gib) {
     if (!ctx) return fail(ctx, UNOMOL_EINVAL, "null context");
-    CU(cudaSetDevice(ctx->dev));
+    DeviceScope scope(ctx->dev);
     IntStore* st = nullptr;
     std::string err;
     const int rc = store_from_integrals(ctx_view(ctx), kind, max_gib, &st, err);
@@ -1109,7 +1122,7 @@ int unomol_gpu_store_integrals(UnomolCtx* ctx, int kind, double max_gib) {
 
 int unomol_gpu_store_records(UnomolCtx* ctx, const char* path, int kind, double max_gib) {
     if (!ctx || !path) return fail(ctx, UNOMOL_EINVAL, "null argument");
-    CU(cudaSetDevice(ctx->dev));
+    DeviceScope scope(ctx->dev);
     IntStore* st = nullptr;
     std::string err;
     const int rc = store_from_file(ctx_view(ctx), path, kind, max_gib, &st, err);
@@ -1137,7 +1150,7 @@ int unomol_gpu_store_info(const UnomolCtx* ctx, UnomolStoreInfo* out) {
 
 int unomol_gpu_write_records(UnomolCtx* ctx, const char* path, int64_t* count) {
     if (!ctx || !path || !count) return fail(ctx, UNOMOL_EINVAL, "null argument");
-    CU(cudaSetDevice(ctx->dev));
+    DeviceScope scope(ctx->dev);
     long long n = 0;
     std::string err;
     const int rc = write_records(ctx_view(ctx), path, &n, err);
