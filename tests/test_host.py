@@ -197,3 +197,13 @@ def test_batch_workload_generator():
     nbf = [Basis(text=t).norb for _, t in work]
     assert min(nbf) >= 7 and max(nbf) <= 108 and sum(nbf) == 11246
     assert [l for l, _ in molecules.batch_workload(seed=0)] == labels
+
+
+def test_record_layout_is_the_reference_twoints():
+    """The integral records of the conventional build are the reference's TwoInts (TwoElectronInts.hpp:20-23):
+    a double and four ints, 24 bytes, the header's UnomolRecord."""
+    from unomol_gb300 import native
+    assert native.RECORD_DTYPE.itemsize == 24
+    assert [native.RECORD_DTYPE.fields[k][1] for k in ("val", "i", "j", "k", "l")] == [0, 8, 12, 16, 20]
+    txt = open(os.path.join(ROOT, "include", "unomol_gb300.h")).read()
+    assert "double val;\n    int32_t i, j, k, l;\n} UnomolRecord;" in txt
