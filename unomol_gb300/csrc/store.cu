@@ -394,7 +394,8 @@ int assemble(IntStore* st, const UnomolRecord* d_rec, long long nrec, double bud
     const double avail = budget - used;
     unsigned long long cap = (unsigned long long)std::max(0.0, avail / 2.0 / 24.0);
     cap = std::min<unsigned long long>(std::max(cap, biggest), std::max<unsigned long long>(total, 1));
-    cap = std::min<unsigned long long>(cap, (unsigned long long)INT_MAX);  // CUB item counts are int
+    // CUB item counts are int; the build's element indices (int) step past a slab's end by < 128
+    cap = std::min<unsigned long long>(cap, (unsigned long long)INT_MAX - 1024ull);
     if (biggest > cap) {
         err = "stored build: a row bucket of " + std::to_string(biggest) + " terms exceeds one sort (2^31 items)";
         return UNOMOL_EINVAL;
