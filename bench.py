@@ -564,7 +564,9 @@ def run_ours(args):
                        "shell_quartets_per_build": [int(x) for x in nq], "fp32_shell_quartets_per_build": [int(x) for x in nq32],
                        "screened_shell_quartets_per_build": [int(x) for x in nscr],
                        "fp32_shell_quartets_of_fp64_lists_per_build": [int(x) for x in ndem]},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * b.no2, "d2h_bytes_per_step": 8 * b.no2},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * b.no2, "d2h_bytes_per_step": 8 * b.no2,
+                    "note": "formGmatrix on pinned host P and G, called back to back as an SCF calls it: no L2 "
+                            "flush between calls (the value's device-timed builds each follow a 256 MiB flush)"},
             "roofline": {"bound": "fp64+fp32 pipes", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": profile_traffic(args.form),
                          "kernel": "fock_jk_kernel (all class instances and both precisions of a build)",
