@@ -513,6 +513,21 @@ def run_ours(args):
                         "note": "the value's build sequence, density skip cutoff as the value's, FP32 off: "
                                 "fp32_gain = value / this, incremental_gain = this / plain_fp64"}
     inc64.close()
+    # the same SCFs with pseudo-diagonalisation steps in place of most eigen-solves (the eigen-solve of
+    # cuSOLVER takes ~12 ms at this size, more than a mixed Fock build)
+    p64 = native.scf(plain, b, density=native.DENSITY_PSEUDO, **kw)
+    pm = (native.scf(mixed, b, incremental=True, rebuild_every=REBUILD, density=native.DENSITY_PSEUDO, **kw)
+          if args.form == "mixed" else p64)
+    scf_pseudo = {"energy_plain_fp64": p64["energy"], "energy_form": pm["energy"],
+                  "abs_dE_vs_plain_fp64_eigen_solve": abs(pm["energy"] - r64["energy"]),
+                  "iterations_plain": p64["iterations"], "iterations_form": pm["iterations"],
+                  "pseudo_steps_plain": p64["pseudo_steps"], "pseudo_steps_form": pm["pseudo_steps"],
+                  "converged": bool(p64["converged"] and pm["converged"]),
+                  "scf_wall_s_plain_fp64": p64["seconds"], "scf_wall_s_form": pm["seconds"],
+                  "speedup_of_form": p64["seconds"] / pm["seconds"],
+                  "phases_s_form": {k: pm["seconds_" + k] for k in ("setup", "fock", "diis", "diag")},
+                  "note": "UNOMOL_DENSITY_PSEUDO: first density of each spin, large rotations and the final "
+                          "orbital energies by the eigen-solve, every other density by a pseudo-diagonalisation step"}
     stored = None
     if args.form == "mixed" and not args.no_store:
         stored = stored_form(b, kw, r64, plain, rm["densities"], dev, stream, flush, args.steps)
@@ -592,6 +607,7 @@ def run_ours(args):
                     "fock_ms_plain_fp64": r64["fock_ms"], "fock_ms_form": rm["fock_ms"], "guess_s": t_guess,
                     "phases_s_plain_fp64": {k: r64["seconds_" + k] for k in ("setup", "fock", "diis", "diag")},
                     "phases_s_form": {k: rm["seconds_" + k] for k in ("setup", "fock", "diis", "diag")}},
+            "scf_pseudo_diag": scf_pseudo,
             "scatter": {"algorithmic_bytes_per_build": scatter_bytes / args.steps, "achieved_gbs": scatter_gbs,
                         "hbm_gbs": hbm, "frac_of_hbm": scatter_gbs / hbm if hbm else None,
                         "l2_read_gbs": l2_read, "frac_of_l2_read": scatter_gbs / l2_read,

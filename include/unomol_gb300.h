@@ -329,14 +329,19 @@ typedef struct UnomolScfOptions {
                             convergence test; RHF.hpp:138-162); UNOMOL_SCF_LOOP_DPM: the loop of
                             findPolarizationPotential (one update, then the test; RHF.hpp:323-329) */
     int density;         /* new density from F: UNOMOL_DENSITY_DIAG (default: eigen-solve, C_occ C_occ^T,
-                            RHF.hpp:178-203) or UNOMOL_DENSITY_SP2 (no reference counterpart: second-order
+                            RHF.hpp:178-203), UNOMOL_DENSITY_SP2 (no reference counterpart: second-order
                             spectral projection of X^T F X by matrix products, the same projector when a
                             gap separates the occupied states; an iteration without that gap, and the
-                            final orbital energies, use the eigen-solve) */
+                            final orbital energies, use the eigen-solve) or UNOMOL_DENSITY_PSEUDO (no
+                            reference counterpart: pseudo-diagonalisation, the occupied-virtual block of F
+                            in the last orbitals rotated away to first order by matrix products; the
+                            eigen-solve for the first density of each spin, for steps with a rotation
+                            above 0.2 or a gap below 1e-3 Eh, and for the final orbital energies) */
 } UnomolScfOptions;
 
 #define UNOMOL_DENSITY_DIAG 0
 #define UNOMOL_DENSITY_SP2 1
+#define UNOMOL_DENSITY_PSEUDO 2
 
 #define UNOMOL_SCF_LOOP_GROUND 0
 #define UNOMOL_SCF_LOOP_DPM 1
@@ -365,6 +370,7 @@ typedef struct UnomolScfResult {
     double seconds_diag;  /* diagonalisation and new density */
     int sp2_steps;        /* UNOMOL_DENSITY_SP2: projection steps over the whole SCF */
     int sp2_fallbacks;    /* UNOMOL_DENSITY_SP2: densities that needed the eigen-solve (no gap) */
+    int pseudo_steps;     /* UNOMOL_DENSITY_PSEUDO: densities by the pseudo-diagonalisation step */
 } UnomolScfResult;
 
 #define UNOMOL_GUESS_CORE 0

@@ -99,3 +99,49 @@ def test_sp2_density_on_the_32_water_cluster(gpu):
     r = native.scf(t, b, density=native.DENSITY_SP2, **kw)
     assert abs(r["energy"] - ref["energy"]) <= TOL_E
     assert r["sp2_fallbacks"] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["h2o_631g", "ethane_631g", "ref_b_dhdz", "propane_cation_sto3g", "water3_631g",
+                                  "h2o_cation_631g"])
+def test_pseudo_density_reaches_the_same_energy(gpu, name):
+    """Pseudo-diagonalisation (UNOMOL_DENSITY_PSEUDO: the occupied-virtual block of F in the last orbitals
+    rotated away by matrix products) in place of most eigen-solves: the same converged energy as the
+    eigen-solve path (1e-10 Eh), RHF and UHF, the same density, and the orbital energies of the final F."""
+    from unomol_gb300 import native
+    g = load_golden(name)
+    b = basis_of(g)
+    S, H = (g["S"], g["H"]) if "S" in g else native.one_electron(b)[0::2]
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, eps=1e-12, diis_tol=1e-8)
+    ref = native.scf(native.TwoElectronInts(b), b, **kw)
+    r = native.scf(native.TwoElectronInts(b), b, density=native.DENSITY_PSEUDO, **kw)
+    assert r["converged"] and ref["converged"]
+    assert abs(r["energy"] - ref["energy"]) <= TOL_E, (r["energy"], ref["energy"])
+    assert r["pseudo_steps"] > 0
+    assert r["iterations"] <= ref["iterations"] + 6, (r["iterations"], ref["iterations"])
+    assert np.abs(r["P"] - ref["P"]).max() <= 1e-6
+    assert np.abs(r["orbital_energies"] - ref["orbital_energies"]).max() <= 1e-6
+
+
+@pytest.mark.gpu
+def test_pseudo_density_on_the_32_water_cluster(gpu):
+    """The bench workload: pseudo-diagonalisation SCF of the 32-water cluster (plain FP64 builds and the
+    mixed incremental form) against the eigen-solve SCF."""
+    from unomol_gb300 import guess, molecules, native
+    from unomol_gb300.basis import Basis
+    b = Basis(text=molecules.patin_text(molecules.water_cluster(32, 0), "6-31G", eps=1e-10))
+    S, T, H = native.one_electron(b)
+    kw = dict(S=S, H=H, accel=native.SCF_DIIS, maxits=100, eps=1e-10, diis_tol=1e-7,
+              guess_P=guess.fragment_density(b))
+    t = native.TwoElectronInts(b)
+    ref = native.scf(t, b, **kw)
+    r = native.scf(t, b, density=native.DENSITY_PSEUDO, **kw)
+    assert r["converged"]
+    assert abs(r["energy"] - ref["energy"]) <= TOL_E
+    assert r["pseudo_steps"] >= r["iterations"] // 2, (r["pseudo_steps"], r["iterations"])
+    m = native.TwoElectronInts(b)
+    m.set_precision(native.PREC_MIXED, 1e-3)
+    m.set_density_screening(1e-13)
+    rm = native.scf(m, b, density=native.DENSITY_PSEUDO, incremental=True, rebuild_every=8, **kw)
+    assert rm["converged"]
+    assert abs(rm["energy"] - ref["energy"]) <= 1e-7

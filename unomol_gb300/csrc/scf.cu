@@ -339,6 +339,112 @@ int sp2_density(Dev& d, const std::vector<double>& Fpk, double* d_pk, int nocc, 
     return UNOMOL_OK;
 }
 
+// ---- Density by pseudo-diagonalisation (J. J. P. Stewart, P. Csaszar, P. Pulay, J. Comput. Chem. 3,
+// 227 (1982)), in place of the eigen-solve once the orbitals change little ----
+// W holds the orbitals of the last step in the orthonormal basis (columns; the nocc occupied first).
+// In those orbitals F_mo = W^T X^T F X W is nearly diagonal; its occupied-virtual block is rotated away
+// to first order, theta_ai = F_ai / (e_i - e_a) with e the diagonal of F_mo, by W <- W exp(A) (A the
+// antisymmetric generator, exp to second order, then Newton-Schulz re-orthonormalisation), all by
+// matrix products.  At self-consistency F_ai -> 0, so the density converges to the projector of F; a
+// step whose rotation is large or whose occupied and virtual levels come close takes the eigen-solve.
+constexpr double PSEUDO_MAX_THETA = 0.2;  // largest |theta| of a step (else the eigen-solve)
+constexpr double PSEUDO_MIN_GAP = 1e-3;   // smallest e_a - e_i (Eh) of a step (else the eigen-solve)
+
+// A (n x n, column-major) = the generator of the occupied-virtual rotation of Fmo; st[0] = max |theta|,
+// st[1] = min e_virtual - max e_occupied (one block)
+__global__ void k_pseudo_gen(const double* __restrict__ Fmo, int n, int nocc, double* __restrict__ A, double* __restrict__ st) {
+    __shared__ double s_th[256], s_eo[256], s_ev[256];
+    double th = 0.0, eo = -1e300, ev = 1e300;
+    for (long long t = threadIdx.x; t < (long long)n * n; t += blockDim.x) {
+        const int r = (int)(t % n), c = (int)(t / n);
+        double v = 0.0;
+        if (r >= nocc && c < nocc) {  // theta_rc, r virtual, c occupied
+            v = Fmo[t] / (Fmo[(size_t)c * n + c] - Fmo[(size_t)r * n + r]);
+            th = fmax(th, fabs(v));
+        } else if (r < nocc && c >= nocc) {
+            v = -Fmo[(size_t)r * n + c] / (Fmo[(size_t)r * n + r] - Fmo[(size_t)c * n + c]);
+        }
+        A[t] = v;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double e = Fmo[(size_t)i * n + i];
+        if (i < nocc) eo = fmax(eo, e);
+        else ev = fmin(ev, e);
+    }
+    s_th[threadIdx.x] = th;
+    s_eo[threadIdx.x] = eo;
+    s_ev[threadIdx.x] = ev;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s_th[threadIdx.x] = fmax(s_th[threadIdx.x], s_th[threadIdx.x + o]);
+            s_eo[threadIdx.x] = fmax(s_eo[threadIdx.x], s_eo[threadIdx.x + o]);
+            s_ev[threadIdx.x] = fmin(s_ev[threadIdx.x], s_ev[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st[0] = s_th[0];
+        st[1] = s_ev[0] - s_eo[0];
+    }
+}
+
+// M = a I + b A + c M, in place on M (column-major n x n)
+__global__ void k_axpy_ident(double* __restrict__ M, const double* __restrict__ A, int n, double a, double b, double c) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    const bool diag = (t % n) == (t / n);
+    M[t] = (diag ? a : 0.0) + (A ? b * A[t] : 0.0) + c * M[t];
+}
+
+// F (packed, host) -> P packed (host) by one pseudo-diagonalisation step on the orbitals Ws (updated in
+// place); ok = false (P and Ws untouched) when the step is too large or the gap too small: the caller
+// then takes the eigen-solve.
+int pseudo_density(Dev& d, double* Ws, const std::vector<double>& Fpk, double* d_pk, int nocc, std::vector<double>& P,
+                   bool& ok) {
+    const int n = d.n;
+    const double one = 1.0, zero = 0.0;
+    ok = false;
+    if (nocc <= 0 || nocc >= n || d.lwork < 48) return UNOMOL_OK;
+    double* st = d.work + 32;  // the eigen-solver workspace is free here
+    const unsigned nb = blocks((long long)n * n);
+    CK(cudaMemcpyAsync(d_pk, Fpk.data(), Fpk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
+    k_unpack<<<nb, 256, 0, d.s>>>(d_pk, d.F, n);
+    // F' = X^T F X (C), F_mo = Ws^T F' Ws (F)
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.F, n, d.X, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, d.X, n, d.T1, n, &zero, d.C, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.C, n, Ws, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, Ws, n, d.T1, n, &zero, d.F, n), UNOMOL_ECUDA);
+    k_pseudo_gen<<<1, 256, 0, d.s>>>(d.F, n, nocc, d.T1, st);
+    double h[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(h, st, sizeof(h), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    if (!(h[0] <= PSEUDO_MAX_THETA && h[1] >= PSEUDO_MIN_GAP)) return UNOMOL_OK;
+    // M = I + A + A^2 / 2 (W), C = Ws M
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.T1, n, d.T1, n, &zero, d.W, n), UNOMOL_ECUDA);
+    k_axpy_ident<<<nb, 256, 0, d.s>>>(d.W, d.T1, n, 1.0, 1.0, 0.5);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, Ws, n, d.W, n, &zero, d.C, n), UNOMOL_ECUDA);
+    // Newton-Schulz: Ws = C (3 I - C^T C) / 2; C^T C = I + O(theta^3), twice for the larger steps
+    const int ns = h[0] > 1e-2 ? 2 : 1;
+    for (int k = 0; k < ns; ++k) {
+        double* src = k == 0 ? d.C : Ws;
+        double* dst = k == 0 ? Ws : d.C;
+        CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, src, n, src, n, &zero, d.W, n), UNOMOL_ECUDA);
+        k_axpy_ident<<<nb, 256, 0, d.s>>>(d.W, nullptr, n, 1.5, 0.0, -0.5);
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, src, n, d.W, n, &zero, dst, n), UNOMOL_ECUDA);
+    }
+    if (ns == 2) CK(cudaMemcpyAsync(Ws, d.C, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, d.s), UNOMOL_ECUDA);
+    // C = X Ws, P = C_occ C_occ^T
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.X, n, Ws, n, &zero, d.C, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &one, d.C, n, d.C, n, &zero, d.T1, n), UNOMOL_ECUDA);
+    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(d.T1, d_pk, n);
+    P.resize((size_t)n * (n + 1) / 2);
+    CK(cudaMemcpyAsync(P.data(), d_pk, P.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
+    CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
+    ok = true;
+    return UNOMOL_OK;
+}
+
 // ---- DIIS (Pulay) on the packed Fock matrices ----
 struct Diis {
     int maxv = 8;
@@ -522,10 +628,11 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     } sg{s};
     int rc = dev_init(d, n, s);
     double *d_pk = nullptr, *d_P = nullptr, *d_G = nullptr, *d_Pb = nullptr, *d_Gb = nullptr, *d_S = nullptr;
+    double* d_Ws[2] = {nullptr, nullptr};  // pseudo-diagonalisation: the orbitals of each spin (orthonormal basis)
     struct Bufs {
-        double** p[6];
+        double** p[8];
         ~Bufs() { for (auto q : p) if (*q) cudaFree(*q); }
-    } bufs{{&d_pk, &d_P, &d_G, &d_Pb, &d_Gb, &d_S}};
+    } bufs{{&d_pk, &d_P, &d_G, &d_Pb, &d_Gb, &d_S, &d_Ws[0], &d_Ws[1]}};
     auto fail = [&](int code) {
         res->status = code;
         std::snprintf(res->message, sizeof(res->message), "%s", d.err.c_str());
@@ -538,6 +645,14 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
         d.err = "device allocation failed";
         return fail(UNOMOL_ENOMEM);
     }
+    const bool pseudo = opt->density == UNOMOL_DENSITY_PSEUDO;
+    if (pseudo && (cudaMalloc(&d_Ws[0], (size_t)n * n * sizeof(double)) ||
+                   (uhf && cudaMalloc(&d_Ws[1], (size_t)n * n * sizeof(double))))) {
+        d.err = "device allocation failed";
+        return fail(UNOMOL_ENOMEM);
+    }
+    bool have_orbitals[2] = {false, false};
+    int pseudo_steps = 0;
     std::vector<double> S(in->S, in->S + no2), H(in->H, in->H + no2);
     rc = form_x(d, S, d_pk);
     if (rc) return fail(rc);
@@ -690,8 +805,10 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
         const auto tg = clk::now();
         PoldA2 = PoldA;
         PoldA = Pa;
-        // the density of F: SP2 when asked for (falls back to the eigen-solve without a gap), else syevd
-        auto density_of = [&](const std::vector<double>& F, int nocc, std::vector<double>& P, std::vector<double>& ev) -> int {
+        // the density of F: SP2 or a pseudo-diagonalisation step when asked for (each falls back to the
+        // eigen-solve: no gap, a large rotation, no orbitals yet), else syevd
+        auto density_of = [&](int spin, const std::vector<double>& F, int nocc, std::vector<double>& P,
+                              std::vector<double>& ev) -> int {
             if (opt->density == UNOMOL_DENSITY_SP2) {
                 bool ok = false;
                 int st = 0;
@@ -701,15 +818,32 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
                 if (ok) return UNOMOL_OK;
                 ++sp2_fallbacks;
             }
-            return diag_density(d, F, d_pk, nocc, P, ev, nullptr);
+            if (pseudo && have_orbitals[spin]) {
+                bool ok = false;
+                const int rr = pseudo_density(d, d_Ws[spin], F, d_pk, nocc, P, ok);
+                if (rr) return rr;
+                if (ok) {
+                    ++pseudo_steps;
+                    return UNOMOL_OK;
+                }
+            }
+            const int rr = diag_density(d, F, d_pk, nocc, P, ev, nullptr);
+            if (!rr && pseudo) {  // the eigenvectors (orthonormal basis) start the next pseudo step
+                if (cudaMemcpyAsync(d_Ws[spin], d.W, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+                    d.err = "orbital copy failed";
+                    return UNOMOL_ECUDA;
+                }
+                have_orbitals[spin] = true;
+            }
+            return rr;
         };
-        r = density_of(Fa, noccA, Pa, evA);
+        r = density_of(0, Fa, noccA, Pa, evA);
         if (r) return r;
         pdiff = diffnorm_packed(Pa, PoldA, n);
         if (uhf) {
             PoldB2 = PoldB;
             PoldB = Pb;
-            r = density_of(Fb, noccB, Pb, evB);
+            r = density_of(1, Fb, noccB, Pb, evB);
             if (r) return r;
             pdiff += diffnorm_packed(Pb, PoldB, n);
         }
@@ -756,7 +890,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     std::memcpy(P_io, Pa.data(), no2 * sizeof(double));
     if (uhf) std::memcpy(P_io + no2, Pb.data(), no2 * sizeof(double));
     if (orbital_energies) {
-        if (opt->density == UNOMOL_DENSITY_SP2) {  // the projection gives no eigenvalues: one eigen-solve
+        if (opt->density == UNOMOL_DENSITY_SP2 || pseudo) {  // no eigenvalues from those steps: one eigen-solve
             const auto tg = std::chrono::steady_clock::now();
             if ((rc = diag_density(d, Fa, d_pk, noccA, tmp, evA, nullptr))) return fail(rc);
             if (uhf && (rc = diag_density(d, Fb, d_pk, noccB, tmp, evB, nullptr))) return fail(rc);
@@ -787,6 +921,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     res->seconds_diag = t_diag;
     res->sp2_steps = sp2_steps;
     res->sp2_fallbacks = sp2_fallbacks;
+    res->pseudo_steps = pseudo_steps;
     res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return UNOMOL_OK;
 }

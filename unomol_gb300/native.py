@@ -303,7 +303,8 @@ class ScfResult(C.Structure):
                 ("densities", C.POINTER(C.c_double)), ("densities_cap", C.c_int), ("guess_used", C.c_int),
                 ("purify_iterations", C.c_int), ("purify_error", C.c_double), ("guess_trace", C.c_double),
                 ("seconds_setup", C.c_double), ("seconds_fock", C.c_double), ("seconds_diis", C.c_double),
-                ("seconds_diag", C.c_double), ("sp2_steps", C.c_int), ("sp2_fallbacks", C.c_int)]
+                ("seconds_diag", C.c_double), ("sp2_steps", C.c_int), ("sp2_fallbacks", C.c_int),
+                ("pseudo_steps", C.c_int)]
 
 
 class BatchScfResult(C.Structure):
@@ -314,6 +315,7 @@ class BatchScfResult(C.Structure):
 
 DENSITY_DIAG = 0
 DENSITY_SP2 = 1
+DENSITY_PSEUDO = 2
 SCF_DAMPED = 0
 SCF_DIIS = 2
 SCF_LOOP_GROUND, SCF_LOOP_DPM = 0, 1
@@ -385,8 +387,10 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
         rebuild_every: int = 8, keep_densities: int = 0, purify: bool = False, loop: int = 0, density: int = 0):
     """SCF on the GPU (unomol_scf).  Returns a dict: energy, init_energy, iterations, converged, P, ...
     purify: start from guess_P after McWeeny purification and a trace check, or from the core
-    Hamiltonian when it fails them (out["guess_used"] says which).  density: DENSITY_DIAG (eigen-solve)
-    or DENSITY_SP2 (second-order spectral projection, eigen-solve where it finds no gap)."""
+    Hamiltonian when it fails them (out["guess_used"] says which).  density: DENSITY_DIAG (eigen-solve),
+    DENSITY_SP2 (second-order spectral projection, eigen-solve where it finds no gap) or DENSITY_PSEUDO
+    (pseudo-diagonalisation steps on the last orbitals, eigen-solve for the first density, large steps
+    and small gaps; out["pseudo_steps"] counts the steps)."""
     L = lib()
     L.unomol_scf.argtypes = [C.c_void_p, C.POINTER(ScfInput), C.POINTER(ScfOptions), C.POINTER(ScfResult),
                              _dp, C.c_void_p]
@@ -422,7 +426,7 @@ def scf(ctx: "TwoElectronInts", b: Basis, S=None, H=None, accel: int = SCF_DAMPE
                                         "seconds", "iterations", "converged", "fock_builds", "fock_ms",
                                         "purify_iterations", "purify_error", "guess_trace", "seconds_setup",
                                         "seconds_fock", "seconds_diis", "seconds_diag", "sp2_steps",
-                                        "sp2_fallbacks")}
+                                        "sp2_fallbacks", "pseudo_steps")}
     out["guess_used"] = GUESS_USED.get(res.guess_used, str(res.guess_used))
     out["P"] = P
     out["orbital_energies"] = eps_orb
