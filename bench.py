@@ -331,6 +331,12 @@ def batch_form(args, dev, stream, flush):
     bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, SKIP_CUTOFF)
     bat.scf(S=S, H=H, maxits=4, incremental=True)  # warm-up of the precision form's capture
     rm = bat.scf(S=S, H=H, incremental=True)
+    # the same SCFs with pseudo-diagonalisation steps after the first two iterations
+    bat.scf(S=S, H=H, maxits=4, incremental=True, density=native.DENSITY_PSEUDO)  # warm-up of its capture
+    rmp = bat.scf(S=S, H=H, incremental=True, density=native.DENSITY_PSEUDO)
+    bat.set_precision(native.PREC_FP64, 0.0, SKIP_CUTOFF)
+    r64p = bat.scf(S=S, H=H, density=native.DENSITY_PSEUDO)
+    bat.set_precision(native.PREC_MIXED, args.fp32_cutoff, SKIP_CUTOFF)
     dE = np.abs(rm["energy"] - r64["energy"])
     rate64 = r64["builds"] / (r64["fock_ms"] / 1e3)
     ratem = rm["builds"] / (rm["fock_ms"] / 1e3)
@@ -357,6 +363,16 @@ def batch_form(args, dev, stream, flush):
                 "scf_converged": int(np.sum(r64["converged"] & rm["converged"])),
                 "scf_wall_s_fp64": r64["seconds"], "scf_wall_s_form": rm["seconds"],
                 "graph_used": bool(r64["graph_used"] and rm["graph_used"]),
+                "scf_pseudo_diag": {"scf_wall_s_fp64": r64p["seconds"], "scf_wall_s_form": rmp["seconds"],
+                                    "speedup_of_form": r64p["seconds"] / rmp["seconds"],
+                                    "builds_fp64": r64p["builds"], "builds_form": rmp["builds"],
+                                    "pseudo_steps_form": rmp["pseudo_steps"], "pseudo_refused_form": rmp["pseudo_refused"],
+                                    "max_abs_dE_vs_fp64_eigen_solve": float(np.abs(rmp["energy"] - r64["energy"]).max()),
+                                    "scf_converged": int(np.sum(r64p["converged"] & rmp["converged"])),
+                                    "graph_used": bool(r64p["graph_used"] and rmp["graph_used"]),
+                                    "note": "density=UNOMOL_DENSITY_PSEUDO: batched eigen-solve for two iterations, then "
+                                            "pseudo-diagonalisation steps (grouped matrix products) where every molecule "
+                                            "passes the step check, the batched eigen-solve where one does not"},
                 "converged_density_builds": {"fp64_ms": conv_rates["fp64"][1], "form_ms": conv_rates["mixed"][1],
                                              "speedup": conv_rates["mixed"][0] / conv_rates["fp64"][0],
                                              "note": "full builds of the FP64 SCF's converged densities, L2 flushed per build"},

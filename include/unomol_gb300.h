@@ -396,8 +396,12 @@ int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* input, const UnomolScfOptio
  * inputs: [nmol] (S, H packed, nelec even); options: maxits, eps, conv_type, accel (UNOMOL_SCF_DIIS:
  * the DIIS update and test of unomol_scf; otherwise the reference's damping and is_converged),
  * guess (core Hamiltonian, or UNOMOL_GUESS_GIVEN: the densities in P_io), loop (ground-state or DPM
- * loop order), diis_size, diis_tol, incremental and rebuild_every.  P_io: the batch's packed densities (in: the guess when given;
- * out: the final densities; may be NULL with the core-Hamiltonian guess). */
+ * loop order), diis_size, diis_tol, incremental, rebuild_every and density (UNOMOL_DENSITY_PSEUDO with
+ * UNOMOL_SCF_DIIS: from the third iteration on, pseudo-diagonalisation steps by grouped matrix products
+ * whenever every active molecule's step passes the check of unomol_scf (rotation at most 0.2, occupied
+ * and virtual levels 1e-3 Eh apart), the batched eigen-solve for all molecules otherwise; other values:
+ * the batched eigen-solve).  P_io: the batch's packed densities (in: the guess when given; out: the
+ * final densities; may be NULL with the core-Hamiltonian guess). */
 typedef struct UnomolBatchScfResult {
     double energy, e_electronic, diis_error;
     int iterations, converged;
@@ -413,6 +417,10 @@ const char* unomol_gpu_batch_scf_last_error(void);
  * (the single-molecule scheme; the build count is kept on the device), so that in the precision form
  * the density bound of each build shrinks as the molecules converge. */
 int unomol_gpu_batch_scf_last_builds(double* fock_ms, int* builds);
+/* Iterations of the last batched SCF on this thread (UNOMOL_DENSITY_PSEUDO) whose densities came from
+ * the pseudo-diagonalisation step (steps) and those where a molecule's check sent every molecule to the
+ * eigen-solve (refused). */
+int unomol_gpu_batch_scf_last_pseudo(int* steps, int* refused);
 
 /* ---- Learned initial density (no reference counterpart; the reference starts from the core
  * Hamiltonian, RHF.hpp:205-211, or reads PMATRIX.DAT, RHF.hpp:120-123) ----

@@ -48,6 +48,8 @@ struct BState {
     double *B = nullptr, *coef = nullptr;  // [nmol][maxv][maxv], [nmol][maxv]
     double *Enew = nullptr, *Eold = nullptr, *err = nullptr, *dE = nullptr, *pdiff = nullptr, *Einit = nullptr;  // [nmol]
     double* Pold = nullptr;               // packed, batch order: the density before the last update's diagonalisation
+    double* Wp = nullptr;                 // pseudo-diagonalisation: every molecule's orbitals (orthonormal basis)
+    int* pbad = nullptr;                  // pseudo-diagonalisation: per molecule (batch order), 1 = step refused
     // incremental builds: the density of the last build, the G kept, the build count (device)
     double *Pprev = nullptr, *Gacc = nullptr;
     int* step = nullptr;
@@ -55,11 +57,13 @@ struct BState {
     cudaEvent_t eb[2] = {nullptr, nullptr};  // around every iteration's Fock build
     double fock_ms = 0.0;
     int builds = 0;
+    int pseudo_steps = 0, pseudo_refused = 0;  // iterations by the pseudo-diagonalisation tail / the eigen-solve tail
     int *nupd = nullptr, *conv = nullptr, *its = nullptr, *info = nullptr, *bad = nullptr;
     // grouped-GEMM pointer arrays (device) per product
-    const double** pa[8] = {};
-    const double** pb[8] = {};
-    double** pc[8] = {};
+    static constexpr int NPROD = 16;
+    const double** pa[NPROD] = {};
+    const double** pb[NPROD] = {};
+    double** pc[NPROD] = {};
     cublasHandle_t cb = nullptr;
     cusolverDnHandle_t cs = nullptr;
     cusolverDnParams_t prm = nullptr;
@@ -73,11 +77,11 @@ struct BState {
     ~BState() {
         for (void* p : std::vector<void*>{d_mols, S, X, H, F, Fo, T1, T2, Pf, Ecur, W, Hpk, Fh, Eh, B, coef, Enew, Eold,
                                           err, dE, pdiff, Einit, Pold, nupd, conv, its, info, bad, dwork, cublas_ws,
-                                          Pprev, Gacc, step})
+                                          Pprev, Gacc, step, Wp, pbad})
             if (p) cudaFree(p);
         for (cudaEvent_t e : eb)
             if (e) cudaEventDestroy(e);
-        for (int k = 0; k < 8; ++k) {
+        for (int k = 0; k < NPROD; ++k) {
             if (pa[k]) cudaFree(pa[k]);
             if (pb[k]) cudaFree(pb[k]);
             if (pc[k]) cudaFree(pc[k]);
@@ -129,6 +133,21 @@ __device__ double block_max(double v) {
     }
     __syncthreads();
     return t;
+}
+
+// the same for values of any sign (block_max's idle lanes hold 0, which suits magnitudes only)
+__device__ double block_max_signed(double v) {
+    __shared__ double ws[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = -1e300;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : -1e300;
+        for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+    }
+    __syncthreads();
+    return t;  // valid in thread 0
 }
 
 // packed (batch order) -> full (group order)
@@ -383,6 +402,54 @@ __global__ void k_inc_post(long long n, double* __restrict__ P, const double* __
 
 __global__ void k_inc_step(int* step) { ++*step; }
 
+// Pseudo-diagonalisation (J. J. P. Stewart, P. Csaszar, P. Pulay, J. Comput. Chem. 3, 227 (1982)), as
+// the single-molecule driver's: in the last orbitals W, F_mo = W^T F' W; A = the antisymmetric generator
+// of the occupied-virtual rotation theta_ai = F_ai / (e_i - e_a) (e the diagonal of F_mo).  bad[m] = 1
+// when an active molecule's step is large (max |theta| > thmax) or its occupied and virtual levels are
+// not separated by gap_min (the occupation of the last orbitals is then no longer the lowest one): the
+// iteration then takes the eigen-solve for every molecule.
+__global__ void k_pseudo_gen(const MolDev* __restrict__ M, const int* __restrict__ conv, const double* __restrict__ Fmo,
+                             double* __restrict__ A, int* __restrict__ bad, double thmax, double gap_min) {
+    const MolDev m = M[blockIdx.x];
+    const int n = m.n, no = m.nocc;
+    const double* F = Fmo + m.o2;
+    double* Am = A + m.o2;
+    double th = 0.0, eo = -1e300, ev = 1e300;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int r = t % n, c = t / n;
+        double v = 0.0;
+        if (r >= no && c < no) {  // theta_rc: r virtual, c occupied
+            v = F[t] / (F[(long long)c * n + c] - F[(long long)r * n + r]);
+            th = fmax(th, fabs(v));
+        } else if (r < no && c >= no) {  // -theta_cr
+            v = -F[(long long)r * n + c] / (F[(long long)r * n + r] - F[(long long)c * n + c]);
+        }
+        Am[t] = v;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double e = F[(long long)i * n + i];
+        if (i < no) eo = fmax(eo, e);
+        else ev = fmin(ev, e);
+    }
+    th = block_max(th);
+    eo = block_max_signed(eo);
+    ev = -block_max_signed(-ev);
+    if (threadIdx.x == 0) {
+        const bool ok = no <= 0 || no >= n || (th <= thmax && ev - eo >= gap_min);  // NaN: not ok
+        bad[m.bidx] = conv[m.bidx] || ok ? 0 : 1;
+    }
+}
+
+// per molecule: Mt = a I + b A + c Mt (A may be null)
+__global__ void k_mident(const MolDev* __restrict__ M, double* __restrict__ Mt, const double* __restrict__ A, double a, double b,
+                         double c) {
+    const MolDev m = M[blockIdx.x];
+    for (int t = threadIdx.x; t < m.n * m.n; t += blockDim.x) {
+        const bool diag = (t % m.n) == (t / m.n);
+        Mt[m.o2 + t] = (diag ? a : 0.0) + (A ? b * A[m.o2 + t] : 0.0) + c * Mt[m.o2 + t];
+    }
+}
+
 // grouped GEMM C = op(A) op(B) for every molecule; pointer arrays were filled once for product `id`
 int gemm(BState& st, int id, cublasOperation_t ta, cublasOperation_t tb, bool k_occ) {
     const int ng = (int)st.gn.size();
@@ -451,15 +518,58 @@ int eig(BState& st, double* A) {
     return UNOMOL_OK;
 }
 
-// F (full) -> P: F' = X^T F X, eigenvectors W, C = X W, P = C_occ C_occ^T, packed into the batch buffer
+// Fo = F' -> P: the eigenvectors of F' (in place), C = X Fo, P = C_occ C_occ^T, packed into the batch
+// buffer (and the eigenvectors kept for the pseudo-diagonalisation steps)
+int density_eig_tail(BState& st, double* dP, cudaStream_t s) {
+    int rc;
+    if ((rc = eig(st, st.Fo))) return rc;
+    if (st.Wp) BK(cudaMemcpyAsync(st.Wp, st.Fo, st.tot2 * sizeof(double), cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
+    if ((rc = gemm(st, 6, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T2 = C = X Fo
+    if ((rc = gemm(st, 7, CUBLAS_OP_N, CUBLAS_OP_T, true))) return rc;   // Pf = C_occ C_occ^T
+    k_pack<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.Pf, dP);
+    BK(cudaGetLastError(), UNOMOL_ECUDA);
+    return UNOMOL_OK;
+}
+
+// F (full) -> P: F' = X^T F X, then the eigen-solve tail
 int density_from_F(BState& st, double* dP, cudaStream_t s) {
     int rc;
     if ((rc = gemm(st, 4, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T1 = F X
     if ((rc = gemm(st, 5, CUBLAS_OP_T, CUBLAS_OP_N, false))) return rc;  // Fo = X^T T1
-    if ((rc = eig(st, st.Fo))) return rc;
-    if ((rc = gemm(st, 6, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T2 = C = X Fo
-    if ((rc = gemm(st, 7, CUBLAS_OP_N, CUBLAS_OP_T, true))) return rc;   // Pf = C_occ C_occ^T
-    k_pack<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.Pf, dP);
+    return density_eig_tail(st, dP, s);
+}
+
+// Pseudo-diagonalisation, first part: F' = X^T F X (Fo), F_mo = Wp^T F' Wp (T2), the rotation generator
+// (T1) and the per-molecule check (st.pbad)
+int pseudo_head(BState& st, cudaStream_t s) {
+    int rc;
+    if ((rc = gemm(st, 4, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T1 = F X
+    if ((rc = gemm(st, 5, CUBLAS_OP_T, CUBLAS_OP_N, false))) return rc;  // Fo = X^T T1
+    if ((rc = gemm(st, 8, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T1 = Fo Wp
+    if ((rc = gemm(st, 9, CUBLAS_OP_T, CUBLAS_OP_N, false))) return rc;  // T2 = Wp^T T1 = F_mo
+    k_pseudo_gen<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.T2, st.T1, st.pbad, 0.2, 1e-3);  // T1 = A
+    BK(cudaGetLastError(), UNOMOL_ECUDA);
+    return UNOMOL_OK;
+}
+
+// Pseudo-diagonalisation, second part: Wp <- Wp (I + A + A^2 / 2), two Newton-Schulz steps
+// W <- W (3 I - W^T W) / 2, then C = X Wp and P = C_occ C_occ^T as the eigen-solve tail
+int pseudo_tail(BState& st, double* dP, cudaStream_t s) {
+    int rc;
+    const unsigned nm = (unsigned)st.nmol;
+    if ((rc = gemm(st, 10, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // T2 = A A
+    k_mident<<<nm, 256, 0, s>>>(st.d_mols, st.T2, st.T1, 1.0, 1.0, 0.5);   // T2 = I + A + A^2 / 2
+    if ((rc = gemm(st, 11, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // Fo = Wp T2
+    if ((rc = gemm(st, 12, CUBLAS_OP_T, CUBLAS_OP_N, false))) return rc;  // T1 = Fo^T Fo
+    k_mident<<<nm, 256, 0, s>>>(st.d_mols, st.T1, nullptr, 1.5, 0.0, -0.5);
+    if ((rc = gemm(st, 13, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // Wp = Fo T1
+    if ((rc = gemm(st, 14, CUBLAS_OP_T, CUBLAS_OP_N, false))) return rc;  // T1 = Wp^T Wp
+    k_mident<<<nm, 256, 0, s>>>(st.d_mols, st.T1, nullptr, 1.5, 0.0, -0.5);
+    if ((rc = gemm(st, 15, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;  // Fo = Wp T1
+    BK(cudaMemcpyAsync(st.Wp, st.Fo, st.tot2 * sizeof(double), cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
+    if ((rc = gemm(st, 6, CUBLAS_OP_N, CUBLAS_OP_N, false))) return rc;   // T2 = C = X Fo
+    if ((rc = gemm(st, 7, CUBLAS_OP_N, CUBLAS_OP_T, true))) return rc;    // Pf = C_occ C_occ^T
+    k_pack<<<nm, 256, 0, s>>>(st.d_mols, st.conv, st.Pf, dP);
     BK(cudaGetLastError(), UNOMOL_ECUDA);
     return UNOMOL_OK;
 }
@@ -470,8 +580,22 @@ struct BOpts {
     int incremental, rebuild;
 };
 
+// Parts of one DIIS-loop iteration with pseudo-diagonalisation: the whole iteration with the eigen-solve
+// (ITER_FULL), or its head up to the pseudo-diagonalisation check (ITER_HEAD) followed, after the host
+// has read the check, by the pseudo-diagonalisation tail (ITER_PSEUDO) or the eigen-solve tail (ITER_EIG).
+enum IterPart { ITER_FULL = 0, ITER_HEAD = 1, ITER_PSEUDO = 2, ITER_EIG = 3 };
+
 // one SCF update of every active molecule (the part that is captured as a graph)
-int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, const BOpts& o, cudaStream_t s) {
+int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, const BOpts& o, cudaStream_t s,
+              int part = ITER_FULL) {
+    int rc;
+    if (part == ITER_PSEUDO || part == ITER_EIG) {  // the tails of a pseudo-diagonalisation iteration (DIIS loop)
+        if ((rc = part == ITER_PSEUDO ? pseudo_tail(st, dP, s) : density_eig_tail(st, dP, s))) return rc;
+        k_converge<<<blocks(st.nmol), 256, 0, s>>>(st.nmol, st.Enew, st.Eold, st.dE, st.Einit, st.nupd, st.conv, st.its, st.err,
+                                                   st.pdiff, o.accel, o.cflag, o.first_check, o.eps, o.tol);
+        BK(cudaGetLastError(), UNOMOL_ECUDA);
+        return UNOMOL_OK;
+    }
     if (o.accel != 2) k_damp<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.nupd, st.dE, o.first_check - 1, st.Pold, dP);
     if (o.incremental) k_inc_pre<<<blocks(st.ptot), 256, 0, s>>>(st.ptot, dP, st.Pprev, st.step, o.rebuild);
     // in a captured iteration the records are external event nodes, timed after every replay
@@ -479,7 +603,7 @@ int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, const BOpt
     BK(cudaStreamIsCapturing(s, &cap), UNOMOL_ECUDA);
     const unsigned evf = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     BK(cudaEventRecordWithFlags(st.eb[0], s, evf), UNOMOL_ECUDA);
-    int rc = unomol_gpu_batch_fock(batch, UNOMOL_BATCH_LAUNCHES, s);
+    rc = unomol_gpu_batch_fock(batch, UNOMOL_BATCH_LAUNCHES, s);
     if (rc) {
         st.err_msg = unomol_gpu_batch_last_error(batch);
         return rc;
@@ -513,6 +637,7 @@ int iteration(BState& st, UnomolBatch* batch, double* dP, double* dG, const BOpt
     k_diis_solve<<<blocks(st.nmol), 256, 0, s>>>(st.nmol, st.conv, st.nupd, st.maxv, st.B, st.coef);
     k_diis_extrap<<<st.nmol, 256, 0, s>>>(st.d_mols, st.conv, st.nupd, st.maxv, st.tot2, st.coef, st.Fh, st.F);
     BK(cudaGetLastError(), UNOMOL_ECUDA);
+    if (part == ITER_HEAD) return pseudo_head(st, s);
     if ((rc = density_from_F(st, dP, s))) return rc;
     k_converge<<<blocks(st.nmol), 256, 0, s>>>(st.nmol, st.Enew, st.Eold, st.dE, st.Einit, st.nupd, st.conv, st.its, st.err,
                                                st.pdiff, o.accel, o.cflag, o.first_check, o.eps, o.tol);
@@ -579,6 +704,12 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     BK(cudaMalloc(&st.coef, sizeof(double) * nmol * st.maxv), UNOMOL_ENOMEM);
     for (double** p : {&st.Enew, &st.Eold, &st.err, &st.dE, &st.pdiff, &st.Einit}) BK(cudaMalloc(p, sizeof(double) * nmol), UNOMOL_ENOMEM);
     BK(cudaMalloc(&st.Pold, sizeof(double) * ptot), UNOMOL_ENOMEM);
+    // pseudo-diagonalisation (DIIS loop only; the damped loop keeps the reference's eigen-solve)
+    const bool pseudo = opt->density == UNOMOL_DENSITY_PSEUDO && opt->accel == UNOMOL_SCF_DIIS;
+    if (pseudo) {
+        BK(cudaMalloc(&st.Wp, b2), UNOMOL_ENOMEM);
+        BK(cudaMalloc(&st.pbad, sizeof(int) * nmol), UNOMOL_ENOMEM);
+    }
     st.ptot = ptot;
     if (opt->incremental) {
         BK(cudaMalloc(&st.Pprev, sizeof(double) * ptot), UNOMOL_ENOMEM);
@@ -648,6 +779,11 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         (rc = set_ptrs(st, 4, st.F, st.X, st.T1)) || (rc = set_ptrs(st, 5, st.X, st.T1, st.Fo)) ||
         (rc = set_ptrs(st, 6, st.X, st.Fo, st.T2)) || (rc = set_ptrs(st, 7, st.T2, st.T2, st.Pf)))
         return fail(rc);
+    if (pseudo && ((rc = set_ptrs(st, 8, st.Fo, st.Wp, st.T1)) || (rc = set_ptrs(st, 9, st.Wp, st.T1, st.T2)) ||
+                   (rc = set_ptrs(st, 10, st.T1, st.T1, st.T2)) || (rc = set_ptrs(st, 11, st.Wp, st.T2, st.Fo)) ||
+                   (rc = set_ptrs(st, 12, st.Fo, st.Fo, st.T1)) || (rc = set_ptrs(st, 13, st.Fo, st.T1, st.Wp)) ||
+                   (rc = set_ptrs(st, 14, st.Wp, st.Wp, st.T1)) || (rc = set_ptrs(st, 15, st.Wp, st.T1, st.Fo))))
+        return fail(rc);
     // X from S (canonical, RHF.hpp:214-233)
     BK(cudaMemcpyAsync(st.X, st.S, b2, cudaMemcpyDeviceToDevice, s), UNOMOL_ECUDA);
     if ((rc = eig(st, st.X))) return fail(rc);
@@ -679,29 +815,57 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
     const int maxits = opt->maxits > 0 ? opt->maxits : 300;
     const BOpts o{opt->accel == UNOMOL_SCF_DIIS ? 2 : 0, opt->conv_type, opt->loop == UNOMOL_SCF_LOOP_DPM ? 2 : 3, opt->eps,
                   opt->diis_tol, opt->incremental ? 1 : 0, opt->rebuild_every > 0 ? opt->rebuild_every : 8};
-    cudaGraphExec_t exec = nullptr;
+    // the eigen-solve for the first PSEUDO_AFTER iterations, then pseudo-diagonalisation steps where every
+    // active molecule passes the check, the eigen-solve tail where one does not
+    constexpr int PSEUDO_AFTER = 2;
+    const int nparts = pseudo ? 4 : 1;
+    cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
+    struct ExecGuard {
+        cudaGraphExec_t* e;
+        ~ExecGuard() { for (int k = 0; k < 4; ++k) if (e[k]) cudaGraphExecDestroy(e[k]); }
+    } eg{exec};
     int used_graph = 0;
     if (graph) {
-        // capture one iteration; a library call that cannot be captured leaves plain launches
-        cudaGraph_t gr = nullptr;
-        BK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), UNOMOL_ECUDA);
-        rc = iteration(st, batch, dP, dG, o, s);
-        const cudaError_t e = cudaStreamEndCapture(s, &gr);
-        if (!rc && e == cudaSuccess && gr && cudaGraphInstantiate(&exec, gr, 0) == cudaSuccess) used_graph = 1;
-        if (gr) cudaGraphDestroy(gr);
-        cudaGetLastError();
+        // capture one iteration (and its parts with pseudo-diagonalisation); a library call that cannot be
+        // captured leaves plain launches
+        used_graph = 1;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < nparts && used_graph; ++k) {
+            cudaGraph_t gr = nullptr;
+            BK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), UNOMOL_ECUDA);
+            rc = iteration(st, batch, dP, dG, o, s, k);
+            e = cudaStreamEndCapture(s, &gr);
+            if (rc || e != cudaSuccess || !gr || cudaGraphInstantiate(&exec[k], gr, 0) != cudaSuccess) used_graph = 0;
+            if (gr) cudaGraphDestroy(gr);
+            cudaGetLastError();
+        }
         if (!used_graph) {
-            if (exec) cudaGraphExecDestroy(exec), exec = nullptr;
+            for (int k = 0; k < 4; ++k)
+                if (exec[k]) cudaGraphExecDestroy(exec[k]), exec[k] = nullptr;
             st.capture_error = st.err_msg.empty() ? std::string(cudaGetErrorString(e)) : st.err_msg;
             st.err_msg.clear();
             BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
         }
     }
     if (graph_used) *graph_used = used_graph;
-    std::vector<int> conv(nmol);
+    auto run = [&](int part) -> int {
+        if (used_graph) BK(cudaGraphLaunch(exec[part], s), UNOMOL_ECUDA);
+        else return iteration(st, batch, dP, dG, o, s, part);
+        return UNOMOL_OK;
+    };
+    std::vector<int> conv(nmol), pbad(pseudo ? nmol : 0);
     for (int it = 0; it < maxits; ++it) {
-        if (used_graph) BK(cudaGraphLaunch(exec, s), UNOMOL_ECUDA);
-        else if ((rc = iteration(st, batch, dP, dG, o, s))) return fail(rc);
+        if (!pseudo || it < PSEUDO_AFTER) {
+            if ((rc = run(ITER_FULL))) return fail(rc);
+        } else {
+            if ((rc = run(ITER_HEAD))) return fail(rc);
+            BK(cudaMemcpyAsync(pbad.data(), st.pbad, sizeof(int) * nmol, cudaMemcpyDeviceToHost, s), UNOMOL_ECUDA);
+            BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
+            const bool refuse = std::any_of(pbad.begin(), pbad.end(), [](int b) { return b != 0; });
+            if ((rc = run(refuse ? ITER_EIG : ITER_PSEUDO))) return fail(rc);
+            if (refuse) ++st.pseudo_refused;
+            else ++st.pseudo_steps;
+        }
         BK(cudaMemcpyAsync(conv.data(), st.conv, sizeof(int) * nmol, cudaMemcpyDeviceToHost, s), UNOMOL_ECUDA);
         BK(cudaStreamSynchronize(s), UNOMOL_ECUDA);
         float ms = 0.f;
@@ -709,7 +873,6 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
         ++st.builds;
         if (std::all_of(conv.begin(), conv.end(), [](int c) { return c != 0; })) break;
     }
-    if (exec) cudaGraphExecDestroy(exec);
     std::vector<double> E(nmol), err(nmol), E1(nmol), pd(nmol), de(nmol);
     BK(cudaMemcpy(E1.data(), st.Einit, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
     BK(cudaMemcpy(pd.data(), st.pdiff, sizeof(double) * nmol, cudaMemcpyDeviceToHost), UNOMOL_ECUDA);
@@ -743,6 +906,7 @@ int batch_scf(BState& st, UnomolBatch* batch, const UnomolScfInput* in, int nmol
 
 thread_local double g_bscf_fock_ms = 0.0;
 thread_local int g_bscf_builds = 0;
+thread_local int g_bscf_pseudo[2] = {0, 0};
 
 extern "C" int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* in, int nmol, const UnomolScfOptions* opt,
                                     int graph, UnomolBatchScfResult* res, double* P_out, double* seconds, int* graph_used) {
@@ -756,6 +920,8 @@ extern "C" int unomol_gpu_batch_scf(UnomolBatch* batch, const UnomolScfInput* in
         g_bscf_err = rc ? st.err_msg : st.capture_error;
         g_bscf_fock_ms = st.fock_ms;
         g_bscf_builds = st.builds;
+        g_bscf_pseudo[0] = st.pseudo_steps;
+        g_bscf_pseudo[1] = st.pseudo_refused;
     }
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;
@@ -767,5 +933,12 @@ extern "C" int unomol_gpu_batch_scf_last_builds(double* fock_ms, int* builds) {
     if (!fock_ms || !builds) return UNOMOL_EINVAL;
     *fock_ms = g_bscf_fock_ms;
     *builds = g_bscf_builds;
+    return UNOMOL_OK;
+}
+
+extern "C" int unomol_gpu_batch_scf_last_pseudo(int* steps, int* refused) {
+    if (!steps || !refused) return UNOMOL_EINVAL;
+    *steps = g_bscf_pseudo[0];
+    *refused = g_bscf_pseudo[1];
     return UNOMOL_OK;
 }

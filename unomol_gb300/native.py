@@ -36,6 +36,7 @@ EXPORTS = [
     "unomol_gpu_batch_scf_last_error", "unomol_gpu_batch_size", "unomol_gpu_gdpm", "unomol_gpu_gdpm_last_error",
     "unomol_gpu_moment_ints", "unomol_gpu_batch_set_precision", "unomol_gpu_batch_fock_device",
     "unomol_tc_set_wait_polls", "unomol_gpu_set_launch_order", "unomol_gpu_batch_scf_last_builds",
+    "unomol_gpu_batch_scf_last_pseudo",
     "unomol_gpu_store_integrals", "unomol_gpu_store_records", "unomol_gpu_drop_store", "unomol_gpu_store_info",
     "unomol_gpu_write_records",
 ]
@@ -511,10 +512,13 @@ class Batch:
 
     def scf(self, S=None, H=None, eps: float = 1e-10, diis_tol: float = 1e-6, maxits: int = 200,
             diis_size: int = 8, graph: bool = True, accel: int = SCF_DIIS, conv_type: int = 0, guess_P=None,
-            loop: int = SCF_LOOP_GROUND, incremental: bool = False, rebuild_every: int = 8):
+            loop: int = SCF_LOOP_GROUND, incremental: bool = False, rebuild_every: int = 8, density: int = 0):
         """RHF SCF of every molecule at once (unomol_gpu_batch_scf).  S, H: lists of packed matrices
         (default: the GPU one-electron integrals of each basis); guess_P: list of packed starting
-        densities (default: core Hamiltonian); accel / conv_type / loop as for scf().  Returns a dict
+        densities (default: core Hamiltonian); accel / conv_type / loop as for scf(); density:
+        DENSITY_DIAG, or DENSITY_PSEUDO (DIIS loop: pseudo-diagonalisation steps after the first two
+        iterations where every active molecule passes the step check, else the eigen-solve; the counts
+        come back as pseudo_steps / pseudo_refused).  Returns a dict
         with per-molecule energies, iterations and convergence, the packed densities, the wall time
         and whether the iteration ran as a CUDA graph."""
         L = lib()
@@ -531,7 +535,7 @@ class Batch:
         inp = (ScfInput * n)(*[ScfInput(b.norb, b.nelec, b.nuclear_repulsion(), s.ctypes.data_as(dp), h.ctypes.data_as(dp))
                                for b, s, h in zip(self.bases, S, H)])
         opt = ScfOptions(maxits, eps, conv_type, accel, GUESS_CORE if guess_P is None else GUESS_GIVEN, diis_size,
-                         diis_tol, 0.0, 0.0, 0.0, 1 if incremental else 0, rebuild_every, loop)
+                         diis_tol, 0.0, 0.0, 0.0, 1 if incremental else 0, rebuild_every, loop, density)
         res = (BatchScfResult * n)()
         P = np.zeros(self.total)
         if guess_P is not None:
@@ -544,7 +548,10 @@ class Batch:
         L.unomol_gpu_batch_scf_last_builds.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int)]
         fms, nb = C.c_double(), C.c_int()
         L.unomol_gpu_batch_scf_last_builds(C.byref(fms), C.byref(nb))
-        return {"fock_ms": fms.value, "builds": nb.value,"energy": np.array([r.energy for r in res]), "iterations": np.array([r.iterations for r in res]),
+        L.unomol_gpu_batch_scf_last_pseudo.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        ps, pr = C.c_int(), C.c_int()
+        L.unomol_gpu_batch_scf_last_pseudo(C.byref(ps), C.byref(pr))
+        return {"fock_ms": fms.value, "builds": nb.value, "pseudo_steps": ps.value, "pseudo_refused": pr.value,"energy": np.array([r.energy for r in res]), "iterations": np.array([r.iterations for r in res]),
                 "init_energy": np.array([r.init_energy for r in res]), "ediff": np.array([r.ediff for r in res]),
                 "pdiff": np.array([r.pdiff for r in res]),
                 "converged": np.array([bool(r.converged) for r in res]),
