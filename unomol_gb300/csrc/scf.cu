@@ -449,24 +449,30 @@ int pseudo_density(Dev& d, double* Ws, const std::vector<double>& Fpk, double* d
 struct Diis {
     int maxv = 8;
     std::vector<std::vector<double>> F, E;
+    std::vector<std::vector<double>> gram;  // gram[i][j] = E_i . E_j (j <= i), one new row per push
     void push(const std::vector<double>& f, const std::vector<double>& e) {
         if ((int)F.size() == maxv) {
             F.erase(F.begin());
             E.erase(E.begin());
+            gram.erase(gram.begin());
+            for (auto& row : gram) row.erase(row.begin());
         }
         F.push_back(f);
         E.push_back(e);
+        std::vector<double> row(E.size());
+        for (size_t j = 0; j < E.size(); ++j) {
+            double s = 0.0;
+            for (size_t k = 0; k < e.size(); ++k) s += e[k] * E[j][k];
+            row[j] = s;
+        }
+        gram.push_back(std::move(row));
     }
     bool extrapolate(std::vector<double>& out) {
         const int m = (int)F.size();
         if (m < 2) return false;
         std::vector<double> B((m + 1) * (m + 1), 0.0), rhs(m + 1, 0.0);
         for (int i = 0; i < m; ++i)
-            for (int j = 0; j <= i; ++j) {
-                double s = 0.0;
-                for (size_t k = 0; k < E[i].size(); ++k) s += E[i][k] * E[j][k];
-                B[i * (m + 1) + j] = B[j * (m + 1) + i] = s;
-            }
+            for (int j = 0; j <= i; ++j) B[i * (m + 1) + j] = B[j * (m + 1) + i] = gram[i][j];
         for (int i = 0; i < m; ++i) B[i * (m + 1) + m] = B[m * (m + 1) + i] = -1.0;
         rhs[m] = -1.0;
         // Gaussian elimination with partial pivoting
