@@ -341,37 +341,48 @@ int sp2_density(Dev& d, const std::vector<double>& Fpk, double* d_pk, int nocc, 
 
 // ---- Density by pseudo-diagonalisation (J. J. P. Stewart, P. Csaszar, P. Pulay, J. Comput. Chem. 3,
 // 227 (1982)), in place of the eigen-solve once the orbitals change little ----
-// W holds the orbitals of the last step in the orthonormal basis (columns; the nocc occupied first).
-// In those orbitals F_mo = W^T X^T F X W is nearly diagonal; its occupied-virtual block is rotated away
-// to first order, theta_ai = F_ai / (e_i - e_a) with e the diagonal of F_mo, by W <- W exp(A) (A the
-// antisymmetric generator, exp to second order, then Newton-Schulz re-orthonormalisation), all by
-// matrix products.  At self-consistency F_ai -> 0, so the density converges to the projector of F; a
-// step whose rotation is large or whose occupied and virtual levels come close takes the eigen-solve.
+// C holds the orbitals of the last step (AO coefficients, columns, C^T S C = I; the nocc occupied first).
+// In those orbitals F_mo = C^T F C is nearly diagonal; its occupied-virtual block is rotated away to
+// first order, theta_ai = F_ai / (e_i - e_a) with e the diagonal of F_mo, by the rotation exp(A) of the
+// antisymmetric generator A = [[0, -theta^T], [theta, 0]] taken to second order block by block,
+//   C_o <- C_o + C_v theta - C_o (theta^T theta) / 2,   C_v <- C_v - C_o theta^T - C_v (theta theta^T) / 2,
+// then re-orthonormalised in the S metric by Newton-Schulz, C <- C (3 I - C^T S C) / 2.  At
+// self-consistency F_ai -> 0, so the density converges to the projector of F; a step whose rotation is
+// large or whose occupied and virtual levels come close takes the eigen-solve.
 constexpr double PSEUDO_MAX_THETA = 0.2;  // largest |theta| of a step (else the eigen-solve)
 constexpr double PSEUDO_MIN_GAP = 1e-3;   // smallest e_a - e_i (Eh) of a step (else the eigen-solve)
 
-// A (n x n, column-major) = the generator of the occupied-virtual rotation of Fmo; st[0] = max |theta|,
+// e[j] = sum_k A[k, j] B[k, j] (column-major n x n; one block per column)
+__global__ void k_coldot(const double* __restrict__ A, const double* __restrict__ B, int n, double* __restrict__ e) {
+    __shared__ double s_[128];
+    const size_t c = (size_t)blockIdx.x * n;
+    double v = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) v = fma(A[c + k], B[c + k], v);
+    s_[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s_[threadIdx.x] += s_[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) e[blockIdx.x] = s_[0];
+}
+
+// theta (nv x nocc, column-major, in place over F_vo) = F_ai / (e_i - e_a); st[0] = max |theta|,
 // st[1] = min e_virtual - max e_occupied (one block)
-__global__ void k_pseudo_gen(const double* __restrict__ Fmo, int n, int nocc, double* __restrict__ A, double* __restrict__ st) {
+__global__ void k_pseudo_theta(double* __restrict__ th, const double* __restrict__ e, int nocc, int nv, double* __restrict__ st) {
     __shared__ double s_th[256], s_eo[256], s_ev[256];
-    double th = 0.0, eo = -1e300, ev = 1e300;
-    for (long long t = threadIdx.x; t < (long long)n * n; t += blockDim.x) {
-        const int r = (int)(t % n), c = (int)(t / n);
-        double v = 0.0;
-        if (r >= nocc && c < nocc) {  // theta_rc, r virtual, c occupied
-            v = Fmo[t] / (Fmo[(size_t)c * n + c] - Fmo[(size_t)r * n + r]);
-            th = fmax(th, fabs(v));
-        } else if (r < nocc && c >= nocc) {
-            v = -Fmo[(size_t)r * n + c] / (Fmo[(size_t)r * n + r] - Fmo[(size_t)c * n + c]);
-        }
-        A[t] = v;
+    double t = 0.0, eo = -1e300, ev = 1e300;
+    for (long long q = threadIdx.x; q < (long long)nv * nocc; q += blockDim.x) {
+        const int a = (int)(q % nv), i = (int)(q / nv);
+        const double v = th[q] / (e[i] - e[nocc + a]);
+        th[q] = v;
+        t = fmax(t, fabs(v));
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double e = Fmo[(size_t)i * n + i];
-        if (i < nocc) eo = fmax(eo, e);
-        else ev = fmin(ev, e);
+    for (int k = threadIdx.x; k < nocc + nv; k += blockDim.x) {
+        if (k < nocc) eo = fmax(eo, e[k]);
+        else ev = fmin(ev, e[k]);
     }
-    s_th[threadIdx.x] = th;
+    s_th[threadIdx.x] = t;
     s_eo[threadIdx.x] = eo;
     s_ev[threadIdx.x] = ev;
     __syncthreads();
@@ -389,55 +400,66 @@ __global__ void k_pseudo_gen(const double* __restrict__ Fmo, int n, int nocc, do
     }
 }
 
-// M = a I + b A + c M, in place on M (column-major n x n)
-__global__ void k_axpy_ident(double* __restrict__ M, const double* __restrict__ A, int n, double a, double b, double c) {
+// M = a I + c M, in place (column-major n x n)
+__global__ void k_scale_ident(double* __restrict__ M, int n, double a, double c) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n * n) return;
-    const bool diag = (t % n) == (t / n);
-    M[t] = (diag ? a : 0.0) + (A ? b * A[t] : 0.0) + c * M[t];
+    M[t] = ((t % n) == (t / n) ? a : 0.0) + c * M[t];
 }
 
-// F (packed, host) -> P packed (host) by one pseudo-diagonalisation step on the orbitals Ws (updated in
-// place); ok = false (P and Ws untouched) when the step is too large or the gap too small: the caller
+// F (packed, host) -> P packed (host) by one pseudo-diagonalisation step on the orbitals Cs (updated in
+// place); ok = false (P and Cs untouched) when the step is too large or the gap too small: the caller
 // then takes the eigen-solve.
-int pseudo_density(Dev& d, double* Ws, const std::vector<double>& Fpk, double* d_pk, int nocc, std::vector<double>& P,
-                   bool& ok) {
-    const int n = d.n;
-    const double one = 1.0, zero = 0.0;
+int pseudo_density(Dev& d, double* Cs, const double* d_S, const std::vector<double>& Fpk, double* d_pk, int nocc,
+                   std::vector<double>& P, bool& ok) {
+    const int n = d.n, nv = n - nocc;
+    const double one = 1.0, zero = 0.0, mone = -1.0, mhalf = -0.5;
     ok = false;
-    if (nocc <= 0 || nocc >= n || d.lwork < 48) return UNOMOL_OK;
+    if (nocc <= 0 || nv <= 0 || d.lwork < 48) return UNOMOL_OK;
     double* st = d.work + 32;  // the eigen-solver workspace is free here
     const unsigned nb = blocks((long long)n * n);
+    double *FC = d.T1, *th = d.C, *Goo = d.F, *Gvv = d.F + (size_t)nocc * nocc, *Cn = d.W;
     CK(cudaMemcpyAsync(d_pk, Fpk.data(), Fpk.size() * sizeof(double), cudaMemcpyHostToDevice, d.s), UNOMOL_ECUDA);
     k_unpack<<<nb, 256, 0, d.s>>>(d_pk, d.F, n);
-    // F' = X^T F X (C), F_mo = Ws^T F' Ws (F)
-    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.F, n, d.X, n, &zero, d.T1, n), UNOMOL_ECUDA);
-    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, d.X, n, d.T1, n, &zero, d.C, n), UNOMOL_ECUDA);
-    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.C, n, Ws, n, &zero, d.T1, n), UNOMOL_ECUDA);
-    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, Ws, n, d.T1, n, &zero, d.F, n), UNOMOL_ECUDA);
-    k_pseudo_gen<<<1, 256, 0, d.s>>>(d.F, n, nocc, d.T1, st);
+    // FC = F Cs; e = diag(Cs^T F Cs); F_vo = Cs_v^T FC_o -> theta
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.F, n, Cs, n, &zero, FC, n), UNOMOL_ECUDA);
+    k_coldot<<<n, 128, 0, d.s>>>(Cs, FC, n, d.ev);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, nv, nocc, n, &one, Cs + (size_t)nocc * n, n, FC, n, &zero, th, nv),
+       UNOMOL_ECUDA);
+    k_pseudo_theta<<<1, 256, 0, d.s>>>(th, d.ev, nocc, nv, st);
     double h[2] = {0.0, 0.0};
     CK(cudaMemcpyAsync(h, st, sizeof(h), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
     CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
     if (!(h[0] <= PSEUDO_MAX_THETA && h[1] >= PSEUDO_MIN_GAP)) return UNOMOL_OK;
-    // M = I + A + A^2 / 2 (W), C = Ws M
-    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.T1, n, d.T1, n, &zero, d.W, n), UNOMOL_ECUDA);
-    k_axpy_ident<<<nb, 256, 0, d.s>>>(d.W, d.T1, n, 1.0, 1.0, 0.5);
-    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, Ws, n, d.W, n, &zero, d.C, n), UNOMOL_ECUDA);
-    // Newton-Schulz: Ws = C (3 I - C^T C) / 2; C^T C = I + O(theta^3), twice for the larger steps
+    // the rotation, block by block, into Cn (second-order terms only where they reach 1e-6)
+    const bool second = h[0] > 1e-3;
+    double* Co = Cs;
+    double* Cv = Cs + (size_t)nocc * n;
+    CK(cudaMemcpyAsync(Cn, Cs, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, d.s), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, nocc, nv, &one, Cv, n, th, nv, &one, Cn, n), UNOMOL_ECUDA);
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, nv, nocc, &mone, Co, n, th, nv, &one, Cn + (size_t)nocc * n, n),
+       UNOMOL_ECUDA);
+    if (second) {
+        CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, nocc, nocc, nv, &one, th, nv, th, nv, &zero, Goo, nocc), UNOMOL_ECUDA);
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, nv, nv, nocc, &one, th, nv, th, nv, &zero, Gvv, nv), UNOMOL_ECUDA);
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, nocc, nocc, &mhalf, Co, n, Goo, nocc, &one, Cn, n), UNOMOL_ECUDA);
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, nv, nv, &mhalf, Cv, n, Gvv, nv, &one, Cn + (size_t)nocc * n, n),
+           UNOMOL_ECUDA);
+    }
+    // Newton-Schulz in the S metric: C <- C (3 I - C^T S C) / 2, twice for the larger steps; the result in Cs
     const int ns = h[0] > 1e-2 ? 2 : 1;
     for (int k = 0; k < ns; ++k) {
-        double* src = k == 0 ? d.C : Ws;
-        double* dst = k == 0 ? Ws : d.C;
-        CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, src, n, src, n, &zero, d.W, n), UNOMOL_ECUDA);
-        k_axpy_ident<<<nb, 256, 0, d.s>>>(d.W, nullptr, n, 1.5, 0.0, -0.5);
-        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, src, n, d.W, n, &zero, dst, n), UNOMOL_ECUDA);
+        double* src = k == 0 ? Cn : Cs;
+        double* dst = k == 0 ? Cs : Cn;
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d_S, n, src, n, &zero, FC, n), UNOMOL_ECUDA);
+        CK(cublasDgemm(d.cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, src, n, FC, n, &zero, d.C, n), UNOMOL_ECUDA);
+        k_scale_ident<<<nb, 256, 0, d.s>>>(d.C, n, 1.5, -0.5);
+        CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, src, n, d.C, n, &zero, dst, n), UNOMOL_ECUDA);
     }
-    if (ns == 2) CK(cudaMemcpyAsync(Ws, d.C, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, d.s), UNOMOL_ECUDA);
-    // C = X Ws, P = C_occ C_occ^T
-    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, d.X, n, Ws, n, &zero, d.C, n), UNOMOL_ECUDA);
-    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &one, d.C, n, d.C, n, &zero, d.T1, n), UNOMOL_ECUDA);
-    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(d.T1, d_pk, n);
+    if (ns == 2) CK(cudaMemcpyAsync(Cs, Cn, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, d.s), UNOMOL_ECUDA);
+    // P = C_occ C_occ^T
+    CK(cublasDgemm(d.cb, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &one, Cs, n, Cs, n, &zero, FC, n), UNOMOL_ECUDA);
+    k_pack<<<blocks((long long)n * (n + 1) / 2), 256, 0, d.s>>>(FC, d_pk, n);
     P.resize((size_t)n * (n + 1) / 2);
     CK(cudaMemcpyAsync(P.data(), d_pk, P.size() * sizeof(double), cudaMemcpyDeviceToHost, d.s), UNOMOL_ECUDA);
     CK(cudaStreamSynchronize(d.s), UNOMOL_ECUDA);
@@ -634,7 +656,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
     } sg{s};
     int rc = dev_init(d, n, s);
     double *d_pk = nullptr, *d_P = nullptr, *d_G = nullptr, *d_Pb = nullptr, *d_Gb = nullptr, *d_S = nullptr;
-    double* d_Ws[2] = {nullptr, nullptr};  // pseudo-diagonalisation: the orbitals of each spin (orthonormal basis)
+    double* d_Ws[2] = {nullptr, nullptr};  // pseudo-diagonalisation: the orbitals of each spin (AO coefficients)
     struct Bufs {
         double** p[8];
         ~Bufs() { for (auto q : p) if (*q) cudaFree(*q); }
@@ -826,7 +848,7 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
             }
             if (pseudo && have_orbitals[spin]) {
                 bool ok = false;
-                const int rr = pseudo_density(d, d_Ws[spin], F, d_pk, nocc, P, ok);
+                const int rr = pseudo_density(d, d_Ws[spin], d_S, F, d_pk, nocc, P, ok);
                 if (rr) return rr;
                 if (ok) {
                     ++pseudo_steps;
@@ -834,8 +856,8 @@ extern "C" int unomol_scf(UnomolCtx* ctx, const UnomolScfInput* in, const Unomol
                 }
             }
             const int rr = diag_density(d, F, d_pk, nocc, P, ev, nullptr);
-            if (!rr && pseudo) {  // the eigenvectors (orthonormal basis) start the next pseudo step
-                if (cudaMemcpyAsync(d_Ws[spin], d.W, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            if (!rr && pseudo) {  // the orbitals C = X W start the next pseudo step
+                if (cudaMemcpyAsync(d_Ws[spin], d.C, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
                     d.err = "orbital copy failed";
                     return UNOMOL_ECUDA;
                 }
