@@ -207,3 +207,31 @@ def test_record_layout_is_the_reference_twoints():
     assert [native.RECORD_DTYPE.fields[k][1] for k in ("val", "i", "j", "k", "l")] == [0, 8, 12, 16, 20]
     txt = open(os.path.join(ROOT, "include", "unomol_gb300.h")).read()
     assert "double val;\n    int32_t i, j, k, l;\n} UnomolRecord;" in txt
+
+
+def test_python_structures_match_the_c_header(tmp_path):
+    """Every ctypes mirror of a structure of include/unomol_gb300.h has the C layout: the same size and the
+    same offset for every field, as gcc lays out the header (the C ABI the bindings call through)."""
+    import ctypes
+    import subprocess
+    from unomol_gb300 import learned, native
+    structs = {"UnomolBasisDesc": native.BasisDesc, "UnomolStats": native.Stats, "UnomolStoreInfo": native.StoreInfo,
+               "UnomolScfInput": native.ScfInput, "UnomolScfOptions": native.ScfOptions,
+               "UnomolScfResult": native.ScfResult, "UnomolBatchScfResult": native.BatchScfResult,
+               "UnomolGuessConfig": learned.GuessConfig, "UnomolGuessTrainOptions": learned.TrainOptions}
+    src = ["#include <stdio.h>", "#include <stddef.h>", '#include "unomol_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        src.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            src.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    src += ["return 0;", "}"]
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                      text=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
