@@ -8,7 +8,9 @@
 // accelerator, its damping (RHF.hpp:536-569) and convergence tests.  With `graph` set the whole iteration is
 // captured once as a CUDA graph and replayed; the host reads only the per-molecule convergence flags
 // after each replay.  A molecule that has converged is frozen (its P and energy stop changing) while
-// the others go on.
+// the others go on.  With UNOMOL_DENSITY_PSEUDO (DIIS loop) the iterations after the second replace the
+// batched eigen-solve by a pseudo-diagonalisation step (grouped matrix products) whenever every active
+// molecule passes its step check; the host reads the check between the iteration's head and its tail.
 //
 // Layout: molecules are grouped by (nbf, nocc); full N x N matrices (column major, symmetric) of a
 // group are contiguous with stride N^2 so that each group is one batched eigen-solve and one entry of
