@@ -7,7 +7,9 @@
 // `extrap` stays 0, so only the averaging runs), is_converged() on the signed ediff and/or pdiff
 // (RHF.hpp:390-402), canonical X = U s^{-1/2} (RHF.hpp:214-233) and the core-Hamiltonian guess
 // (RHF.hpp:205-211).  DIIS (accel 2) is new: Pulay extrapolation of F on the orthonormal-basis error
-// X^T (F P S - S P F) X, for systems on which the damped loop oscillates.
+// X^T (F P S - S P F) X, for systems on which the damped loop oscillates.  Two new ways to the density
+// of F beside the eigen-solve: second-order spectral projection (SP2) and pseudo-diagonalisation steps
+// on the last orbitals (both fall back to the eigen-solve where their conditions fail).
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
